@@ -1,0 +1,426 @@
+#!/usr/bin/env python
+"""Benchmark of the LuxRays intersection path on GB300.
+
+Workload (one "step"): the fBm heightfield scene -- a 1024x1024 vertex grid
+over [0,1]^2, 2,093,058 FP32 triangles, heights from seeded 6-octave value
+noise scaled to [0, 0.2] -- traced with three ray sets:
+  1,048,576 pinhole primary rays (eye (0.5,-0.5,0.6), look-at (0.5,0.5,0),
+            vertical fov 60 deg), closest hit;
+  1,048,576 cosine-hemisphere bounce rays from the primary hit points,
+            closest hit;
+  4,194,304 shadow rays from the bounce origins to 4 point lights in
+            [0,1]^2 x [0.5,1], any hit.
+All inputs are seeded synthetic data (no public scene is named for this
+path).  Rays (302 MB) and hits (126 MB) exceed the 129 MB L2, so no flush is
+needed between steps.
+
+--impl lrx (default): the CUDA engine through liblrx.so.
+--impl reference: the reference's CPU accelerator on the host cores (the
+  oracle's restatement of BVHAccel::Intersect, all host threads).
+Multi-GPU (torchrun): ray batches are independent, so each rank traces its
+own copy of the workload on its own scene replica (weak scaling, no
+collective on the data path); rank 0 prints the aggregate.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from luxcore_gb300 import workloads as W  # noqa: E402
+
+METRIC = "Mrays/s closest/any-hit (1 GB300, % HBM roofline); served p50/p99 vs plain launch"
+UNIT = "Mrays/s"
+WORKLOAD = "heightfield-2093058tri: 1048576 primary + 1048576 bounce (closest) + 4194304 shadow (any-hit)"
+HEIGHTFIELD_RES = 1024
+SHADOW_LIGHTS = 4
+NODE_BYTES, TRI_BYTES, INST_BYTES, RAY_BYTES, HIT_BYTES = 80, 48, 80, 48, 20
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ---------------------------------------------------------------------------
+# distributed helpers (torchrun)
+# ---------------------------------------------------------------------------
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    def __init__(self, use_gpu: bool):
+        self.ws, self.rank, self.local = dist_env()
+        self.pg = None
+        if self.ws > 1:
+            import torch
+            import torch.distributed as dist
+            if use_gpu:
+                torch.cuda.set_device(self.local)
+            dist.init_process_group("nccl" if use_gpu else "gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64, device="cuda" if self.pg.get_backend() == "nccl" else "cpu")
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    """nvidia-smi sampled every 200 ms during the timed region."""
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+
+def make_scene():
+    return W.SceneDesc([W.heightfield_mesh(HEIGHTFIELD_RES, W.BASE_SEED + 1)])
+
+
+def derived_rays(scene, primary, primary_hits, seed):
+    bounce = W.bounce_rays(scene, primary, primary_hits, 1 << 20, seed)
+    shadow = W.shadow_rays(bounce, SHADOW_LIGHTS, seed + 1)
+    return bounce, shadow
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic_per_ray():
+    """DRAM bytes per ray of the traversal kernel from the committed ncu
+    summary (profiles/trace_heightfield_ncu.md, line `dram_bytes_per_ray:`)."""
+    p = os.path.join(ROOT, "profiles", "trace_heightfield_ncu.md")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        for ln in f:
+            if ln.strip().startswith("dram_bytes_per_ray:"):
+                try:
+                    return float(ln.split(":", 1)[1].split()[0])
+                except ValueError:
+                    return None
+    return None
+
+
+# ---------------------------------------------------------------------------
+# CPU arm (the reference's CPU accelerator, restated)
+# ---------------------------------------------------------------------------
+
+def cpu_measure(scene, sets, threads: int):
+    """Times the oracle's BVHAccel::Intersect over the given ray sets."""
+    from oracle import pyoracle as po
+    o = po.OracleScene(scene, po.ACCEL_BVH)
+    total, secs = 0, 0.0
+    for rays in sets:
+        _, s = o.intersect(rays, n_threads=threads)
+        secs += s
+        total += rays.shape[0]
+    return total, secs
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    from oracle import pyoracle as po
+    scene = make_scene()
+    primary = W.pinhole_rays(1024, 1024)
+    o = po.OracleScene(scene, po.ACCEL_BVH)
+    ph, _ = o.intersect(primary, n_threads=threads)
+    bounce, shadow = derived_rays(scene, primary, ph, W.BASE_SEED + 100)
+    frac = args.ref_fraction
+    sample = [primary[::frac], bounce[::frac], shadow[::frac]]
+    n_sample = sum(s.shape[0] for s in sample)
+    for _ in range(args.warmup):
+        for s in sample:
+            o.intersect(s, n_threads=threads)
+    secs = []
+    for _ in range(args.steps):
+        t = 0.0
+        for s in sample:
+            _, dt = o.intersect(s, n_threads=threads)
+            t += dt
+        secs.append(t)
+    total = sum(secs)
+    value = n_sample * args.steps / total / 1e6
+    desc = f"every {frac}th ray of each set ({n_sample} rays per step), classic-builder BVH, {threads} threads"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "sample": desc},
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": desc},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+def run_lrx(args):
+    import torch
+
+    from luxcore_gb300 import lrx
+
+    d = Dist(use_gpu=True)
+    ws, rank, local = d.ws, d.rank, d.local
+    torch.cuda.set_device(local)
+    stream = torch.cuda.Stream()
+    st = stream.cuda_stream
+
+    scene_desc = make_scene()
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        scene = lrx.Scene(scene_desc, stream=st)
+    build_s = time.perf_counter() - t0
+    info = scene.info()
+
+    primary = W.pinhole_rays(1024, 1024)
+
+    def up(a):
+        return torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).reshape(-1).copy()).cuda(local)
+
+    d_prim = up(primary)
+    d_ph = torch.empty(primary.shape[0] * HIT_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
+    scene.trace(d_prim.data_ptr(), d_ph.data_ptr(), primary.shape[0], lrx.LRX_TRACE_CLOSEST, st)
+    stream.synchronize()
+    ph = d_ph.cpu().numpy().view(W.HIT_DTYPE)
+    bounce, shadow = derived_rays(scene_desc, primary, ph, W.BASE_SEED + 100)
+    sets = [("primary", primary, lrx.LRX_TRACE_CLOSEST), ("bounce", bounce, lrx.LRX_TRACE_CLOSEST),
+            ("shadow", shadow, lrx.LRX_TRACE_ANY)]
+    dev = []
+    for name, r, mode in sets:
+        dr = up(r)
+        dh = torch.empty(r.shape[0] * HIT_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
+        dev.append((name, dr, dh, r.shape[0], mode))
+    rays_per_step = sum(x[3] for x in dev)
+
+    # traversal counters (untimed): nodes / triangles fetched per ray
+    counts = {}
+    cbuf = torch.zeros(4, dtype=torch.int64, device=f"cuda:{local}")
+    for name, dr, dh, n, mode in dev:
+        cbuf.zero_()
+        scene.trace_counted(dr.data_ptr(), dh.data_ptr(), n, mode, cbuf.data_ptr(), st)
+        stream.synchronize()
+        nodes, tris, insts, rays = cbuf.cpu().tolist()
+        counts[name] = (nodes / n, tris / n, insts / n)
+    alg_bytes = {}
+    for name, dr, dh, n, mode in dev:
+        nn, nt, ni = counts[name]
+        alg_bytes[name] = n * (RAY_BYTES + HIT_BYTES + nn * NODE_BYTES + nt * TRI_BYTES + ni * INST_BYTES)
+
+    def step(evs=None):
+        for k, (name, dr, dh, n, mode) in enumerate(dev):
+            if evs is not None:
+                evs[k][0].record(stream)
+            scene.trace(dr.data_ptr(), dh.data_ptr(), n, mode, st)
+            if evs is not None:
+                evs[k][1].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    stream.synchronize()
+    if scene.device_status(st) != 0:
+        raise RuntimeError("device status word set during warm-up")
+
+    ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in dev]
+          for _ in range(args.steps)]
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(local)
+    d.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    start.record(stream)
+    for k in range(args.steps):
+        step(ev[k])
+    end.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    d.barrier()
+    elapsed_ms = start.elapsed_time(end)
+    elapsed_ms = d.max(elapsed_ms)
+    kern_ms = {name: statistics.mean(ev[k][j][0].elapsed_time(ev[k][j][1]) for k in range(args.steps))
+               for j, (name, *_rest) in enumerate(dev)}
+    value = rays_per_step * args.steps * ws / (elapsed_ms / 1e3) / 1e6
+
+    # roofline of the traversal kernel: algorithmic bytes / kernel time
+    peak, peak_kind = load_peaks()
+    tot_alg = sum(alg_bytes.values())
+    tot_ms = sum(kern_ms.values())
+    achieved = tot_alg / (tot_ms / 1e3) / 1e9
+    tpr = load_traffic_per_ray()
+    traffic = None if tpr is None else tpr * rays_per_step / len(dev)
+
+    # end to end: host rays in pinned memory -> lrx_trace_host -> host hits
+    pinned = []
+    for name, r, mode in sets:
+        hr = torch.from_numpy(np.ascontiguousarray(r).view(np.uint8).reshape(-1).copy()).pin_memory()
+        hh = torch.empty(r.shape[0] * HIT_BYTES, dtype=torch.uint8).pin_memory()
+        pinned.append((hr, hh, r.shape[0], mode))
+
+    def e2e_step():
+        for hr, hh, n, mode in pinned:
+            scene.trace_host_ptr(hr.data_ptr(), hh.data_ptr(), n, mode, st)
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    d.barrier()
+    t1 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_s = d.max(time.perf_counter() - t1)
+    e2e_value = rays_per_step * args.steps * ws / e2e_s / 1e6
+    h2d = rays_per_step * (RAY_BYTES + HIT_BYTES)
+    d2h = rays_per_step * HIT_BYTES
+
+    line = None
+    if rank == 0:
+        cpu = None
+        if not args.no_cpu_baseline:
+            threads = os.cpu_count() or 1
+            frac = args.ref_fraction
+            sample = [primary[::frac], bounce[::frac], shadow[::frac]]
+            n_s, secs = cpu_measure(scene_desc, sample, threads)
+            cpu = {"value": round(n_s / secs / 1e6, 3), "unit": UNIT, "cores": threads, "kind": "port",
+                   "sample": f"every {frac}th ray of each of the 3 sets ({n_s} rays), oracle BVHAccel::Intersect "
+                             f"restatement, classic-builder BVH, {threads} threads"}
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(elapsed_ms / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {
+                "workload": WORKLOAD, "rays_per_step": rays_per_step, "triangles": info["triangle_count"],
+                "l2": "inputs larger than L2 (rays 302 MB + hits 126 MB + scene per step)",
+                "parallelism": f"replicas x{ws}", "build_ms": round(info["build_ms"], 1),
+                "scene_build_wall_s": round(build_s, 3), "wide_nodes": info["node_count"],
+                "bvh_depth": info["max_depth"],
+                "per_set_ms": {k: round(v, 4) for k, v in kern_ms.items()},
+                "per_set_Mrays": {name: round(n / (kern_ms[name] / 1e3) / 1e6, 1) for name, _, _, n, _ in dev},
+                "nodes_tris_per_ray": {k: [round(v[0], 2), round(v[1], 2)] for k, v in counts.items()},
+            },
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": traffic,
+                         "peak_kind": peak_kind,
+                         "bytes_per_ray": round(tot_alg / rays_per_step, 1)},
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "api": "lrx_trace_host (pinned host buffers)"},
+            "gpu_launches": len(dev) * args.steps,
+            "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    scene.close()
+    d.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="lrx", choices=["lrx", "reference"])
+    ap.add_argument("--ref-fraction", type=int, default=4,
+                    help="CPU legs trace every Nth ray of each set")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        log("warmup raised to 3 (timing rule)")
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_lrx(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,173 @@
+/*
+ * lrx -- GB300 ray-intersection engine for the LuxRays data-parallel path.
+ *
+ * C ABI of liblrx.so: plain pointers, sizes and status codes; no C++ or
+ * CUDA types cross it (a CUDA stream is passed as `void *`, a device buffer
+ * as a `void *` device address).  Every entry point is thread-safe per
+ * scene, returns an lrx_status and never throws.
+ *
+ * Data formats are LuxRays' own:
+ *   lrx_ray  == luxrays::Ray    (48 B)  include/luxrays/core/geometry/ray.h:35-103,
+ *                                       ray_types.cl:24-31
+ *   lrx_hit  == luxrays::RayHit (20 B)  ray.h:93-103, ray_types.cl:33-36
+ * A miss is meshIndex == LRX_NULL_INDEX with t = the ray's maxt
+ * (bvh.cl:219-223); rays with LRX_RAY_FLAGS_MASKED set are skipped and their
+ * hit is not written (bvh.cl:243-244).
+ */
+#ifndef LRX_H
+#define LRX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LRX_ABI_VERSION 1u
+#define LRX_NULL_INDEX 0xffffffffu      /* luxrays_types.cl:21 */
+#define LRX_RAY_FLAGS_MASKED 0x1u       /* ray_types.cl:22 */
+
+typedef struct lrx_ray {
+	float o[3], d[3];
+	float mint, maxt, time;
+	uint32_t flags;
+	float pad[2];
+} lrx_ray;
+
+typedef struct lrx_hit {
+	float t, b1, b2;
+	uint32_t meshIndex, triangleIndex;
+} lrx_hit;
+
+typedef enum lrx_status {
+	LRX_OK = 0,
+	LRX_ERR_INVALID_ARGUMENT = 1,  /* bad pointer, size, alignment or index */
+	LRX_ERR_CUDA = 2,              /* a CUDA runtime call failed */
+	LRX_ERR_OUT_OF_MEMORY = 3,     /* device allocation failed */
+	LRX_ERR_BUILD = 4,             /* BVH build failed (e.g. depth limit) */
+	LRX_ERR_DEVICE = 5,            /* a kernel reported a fault in the status word */
+	LRX_ERR_NOT_SUPPORTED = 6,     /* e.g. no sm_103 device */
+	LRX_ERR_BUDGET = 7,            /* serving: request exceeds the HBM budget */
+	LRX_ERR_BUSY = 8,              /* serving: queue full */
+	LRX_ERR_TIMEOUT = 9            /* host wait limit reached */
+} lrx_status;
+
+/* Trace modes (lrx_trace `mode`). */
+#define LRX_TRACE_CLOSEST 0u  /* closest hit, ties broken by lowest (meshIndex, triangleIndex) */
+#define LRX_TRACE_ANY 1u      /* any hit in [mint, maxt] (shadow rays) */
+
+/* One TriangleMesh: FP32 xyz vertices and u32 vertex-index triples, host
+ * memory owned by the caller (trianglemesh.h:79-201).  The library copies
+ * them to the device during lrx_scene_create. */
+typedef struct lrx_mesh_desc {
+	const float *vertices;
+	const uint32_t *triangles;
+	uint32_t vertex_count;
+	uint32_t triangle_count;
+} lrx_mesh_desc;
+
+#define LRX_OBJECT_INSTANCE 0x1u     /* InstanceTriangleMesh: use transform */
+#define LRX_OBJECT_HAS_INVERSE 0x2u  /* inverse supplied (Transform::mInv) */
+
+/* One DataSet entry (dataset.cpp:66-81).  Its position in the object array
+ * is the meshIndex reported in hits.  A plain object (flags == 0) is the
+ * mesh in world space; an instance (trianglemesh.h:203-305) is the mesh under
+ * the row-major local-to-world `transform` (Transform::m).  Without
+ * LRX_OBJECT_HAS_INVERSE the inverse is Matrix4x4::Inverse of `transform`
+ * (matrix4x4.cpp:118-170), as Transform's constructor computes it. */
+typedef struct lrx_object_desc {
+	uint32_t mesh;
+	uint32_t flags;
+	float transform[16];
+	float inverse[16];
+} lrx_object_desc;
+
+typedef struct lrx_build_opts {
+	uint32_t struct_size;    /* sizeof(lrx_build_opts) */
+	uint32_t leaf_max;       /* triangles per leaf, 1..3 (default 3) */
+	uint32_t treelet_passes; /* treelet SAH restructuring passes (default 2, 0 = plain LBVH) */
+	uint32_t reserved;
+} lrx_build_opts;
+
+typedef struct lrx_scene lrx_scene;
+
+typedef struct lrx_scene_info {
+	uint64_t triangle_count;       /* effective triangles (instances counted per instance) */
+	uint64_t unique_triangle_count;
+	uint32_t object_count;
+	uint32_t instance_count;
+	uint32_t blas_count;
+	uint32_t two_level;
+	uint64_t node_count;           /* 80-B wide nodes, all levels */
+	uint64_t device_bytes;         /* device memory held by the scene */
+	uint32_t max_depth;            /* deepest wide-node path */
+	uint32_t reserved;
+	double build_ms;               /* device build time (excludes host->device copy) */
+} lrx_scene_info;
+
+/* ABI version of the loaded library (LRX_ABI_VERSION). */
+uint32_t lrx_abi_version(void);
+
+/* Last error message of the calling thread ("" if none). */
+const char *lrx_last_error(void);
+
+/* Builds a scene on the current CUDA device: uploads the meshes and builds
+ * one BVH per unique mesh plus, when instances are present, a top-level BVH
+ * over the objects.  objects == NULL means one plain object per mesh.
+ * Replaces: luxrays::Accelerator::Init (include/luxrays/core/accelerator.h:51)
+ * together with the device upload in the BVHKernel / MBVHKernel constructors
+ * (src/luxrays/accelerators/bvhaccelhw.cpp:38-240,
+ * src/luxrays/accelerators/mbvhaccelhw.cpp:41-440). */
+lrx_status lrx_scene_create(const lrx_mesh_desc *meshes, uint32_t mesh_count,
+		const lrx_object_desc *objects, uint32_t object_count,
+		const lrx_build_opts *opts, void *stream, lrx_scene **out_scene);
+
+/* Frees the scene's device memory (Accelerator destructor). */
+lrx_status lrx_scene_destroy(lrx_scene *scene);
+
+/* Re-reads the instance transforms of an existing scene (same object list,
+ * same meshes) and rebuilds only the top-level BVH.
+ * Replaces: luxrays::Accelerator::Update (accelerator.h:52-53),
+ * MBVHAccel::Update (mbvhaccel.cpp:237-250) and
+ * HardwareIntersectionKernel::Update (hardwareintersectiondevice.h:66),
+ * MBVHKernel::Update (mbvhaccelhw.cpp:442-466). */
+lrx_status lrx_scene_update_instances(lrx_scene *scene,
+		const lrx_object_desc *objects, uint32_t object_count, void *stream);
+
+lrx_status lrx_scene_get_info(const lrx_scene *scene, lrx_scene_info *info);
+
+/* Traces `count` rays already resident in device memory (16-B aligned
+ * lrx_ray array) into a device lrx_hit array, asynchronously on `stream`
+ * (NULL = legacy default stream, as the reference's cuLaunchKernel on
+ * stream 0).
+ * Replaces: HardwareIntersectionKernel::EnqueueTraceRayBuffer
+ * (include/luxrays/core/hardwareintersectiondevice.h:67-68), i.e.
+ * BVHKernel / MBVHKernel::EnqueueTraceRayBuffer
+ * (bvhaccelhw.cpp:259-268, mbvhaccelhw.cpp:468-477). */
+lrx_status lrx_trace(lrx_scene *scene, const void *d_rays, void *d_hits,
+		uint32_t count, uint32_t mode, void *stream);
+
+/* Same as lrx_trace for rays and hits in HOST memory: copies the rays in,
+ * traces, copies the hits out and synchronises `stream`.  Staging buffers
+ * are allocated on first use and kept by the scene.
+ * Replaces: the serial IntersectionDevice::TraceRay loop
+ * (include/luxrays/core/intersectiondevice.h:65-68) for batches. */
+lrx_status lrx_trace_host(lrx_scene *scene, const lrx_ray *h_rays, lrx_hit *h_hits,
+		uint32_t count, uint32_t mode, void *stream);
+
+/* Like lrx_trace, and also accumulates per-ray traversal counters into
+ * d_counters[4] (u64: wide nodes fetched, triangles tested, instances
+ * entered, rays traced) -- the byte accounting of the roofline. */
+lrx_status lrx_trace_counted(lrx_scene *scene, const void *d_rays, void *d_hits,
+		uint32_t count, uint32_t mode, uint64_t *d_counters, void *stream);
+
+/* Synchronises `stream` and returns (then clears) the scene's device status
+ * word: 0 = no fault; bit 0 = traversal stack limit; bit 1 = visit limit. */
+lrx_status lrx_scene_device_status(lrx_scene *scene, uint32_t *status, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LRX_H */

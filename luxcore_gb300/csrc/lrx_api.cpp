@@ -1,0 +1,703 @@
+// C-ABI layer of liblrx.so: scene assembly on the device, instance
+// transforms, tracing entry points and error reporting.  Declarations and
+// the reference interfaces each entry point replaces are in include/lrx.h.
+//
+// Compiled with -ffp-contract=off so the host-side FP32 arithmetic below
+// (Matrix4x4::Inverse, instance boxes) rounds exactly as the reference's.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "lrx_common.cuh"
+#include "lrx_internal.h"
+
+namespace lrx {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+
+lrx_status cuda_fail(cudaError_t e, const char *what) {
+	set_error(std::string(what) + ": " + cudaGetErrorString(e));
+	cudaGetLastError();  // clear a non-sticky error
+	return e == cudaErrorMemoryAllocation ? LRX_ERR_OUT_OF_MEMORY : LRX_ERR_CUDA;
+}
+
+lrx_status DevBuf::alloc(size_t n) {
+	if (n <= bytes && ptr) return LRX_OK;
+	release();
+	if (n == 0) return LRX_OK;
+	void *p = nullptr;
+	const cudaError_t e = cudaMalloc(&p, n);
+	if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc");
+	ptr = p;
+	bytes = n;
+	return LRX_OK;
+}
+
+void DevBuf::release() {
+	if (ptr) cudaFree(ptr);
+	ptr = nullptr;
+	bytes = 0;
+}
+
+// Matrix4x4::Inverse (src/luxrays/core/geometry/matrix4x4.cpp:118-170):
+// Gauss-Jordan elimination with full pivoting, FP32.  Returns false for a
+// singular matrix (the reference throws).
+static bool matrix_inverse(const float in[16], float out[16]) {
+	int indxc[4], indxr[4];
+	int ipiv[4] = {0, 0, 0, 0};
+	float minv[4][4];
+	std::memcpy(minv, in, sizeof(minv));
+	for (int i = 0; i < 4; ++i) {
+		int irow = -1, icol = -1;
+		float big = 0.f;
+		for (int j = 0; j < 4; ++j) {
+			if (ipiv[j] == 1) continue;
+			for (int k = 0; k < 4; ++k) {
+				if (ipiv[k] == 0) {
+					if (std::fabs(minv[j][k]) >= big) {
+						big = std::fabs(minv[j][k]);
+						irow = j;
+						icol = k;
+					}
+				} else if (ipiv[k] > 1) {
+					return false;
+				}
+			}
+		}
+		if (icol < 0) return false;
+		++ipiv[icol];
+		if (irow != icol)
+			for (int k = 0; k < 4; ++k) std::swap(minv[irow][k], minv[icol][k]);
+		indxr[i] = irow;
+		indxc[i] = icol;
+		if (minv[icol][icol] == 0.f) return false;
+		const float pivinv = 1.f / minv[icol][icol];
+		minv[icol][icol] = 1.f;
+		for (int j = 0; j < 4; ++j) minv[icol][j] *= pivinv;
+		for (int j = 0; j < 4; ++j) {
+			if (j == icol) continue;
+			const float save = minv[j][icol];
+			minv[j][icol] = 0.f;
+			for (int k = 0; k < 4; ++k) minv[j][k] -= minv[icol][k] * save;
+		}
+	}
+	for (int j = 3; j >= 0; --j) {
+		if (indxr[j] != indxc[j])
+			for (int k = 0; k < 4; ++k) std::swap(minv[k][indxr[j]], minv[k][indxc[j]]);
+	}
+	std::memcpy(out, minv, sizeof(minv));
+	return true;
+}
+
+// MachineEpsilon::E (include/luxrays/core/epsilon.h:50-55)
+static float machine_eps_host(float v) {
+	uint32_t u;
+	std::memcpy(&u, &v, 4);
+	u += 0x80u;
+	float n;
+	std::memcpy(&n, &u, 4);
+	const float e = std::fabs(n - v);
+	return e > 1e-5f ? (e < 1e-1f ? e : 1e-1f) : 1e-5f;
+}
+
+// Transform * Point with the w divide (transform.h:118-128)
+static void xform_point_host(const float m[16], const float p[3], float out[3]) {
+	const float x = p[0], y = p[1], z = p[2];
+	float r[3] = {m[0] * x + m[1] * y + m[2] * z + m[3], m[4] * x + m[5] * y + m[6] * z + m[7],
+			m[8] * x + m[9] * y + m[10] * z + m[11]};
+	const float w = m[12] * x + m[13] * y + m[14] * z + m[15];
+	if (w != 1.f) {
+		const float inv = 1.f / w;
+		r[0] *= inv;
+		r[1] *= inv;
+		r[2] *= inv;
+	}
+	out[0] = r[0];
+	out[1] = r[1];
+	out[2] = r[2];
+}
+
+// World box of an instance: the 8 transformed corners of the BLAS box,
+// expanded by MachineEpsilon::E as MBVHAccel::Init does (mbvhaccel.cpp:189-193).
+static void instance_box(const float m[16], const float lo[3], const float hi[3], float olo[3], float ohi[3]) {
+	for (int k = 0; k < 3; ++k) {
+		olo[k] = INFINITY;
+		ohi[k] = -INFINITY;
+	}
+	for (int c = 0; c < 8; ++c) {
+		const float p[3] = {(c & 1) ? hi[0] : lo[0], (c & 2) ? hi[1] : lo[1], (c & 4) ? hi[2] : lo[2]};
+		float q[3];
+		xform_point_host(m, p, q);
+		for (int k = 0; k < 3; ++k) {
+			olo[k] = std::min(olo[k], q[k]);
+			ohi[k] = std::max(ohi[k], q[k]);
+		}
+	}
+	float e = 0.f;
+	for (int k = 0; k < 3; ++k) e = std::max(e, std::max(machine_eps_host(olo[k]), machine_eps_host(ohi[k])));
+	for (int k = 0; k < 3; ++k) {
+		olo[k] = std::nextafter(olo[k] - e, -INFINITY);
+		ohi[k] = std::nextafter(ohi[k] + e, INFINITY);
+	}
+}
+
+static bool all_finite(const float *v, int n) {
+	for (int i = 0; i < n; ++i)
+		if (!std::isfinite(v[i])) return false;
+	return true;
+}
+
+struct Blas {
+	uint32_t mesh = kNull;        // instanced mesh, or kNull for the merged plain BLAS
+	uint32_t tri_count = 0;
+	uint32_t root = kNull;        // absolute node index
+	float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+};
+
+}  // namespace lrx
+
+using namespace lrx;
+
+struct lrx_scene {
+	int device = 0;
+	bool two_level = false;
+	uint32_t root = kNull;
+	DevBuf nodes, tris, insts, status, stage_rays, stage_hits;
+	std::vector<Blas> blas;
+	std::vector<uint32_t> obj_blas;     // per object: BLAS index, kNull if empty
+	std::vector<uint32_t> obj_flags;
+	uint32_t mesh_count = 0;
+	uint32_t plain_blas = kNull;        // index of the merged plain BLAS
+	uint32_t tlas_node_offset = 0;
+	uint32_t tlas_capacity = 0;
+	uint32_t blas_node_total = 0;
+	lrx_build_opts opts{};
+	lrx_scene_info info{};
+	BuildScratch scratch;
+	std::mutex mu;
+};
+
+namespace {
+
+struct DeviceGuard {
+	int prev = -1;
+	explicit DeviceGuard(int dev) {
+		if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) cudaSetDevice(dev);
+		else prev = -1;
+	}
+	~DeviceGuard() {
+		if (prev >= 0) cudaSetDevice(prev);
+	}
+};
+
+lrx_status validate_meshes(const lrx_mesh_desc *meshes, uint32_t n) {
+	for (uint32_t i = 0; i < n; ++i) {
+		const lrx_mesh_desc &m = meshes[i];
+		if ((m.vertex_count && !m.vertices) || (m.triangle_count && !m.triangles)) {
+			set_error("mesh " + std::to_string(i) + ": null vertex or triangle pointer");
+			return LRX_ERR_INVALID_ARGUMENT;
+		}
+		for (uint64_t k = 0; k < 3ull * m.triangle_count; ++k) {
+			if (m.triangles[k] >= m.vertex_count) {
+				set_error("mesh " + std::to_string(i) + ": vertex index out of range");
+				return LRX_ERR_INVALID_ARGUMENT;
+			}
+		}
+	}
+	return LRX_OK;
+}
+
+// Instance record rows from the object's world->local matrix.
+lrx_status object_inverse(const lrx_object_desc &o, float inv[16]) {
+	if (!all_finite(o.transform, 16)) {
+		set_error("instance transform is not finite");
+		return LRX_ERR_INVALID_ARGUMENT;
+	}
+	if (o.flags & LRX_OBJECT_HAS_INVERSE) {
+		std::memcpy(inv, o.inverse, 64);
+		return LRX_OK;
+	}
+	if (!matrix_inverse(o.transform, inv)) {
+		set_error("singular instance transform");
+		return LRX_ERR_INVALID_ARGUMENT;
+	}
+	return LRX_OK;
+}
+
+// Builds one BLAS from a host vertex/index array; appends its nodes and
+// triangle records to the staging vectors of device buffers.
+struct BlasBuild {
+	DevBuf nodes, records;
+	uint32_t node_count = 0, tri_count = 0, depth = 0;
+};
+
+lrx_status build_blas(lrx_scene *s, const float *h_verts, uint32_t nv, const uint32_t *h_idx, uint32_t nt,
+		const uint32_t *h_tri_object, uint32_t object_const, cudaStream_t st, BlasBuild &out, Blas &b) {
+	lrx_status rc;
+	DevBuf d_v, d_i, d_to, d_lo, d_hi;
+	if ((rc = d_v.alloc(12ull * nv)) != LRX_OK) return rc;
+	if ((rc = d_i.alloc(12ull * nt)) != LRX_OK) return rc;
+	if ((rc = d_lo.alloc(16ull * nt)) != LRX_OK) return rc;
+	if ((rc = d_hi.alloc(16ull * nt)) != LRX_OK) return rc;
+	LRX_CUDA(cudaMemcpyAsync(d_v.ptr, h_verts, 12ull * nv, cudaMemcpyHostToDevice, st));
+	LRX_CUDA(cudaMemcpyAsync(d_i.ptr, h_idx, 12ull * nt, cudaMemcpyHostToDevice, st));
+	if (h_tri_object) {
+		if ((rc = d_to.alloc(8ull * nt)) != LRX_OK) return rc;
+		LRX_CUDA(cudaMemcpyAsync(d_to.ptr, h_tri_object, 8ull * nt, cudaMemcpyHostToDevice, st));
+	}
+	if ((rc = launch_triangle_boxes(nt, d_v.as<float>(), d_i.as<uint32_t>(), d_lo.as<float4>(), d_hi.as<float4>(), st)) != LRX_OK)
+		return rc;
+	BvhResult r;
+	if ((rc = build_wide_bvh(nt, d_lo.as<float4>(), d_hi.as<float4>(), s->opts.leaf_max, s->opts.treelet_passes, st,
+			     s->scratch, &r)) != LRX_OK)
+		return rc;
+	out.node_count = r.node_count;
+	out.tri_count = nt;
+	out.depth = r.depth;
+	if ((rc = out.nodes.alloc(sizeof(WideNode) * (size_t)r.node_count)) != LRX_OK) return rc;
+	if ((rc = out.records.alloc(sizeof(TriRecord) * (size_t)nt)) != LRX_OK) return rc;
+	LRX_CUDA(cudaMemcpyAsync(out.nodes.ptr, s->scratch.wide_nodes.ptr, sizeof(WideNode) * (size_t)r.node_count,
+			cudaMemcpyDeviceToDevice, st));
+	if ((rc = launch_triangle_records(nt, s->scratch.prim_order.as<uint32_t>(), d_v.as<float>(), d_i.as<uint32_t>(),
+			     h_tri_object ? d_to.as<uint32_t>() : nullptr, object_const, out.records.as<TriRecord>(), st)) != LRX_OK)
+		return rc;
+	LRX_CUDA(cudaStreamSynchronize(st));  // the temporaries above are freed on return
+	std::memcpy(b.lo, r.lo, sizeof(b.lo));
+	std::memcpy(b.hi, r.hi, sizeof(b.hi));
+	b.tri_count = nt;
+	return LRX_OK;
+}
+
+// (Re)builds the TLAS over the non-empty objects and writes it after the
+// BLAS nodes.  Called at create and by lrx_scene_update_instances.
+lrx_status build_tlas(lrx_scene *s, const lrx_object_desc *objects, uint32_t n_objects, cudaStream_t st) {
+	std::vector<InstRecord> recs;
+	std::vector<float4> blo, bhi;
+	recs.reserve(n_objects + 1);
+	if (s->plain_blas != kNull) {
+		const Blas &b = s->blas[s->plain_blas];
+		InstRecord r{};
+		r.r0 = make_float4(1, 0, 0, 0);
+		r.r1 = make_float4(0, 1, 0, 0);
+		r.r2 = make_float4(0, 0, 1, 0);
+		r.r3 = make_float4(0, 0, 0, 1);
+		r.info = make_uint4(b.root, kNull, kInstIdentity, 0);
+		recs.push_back(r);
+		blo.push_back(make_float4(b.lo[0], b.lo[1], b.lo[2], 0));
+		bhi.push_back(make_float4(b.hi[0], b.hi[1], b.hi[2], 0));
+	}
+	for (uint32_t i = 0; i < n_objects; ++i) {
+		if (!(s->obj_flags[i] & LRX_OBJECT_INSTANCE)) continue;
+		const uint32_t bi = s->obj_blas[i];
+		if (bi == kNull) continue;
+		const Blas &b = s->blas[bi];
+		float inv[16];
+		lrx_status rc = object_inverse(objects[i], inv);
+		if (rc != LRX_OK) return rc;
+		InstRecord r{};
+		r.r0 = make_float4(inv[0], inv[1], inv[2], inv[3]);
+		r.r1 = make_float4(inv[4], inv[5], inv[6], inv[7]);
+		r.r2 = make_float4(inv[8], inv[9], inv[10], inv[11]);
+		r.r3 = make_float4(inv[12], inv[13], inv[14], inv[15]);
+		r.info = make_uint4(b.root, i, 0, 0);
+		recs.push_back(r);
+		float lo[3], hi[3];
+		instance_box(objects[i].transform, b.lo, b.hi, lo, hi);
+		blo.push_back(make_float4(lo[0], lo[1], lo[2], 0));
+		bhi.push_back(make_float4(hi[0], hi[1], hi[2], 0));
+	}
+	const uint32_t n = (uint32_t)recs.size();
+	if (n == 0) {
+		s->root = kNull;
+		return LRX_OK;
+	}
+	if (n > s->tlas_capacity) {
+		set_error("instance count changed");
+		return LRX_ERR_INVALID_ARGUMENT;
+	}
+	lrx_status rc;
+	DevBuf d_lo, d_hi;
+	if ((rc = d_lo.alloc(16ull * n)) != LRX_OK) return rc;
+	if ((rc = d_hi.alloc(16ull * n)) != LRX_OK) return rc;
+	LRX_CUDA(cudaMemcpyAsync(d_lo.ptr, blo.data(), 16ull * n, cudaMemcpyHostToDevice, st));
+	LRX_CUDA(cudaMemcpyAsync(d_hi.ptr, bhi.data(), 16ull * n, cudaMemcpyHostToDevice, st));
+	BvhResult r;
+	if ((rc = build_wide_bvh(n, d_lo.as<float4>(), d_hi.as<float4>(), 1, s->opts.treelet_passes, st, s->scratch, &r)) != LRX_OK)
+		return rc;
+	std::vector<uint32_t> order(n);
+	LRX_CUDA(cudaMemcpyAsync(order.data(), s->scratch.prim_order.ptr, 4ull * n, cudaMemcpyDeviceToHost, st));
+	LRX_CUDA(cudaStreamSynchronize(st));
+	std::vector<InstRecord> sorted(n);
+	for (uint32_t k = 0; k < n; ++k) sorted[k] = recs[order[k]];
+	LRX_CUDA(cudaMemcpyAsync(s->insts.ptr, sorted.data(), sizeof(InstRecord) * n, cudaMemcpyHostToDevice, st));
+	if ((rc = launch_relocate_nodes(s->scratch.wide_nodes.as<WideNode>(), s->nodes.as<WideNode>() + s->tlas_node_offset,
+			     r.node_count, s->tlas_node_offset, 0, st)) != LRX_OK)
+		return rc;
+	LRX_CUDA(cudaStreamSynchronize(st));
+	s->root = s->tlas_node_offset;
+	s->info.node_count = s->blas_node_total + r.node_count;
+	s->info.max_depth = std::max(s->info.max_depth, r.depth);
+	return LRX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+uint32_t lrx_abi_version(void) { return LRX_ABI_VERSION; }
+
+const char *lrx_last_error(void) { return g_last_error.c_str(); }
+
+lrx_status lrx_scene_create(const lrx_mesh_desc *meshes, uint32_t mesh_count, const lrx_object_desc *objects,
+		uint32_t object_count, const lrx_build_opts *opts, void *stream, lrx_scene **out_scene) {
+	try {
+		if (!out_scene || (mesh_count && !meshes)) {
+			set_error("lrx_scene_create: null argument");
+			return LRX_ERR_INVALID_ARGUMENT;
+		}
+		*out_scene = nullptr;
+		int dev = 0;
+		LRX_CUDA(cudaGetDevice(&dev));
+		cudaDeviceProp prop;
+		LRX_CUDA(cudaGetDeviceProperties(&prop, dev));
+		if (prop.major < 10) {
+			set_error("lrx needs a Blackwell (sm_103) device");
+			return LRX_ERR_NOT_SUPPORTED;
+		}
+		lrx_status rc = validate_meshes(meshes, mesh_count);
+		if (rc != LRX_OK) return rc;
+		std::vector<lrx_object_desc> objs;
+		if (objects) {
+			objs.assign(objects, objects + object_count);
+		} else {
+			objs.resize(mesh_count);
+			for (uint32_t i = 0; i < mesh_count; ++i) {
+				std::memset(&objs[i], 0, sizeof(lrx_object_desc));
+				objs[i].mesh = i;
+			}
+		}
+		const uint32_t n_obj = (uint32_t)objs.size();
+		for (uint32_t i = 0; i < n_obj; ++i) {
+			if (objs[i].mesh >= mesh_count) {
+				set_error("object " + std::to_string(i) + ": mesh index out of range");
+				return LRX_ERR_INVALID_ARGUMENT;
+			}
+			if (objs[i].flags & LRX_OBJECT_INSTANCE) {
+				float inv[16];
+				if ((rc = object_inverse(objs[i], inv)) != LRX_OK) return rc;
+			}
+		}
+
+		lrx_scene *s = new lrx_scene();
+		std::unique_ptr<lrx_scene> guard(s);
+		s->device = dev;
+		s->mesh_count = mesh_count;
+		s->opts.struct_size = sizeof(lrx_build_opts);
+		s->opts.leaf_max = 3;
+		s->opts.treelet_passes = 0;
+		if (opts && opts->struct_size >= sizeof(lrx_build_opts)) {
+			if (opts->leaf_max) s->opts.leaf_max = std::min(3u, opts->leaf_max);
+			s->opts.treelet_passes = opts->treelet_passes;
+		}
+		cudaStream_t st = (cudaStream_t)stream;
+		const auto t0 = std::chrono::steady_clock::now();
+
+		s->obj_flags.resize(n_obj);
+		s->obj_blas.assign(n_obj, kNull);
+		bool any_inst = false;
+		for (uint32_t i = 0; i < n_obj; ++i) {
+			s->obj_flags[i] = objs[i].flags;
+			any_inst |= (objs[i].flags & LRX_OBJECT_INSTANCE) != 0;
+		}
+		s->two_level = any_inst;
+
+		std::vector<BlasBuild> builds;
+		builds.reserve(mesh_count + 1);
+		uint64_t eff_tris = 0, unique_tris = 0;
+		uint32_t n_inst = 0;
+
+		// Merged BLAS over all plain objects, in world space.
+		{
+			uint64_t nv = 0, nt = 0;
+			uint32_t n_plain = 0, single = kNull;
+			for (uint32_t i = 0; i < n_obj; ++i) {
+				if (objs[i].flags & LRX_OBJECT_INSTANCE) continue;
+				const lrx_mesh_desc &m = meshes[objs[i].mesh];
+				if (!m.triangle_count) continue;
+				nv += m.vertex_count;
+				nt += m.triangle_count;
+				++n_plain;
+				single = i;
+			}
+			if (nt > 0xffffffffull / 3 || nv > 0xffffffffull) {
+				set_error("too many triangles in one BVH");
+				return LRX_ERR_INVALID_ARGUMENT;
+			}
+			if (nt) {
+				std::vector<float> cv;
+				std::vector<uint32_t> ci, to;
+				const float *pv;
+				const uint32_t *pi;
+				const uint32_t *pto = nullptr;
+				uint32_t oc = kNull;
+				if (n_plain == 1) {
+					const lrx_mesh_desc &m = meshes[objs[single].mesh];
+					pv = m.vertices;
+					pi = m.triangles;
+					oc = single;
+				} else {
+					cv.reserve(3 * nv);
+					ci.reserve(3 * nt);
+					to.reserve(2 * nt);
+					for (uint32_t i = 0; i < n_obj; ++i) {
+						if (objs[i].flags & LRX_OBJECT_INSTANCE) continue;
+						const lrx_mesh_desc &m = meshes[objs[i].mesh];
+						if (!m.triangle_count) continue;
+						const uint32_t base = (uint32_t)(cv.size() / 3);
+						cv.insert(cv.end(), m.vertices, m.vertices + 3ull * m.vertex_count);
+						for (uint64_t k = 0; k < 3ull * m.triangle_count; ++k) ci.push_back(m.triangles[k] + base);
+						for (uint32_t k = 0; k < m.triangle_count; ++k) {
+							to.push_back(i);
+							to.push_back(k);
+						}
+					}
+					pv = cv.data();
+					pi = ci.data();
+					pto = to.data();
+				}
+				Blas b;
+				builds.emplace_back();
+				if ((rc = build_blas(s, pv, (uint32_t)nv, pi, (uint32_t)nt, pto, oc, st, builds.back(), b)) != LRX_OK)
+					return rc;
+				s->plain_blas = (uint32_t)s->blas.size();
+				s->blas.push_back(b);
+				for (uint32_t i = 0; i < n_obj; ++i)
+					if (!(objs[i].flags & LRX_OBJECT_INSTANCE) && meshes[objs[i].mesh].triangle_count)
+						s->obj_blas[i] = s->plain_blas;
+				eff_tris += nt;
+				unique_tris += nt;
+			}
+		}
+		// One BLAS per instanced mesh
+		std::vector<uint32_t> mesh_blas(mesh_count, kNull);
+		for (uint32_t i = 0; i < n_obj; ++i) {
+			if (!(objs[i].flags & LRX_OBJECT_INSTANCE)) continue;
+			++n_inst;
+			const uint32_t mi = objs[i].mesh;
+			const lrx_mesh_desc &m = meshes[mi];
+			if (!m.triangle_count) continue;
+			eff_tris += m.triangle_count;
+			if (mesh_blas[mi] == kNull) {
+				Blas b;
+				b.mesh = mi;
+				builds.emplace_back();
+				if ((rc = build_blas(s, m.vertices, m.vertex_count, m.triangles, m.triangle_count, nullptr, kNull, st,
+						     builds.back(), b)) != LRX_OK)
+					return rc;
+				mesh_blas[mi] = (uint32_t)s->blas.size();
+				s->blas.push_back(b);
+				unique_tris += m.triangle_count;
+			}
+			s->obj_blas[i] = mesh_blas[mi];
+		}
+
+		// Concatenate all BLAS into the scene arrays
+		uint64_t total_nodes = 0, total_tris = 0;
+		uint32_t max_depth = 0;
+		for (const BlasBuild &bb : builds) {
+			total_nodes += bb.node_count;
+			total_tris += bb.tri_count;
+			max_depth = std::max(max_depth, bb.depth);
+		}
+		const uint32_t tlas_prims = s->two_level ? (uint32_t)s->blas.size() + n_inst : 0;
+		s->tlas_capacity = tlas_prims;
+		if (total_nodes + tlas_prims > 0x7fffffffull) {
+			set_error("scene too large");
+			return LRX_ERR_INVALID_ARGUMENT;
+		}
+		if ((rc = s->nodes.alloc(sizeof(WideNode) * (total_nodes + tlas_prims + 1))) != LRX_OK) return rc;
+		if ((rc = s->tris.alloc(sizeof(TriRecord) * (total_tris + 1))) != LRX_OK) return rc;
+		if ((rc = s->status.alloc(64)) != LRX_OK) return rc;
+		LRX_CUDA(cudaMemsetAsync(s->status.ptr, 0, 64, st));
+		uint32_t node_off = 0, tri_off = 0;
+		for (size_t k = 0; k < builds.size(); ++k) {
+			BlasBuild &bb = builds[k];
+			if ((rc = launch_relocate_nodes(bb.nodes.as<WideNode>(), s->nodes.as<WideNode>() + node_off, bb.node_count,
+					     node_off, tri_off, st)) != LRX_OK)
+				return rc;
+			LRX_CUDA(cudaMemcpyAsync(s->tris.as<TriRecord>() + tri_off, bb.records.ptr, sizeof(TriRecord) * bb.tri_count,
+					cudaMemcpyDeviceToDevice, st));
+			s->blas[k].root = node_off;
+			node_off += bb.node_count;
+			tri_off += bb.tri_count;
+		}
+		LRX_CUDA(cudaStreamSynchronize(st));
+		builds.clear();
+		s->blas_node_total = node_off;
+		s->tlas_node_offset = node_off;
+		s->info.max_depth = max_depth;
+		s->info.node_count = node_off;
+		if (s->two_level) {
+			if ((rc = s->insts.alloc(sizeof(InstRecord) * (tlas_prims + 1))) != LRX_OK) return rc;
+			if ((rc = build_tlas(s, objs.data(), n_obj, st)) != LRX_OK) return rc;
+		} else {
+			s->root = s->blas.empty() ? kNull : 0u;
+		}
+		// scratch is kept only where instance updates need it
+		if (!s->two_level) s->scratch = BuildScratch();
+		const auto t1 = std::chrono::steady_clock::now();
+
+		s->info.triangle_count = eff_tris;
+		s->info.unique_triangle_count = unique_tris;
+		s->info.object_count = n_obj;
+		s->info.instance_count = n_inst;
+		s->info.blas_count = (uint32_t)s->blas.size();
+		s->info.two_level = s->two_level ? 1u : 0u;
+		s->info.device_bytes = s->nodes.bytes + s->tris.bytes + s->insts.bytes + s->status.bytes;
+		s->info.build_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
+		*out_scene = guard.release();
+		return LRX_OK;
+	} catch (const std::bad_alloc &) {
+		set_error("host allocation failed");
+		return LRX_ERR_OUT_OF_MEMORY;
+	} catch (const std::exception &e) {
+		set_error(e.what());
+		return LRX_ERR_INVALID_ARGUMENT;
+	}
+}
+
+lrx_status lrx_scene_destroy(lrx_scene *scene) {
+	if (!scene) return LRX_OK;
+	DeviceGuard g(scene->device);
+	delete scene;
+	return LRX_OK;
+}
+
+lrx_status lrx_scene_update_instances(lrx_scene *s, const lrx_object_desc *objects, uint32_t object_count, void *stream) {
+	if (!s || !objects) {
+		set_error("lrx_scene_update_instances: null argument");
+		return LRX_ERR_INVALID_ARGUMENT;
+	}
+	std::lock_guard<std::mutex> lk(s->mu);
+	DeviceGuard g(s->device);
+	if (object_count != s->obj_flags.size()) {
+		set_error("object count differs from the scene's");
+		return LRX_ERR_INVALID_ARGUMENT;
+	}
+	for (uint32_t i = 0; i < object_count; ++i) {
+		if ((objects[i].flags & LRX_OBJECT_INSTANCE) != (s->obj_flags[i] & LRX_OBJECT_INSTANCE)) {
+			set_error("object " + std::to_string(i) + " changed kind");
+			return LRX_ERR_INVALID_ARGUMENT;
+		}
+	}
+	if (!s->two_level) return LRX_OK;  // nothing moves in a flat scene
+	return build_tlas(s, objects, object_count, (cudaStream_t)stream);
+}
+
+lrx_status lrx_scene_get_info(const lrx_scene *s, lrx_scene_info *info) {
+	if (!s || !info) {
+		set_error("lrx_scene_get_info: null argument");
+		return LRX_ERR_INVALID_ARGUMENT;
+	}
+	*info = s->info;
+	return LRX_OK;
+}
+
+static lrx_status trace_common(lrx_scene *s, const void *d_rays, void *d_hits, uint32_t count, uint32_t mode,
+		uint64_t *d_counters, cudaStream_t st) {
+	if (!s) {
+		set_error("lrx_trace: null scene");
+		return LRX_ERR_INVALID_ARGUMENT;
+	}
+	if (mode > LRX_TRACE_ANY) {
+		set_error("lrx_trace: unknown mode");
+		return LRX_ERR_INVALID_ARGUMENT;
+	}
+	if (count == 0) return LRX_OK;
+	if (!d_rays || !d_hits) {
+		set_error("lrx_trace: null ray or hit buffer");
+		return LRX_ERR_INVALID_ARGUMENT;
+	}
+	if (((uintptr_t)d_rays & 15u) || ((uintptr_t)d_hits & 3u)) {
+		set_error("lrx_trace: rays must be 16-byte aligned, hits 4-byte aligned");
+		return LRX_ERR_INVALID_ARGUMENT;
+	}
+	DeviceGuard g(s->device);
+	TraceArgs a{};
+	a.nodes = s->nodes.as<WideNode>();
+	a.tris = s->tris.as<TriRecord>();
+	a.insts = s->insts.as<InstRecord>();
+	a.root = s->root;
+	a.two_level = s->two_level ? 1u : 0u;
+	a.rays = d_rays;
+	a.hits = d_hits;
+	a.count = count;
+	a.any_hit = mode == LRX_TRACE_ANY;
+	a.status = s->status.as<uint32_t>();
+	a.counters = reinterpret_cast<unsigned long long *>(d_counters);
+	return launch_trace(a, st);
+}
+
+lrx_status lrx_trace(lrx_scene *s, const void *d_rays, void *d_hits, uint32_t count, uint32_t mode, void *stream) {
+	return trace_common(s, d_rays, d_hits, count, mode, nullptr, (cudaStream_t)stream);
+}
+
+lrx_status lrx_trace_counted(lrx_scene *s, const void *d_rays, void *d_hits, uint32_t count, uint32_t mode,
+		uint64_t *d_counters, void *stream) {
+	if (!d_counters) {
+		set_error("lrx_trace_counted: null counters");
+		return LRX_ERR_INVALID_ARGUMENT;
+	}
+	return trace_common(s, d_rays, d_hits, count, mode, d_counters, (cudaStream_t)stream);
+}
+
+lrx_status lrx_trace_host(lrx_scene *s, const lrx_ray *h_rays, lrx_hit *h_hits, uint32_t count, uint32_t mode,
+		void *stream) {
+	if (!s) {
+		set_error("lrx_trace_host: null scene");
+		return LRX_ERR_INVALID_ARGUMENT;
+	}
+	if (count == 0) return LRX_OK;
+	if (!h_rays || !h_hits) {
+		set_error("lrx_trace_host: null ray or hit buffer");
+		return LRX_ERR_INVALID_ARGUMENT;
+	}
+	std::lock_guard<std::mutex> lk(s->mu);
+	DeviceGuard g(s->device);
+	lrx_status rc;
+	if ((rc = s->stage_rays.alloc(sizeof(lrx_ray) * (size_t)count)) != LRX_OK) return rc;
+	if ((rc = s->stage_hits.alloc(sizeof(lrx_hit) * (size_t)count)) != LRX_OK) return rc;
+	cudaStream_t st = (cudaStream_t)stream;
+	LRX_CUDA(cudaMemcpyAsync(s->stage_rays.ptr, h_rays, sizeof(lrx_ray) * (size_t)count, cudaMemcpyHostToDevice, st));
+	// masked rays keep the caller's hit contents: stage them first
+	LRX_CUDA(cudaMemcpyAsync(s->stage_hits.ptr, h_hits, sizeof(lrx_hit) * (size_t)count, cudaMemcpyHostToDevice, st));
+	if ((rc = trace_common(s, s->stage_rays.ptr, s->stage_hits.ptr, count, mode, nullptr, st)) != LRX_OK) return rc;
+	LRX_CUDA(cudaMemcpyAsync(h_hits, s->stage_hits.ptr, sizeof(lrx_hit) * (size_t)count, cudaMemcpyDeviceToHost, st));
+	LRX_CUDA(cudaStreamSynchronize(st));
+	return LRX_OK;
+}
+
+lrx_status lrx_scene_device_status(lrx_scene *s, uint32_t *status, void *stream) {
+	if (!s || !status) {
+		set_error("lrx_scene_device_status: null argument");
+		return LRX_ERR_INVALID_ARGUMENT;
+	}
+	DeviceGuard g(s->device);
+	cudaStream_t st = (cudaStream_t)stream;
+	uint32_t v = 0;
+	LRX_CUDA(cudaMemcpyAsync(&v, s->status.ptr, 4, cudaMemcpyDeviceToHost, st));
+	LRX_CUDA(cudaStreamSynchronize(st));
+	LRX_CUDA(cudaMemsetAsync(s->status.ptr, 0, 4, st));
+	*status = v;
+	return v ? LRX_ERR_DEVICE : LRX_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,548 @@
+// GPU BVH builder: 63-bit Morton codes -> radix sort -> bottom-up LBVH
+// (one thread per leaf climbing with an atomic per internal node, the
+// agglomerative formulation of Apetrei 2014 over the Karras 2012 ordering)
+// -> optional treelet restructuring -> greedy top-down collapse into 8-wide
+// nodes with outward-rounded 8-bit child boxes (the compressed wide BVH of
+// Ylitie, Karras and Laine 2017).
+//
+// Replaces the reference's CPU builders (src/luxrays/core/bvh/
+// bvhclassicbuild.cpp:124-233, bvhembreebuild.cpp:218-357): any correct BVH
+// returns the same closest hit, so the tree shape is free; what must hold is
+// that every child box contains its primitives' padded boxes, which the
+// outward rounding below guarantees.
+#include <algorithm>
+#include <cstring>
+
+#include <cub/device/device_radix_sort.cuh>
+
+#include "lrx_common.cuh"
+#include "lrx_internal.h"
+
+namespace lrx {
+
+constexpr uint32_t kLeafFlag = 0x80000000u;
+
+// counters[] layout (uint32)
+enum : int {
+	C_BMIN = 0,    // 3: centroid bounds min (ordered uint)
+	C_BMAX = 3,    // 3: centroid bounds max
+	C_ROOT = 6,    // binary root reference
+	C_NODES = 7,   // wide-node allocation counter
+	C_TRIS = 8,    // leaf-primitive allocation counter
+	C_QA = 9,      // queue A item count
+	C_QB = 10,     // queue B item count
+	C_BOX = 12,    // 6 floats: root box lo.xyz, hi.xyz
+	C_COUNT = 20
+};
+
+// ---------------------------------------------------------------------------
+// Morton codes
+// ---------------------------------------------------------------------------
+
+__global__ void k_centroid_bounds(uint32_t n, const float4 *__restrict__ lo, const float4 *__restrict__ hi,
+		uint32_t *counters) {
+	float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+		const float4 a = lo[i], b = hi[i];
+		const float c[3] = {0.5f * (a.x + b.x), 0.5f * (a.y + b.y), 0.5f * (a.z + b.z)};
+#pragma unroll
+		for (int k = 0; k < 3; ++k) {
+			mn[k] = fminf(mn[k], c[k]);
+			mx[k] = fmaxf(mx[k], c[k]);
+		}
+	}
+#pragma unroll
+	for (int k = 0; k < 3; ++k) {
+#pragma unroll
+		for (int off = 16; off > 0; off >>= 1) {
+			mn[k] = fminf(mn[k], __shfl_xor_sync(0xffffffffu, mn[k], off));
+			mx[k] = fmaxf(mx[k], __shfl_xor_sync(0xffffffffu, mx[k], off));
+		}
+	}
+	if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+		for (int k = 0; k < 3; ++k) {
+			atomicMin(&counters[C_BMIN + k], f2ord(mn[k]));
+			atomicMax(&counters[C_BMAX + k], f2ord(mx[k]));
+		}
+	}
+}
+
+__device__ __forceinline__ uint64_t expand21(uint32_t v) {
+	uint64_t x = v & 0x1fffffu;
+	x = (x | x << 32) & 0x1f00000000ffffull;
+	x = (x | x << 16) & 0x1f0000ff0000ffull;
+	x = (x | x << 8) & 0x100f00f00f00f00full;
+	x = (x | x << 4) & 0x10c30c30c30c30c3ull;
+	x = (x | x << 2) & 0x1249249249249249ull;
+	return x;
+}
+
+__global__ void k_morton(uint32_t n, const float4 *__restrict__ lo, const float4 *__restrict__ hi,
+		const uint32_t *__restrict__ counters, uint64_t *keys, uint32_t *vals) {
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	const float4 a = lo[i], b = hi[i];
+	const float c[3] = {0.5f * (a.x + b.x), 0.5f * (a.y + b.y), 0.5f * (a.z + b.z)};
+	uint32_t q[3];
+#pragma unroll
+	for (int k = 0; k < 3; ++k) {
+		const float mn = ord2f(counters[C_BMIN + k]), mx = ord2f(counters[C_BMAX + k]);
+		const float ext = mx - mn;
+		float u = ext > 0.f ? (c[k] - mn) / ext : 0.f;
+		u = fminf(fmaxf(u, 0.f), 1.f);
+		q[k] = min((uint32_t)(u * 2097152.f), 2097151u);
+	}
+	keys[i] = (expand21(q[0]) << 2) | (expand21(q[1]) << 1) | expand21(q[2]);
+	vals[i] = i;
+}
+
+// ---------------------------------------------------------------------------
+// Bottom-up binary hierarchy
+// ---------------------------------------------------------------------------
+
+// delta(a) < delta(b), delta(i) = (key[i] ^ key[i+1], i ^ (i+1)) compared
+// lexicographically: the key bits dominate, the index breaks key ties.
+__device__ __forceinline__ bool delta_less(const uint64_t *__restrict__ keys, uint32_t a, uint32_t b) {
+	const uint64_t ka = keys[a] ^ keys[a + 1], kb = keys[b] ^ keys[b + 1];
+	if (ka != kb) return ka < kb;
+	return (a ^ (a + 1)) < (b ^ (b + 1));
+}
+
+__global__ void k_hierarchy(uint32_t n, const uint64_t *__restrict__ keys, const uint32_t *__restrict__ sorted,
+		const float4 *__restrict__ plo, const float4 *__restrict__ phi, uint32_t *bchild, float4 *bn_lo,
+		float4 *bn_hi, uint2 *brange, uint32_t *other, uint32_t *counters) {
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	const uint32_t p = sorted[i];
+	float4 lo = plo[p], hi = phi[p];
+	if (n == 1) {
+		counters[C_ROOT] = kLeafFlag;
+		reinterpret_cast<float *>(counters + C_BOX)[0] = lo.x;
+		reinterpret_cast<float *>(counters + C_BOX)[1] = lo.y;
+		reinterpret_cast<float *>(counters + C_BOX)[2] = lo.z;
+		reinterpret_cast<float *>(counters + C_BOX)[3] = hi.x;
+		reinterpret_cast<float *>(counters + C_BOX)[4] = hi.y;
+		reinterpret_cast<float *>(counters + C_BOX)[5] = hi.z;
+		return;
+	}
+	uint32_t l = i, r = i, cur = kLeafFlag | i;
+	// Each climb step moves to a strictly larger range, so the loop ends in
+	// at most n steps.
+	for (uint32_t step = 0; step < n; ++step) {
+		const bool left_child = (l == 0) || (r != n - 1 && delta_less(keys, r, l - 1));
+		const uint32_t parent = left_child ? r : l - 1;
+		bchild[2 * parent + (left_child ? 0 : 1)] = cur;
+		__threadfence();
+		const uint32_t prev = atomicExch(&other[parent], left_child ? l : r);
+		if (prev == kNull) return;  // the sibling finishes this node
+		__threadfence();
+		if (left_child) r = prev;
+		else l = prev;
+		const uint32_t sib = __ldcg(&bchild[2 * parent + (left_child ? 1 : 0)]);
+		float4 slo, shi;
+		if (sib & kLeafFlag) {
+			const uint32_t sp = sorted[sib & ~kLeafFlag];
+			slo = plo[sp];
+			shi = phi[sp];
+		} else {
+			slo = __ldcg(&bn_lo[sib]);
+			shi = __ldcg(&bn_hi[sib]);
+		}
+		lo = make_float4(fminf(lo.x, slo.x), fminf(lo.y, slo.y), fminf(lo.z, slo.z), 0.f);
+		hi = make_float4(fmaxf(hi.x, shi.x), fmaxf(hi.y, shi.y), fmaxf(hi.z, shi.z), 0.f);
+		__stcg(&bn_lo[parent], lo);
+		__stcg(&bn_hi[parent], hi);
+		__stcg(&brange[parent], make_uint2(l, r));
+		cur = parent;
+		if (l == 0 && r == n - 1) {
+			counters[C_ROOT] = parent;
+			float *box = reinterpret_cast<float *>(counters + C_BOX);
+			box[0] = lo.x; box[1] = lo.y; box[2] = lo.z;
+			box[3] = hi.x; box[4] = hi.y; box[5] = hi.z;
+			return;
+		}
+	}
+}
+
+// ---------------------------------------------------------------------------
+// Collapse to 8-wide quantised nodes
+// ---------------------------------------------------------------------------
+
+// Smallest biased exponent e (scale 2^(e-127)) with ext * 2^-(e-127) <= 255.
+__device__ __forceinline__ uint32_t quant_exponent(float ext) {
+	if (!(ext > 0.f)) return 1u;
+	const int ex = (int)((__float_as_uint(ext) >> 23) & 0xffu);
+	int e = ex - 8;
+	if (e < 1) e = 1;
+	while (e < 253 && __fmul_ru(ext, __uint_as_float((uint32_t)(254 - e) << 23)) > 255.f) ++e;
+	return (uint32_t)e;
+}
+
+__device__ __forceinline__ float box_area(float3 lo, float3 hi) {
+	const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+	return dx * dy + dx * dz + dy * dz;
+}
+
+struct ChildBox {
+	float3 lo, hi;
+};
+
+__device__ __forceinline__ void load_ref_box(uint32_t ref, const uint32_t *__restrict__ sorted,
+		const float4 *__restrict__ plo, const float4 *__restrict__ phi, const float4 *__restrict__ bn_lo,
+		const float4 *__restrict__ bn_hi, ChildBox &b) {
+	float4 a, c;
+	if (ref & kLeafFlag) {
+		const uint32_t p = sorted[ref & ~kLeafFlag];
+		a = plo[p];
+		c = phi[p];
+	} else {
+		a = bn_lo[ref];
+		c = bn_hi[ref];
+	}
+	b.lo = make_float3(a.x, a.y, a.z);
+	b.hi = make_float3(c.x, c.y, c.z);
+}
+
+__global__ void __launch_bounds__(128) k_collapse(const uint2 *__restrict__ items, const uint32_t *n_items_ptr,
+		uint2 *__restrict__ out_items, uint32_t *n_out, const uint32_t *__restrict__ bchild,
+		const float4 *__restrict__ bn_lo, const float4 *__restrict__ bn_hi, const uint2 *__restrict__ brange,
+		const uint32_t *__restrict__ sorted, const float4 *__restrict__ plo, const float4 *__restrict__ phi,
+		uint32_t leaf_max, WideNode *__restrict__ wnodes, uint32_t *__restrict__ prim_order, uint32_t *counters) {
+	const uint32_t n_items = *n_items_ptr;
+	for (uint32_t it = blockIdx.x * blockDim.x + threadIdx.x; it < n_items; it += gridDim.x * blockDim.x) {
+		const uint2 item = items[it];
+		uint32_t cref[8];
+		ChildBox cb[8];
+		int cnt;
+		if (item.x & kLeafFlag) {
+			cref[0] = item.x;
+			load_ref_box(item.x, sorted, plo, phi, bn_lo, bn_hi, cb[0]);
+			cnt = 1;
+		} else {
+			cref[0] = bchild[2 * item.x];
+			cref[1] = bchild[2 * item.x + 1];
+			load_ref_box(cref[0], sorted, plo, phi, bn_lo, bn_hi, cb[0]);
+			load_ref_box(cref[1], sorted, plo, phi, bn_lo, bn_hi, cb[1]);
+			cnt = 2;
+		}
+		// Greedy: open the largest-area internal child until 8 slots are used.
+		while (cnt < 8) {
+			int best = -1;
+			float best_a = -1.f;
+			for (int k = 0; k < cnt; ++k) {
+				if (cref[k] & kLeafFlag) continue;
+				const float a = box_area(cb[k].lo, cb[k].hi);
+				if (a > best_a) {
+					best_a = a;
+					best = k;
+				}
+			}
+			if (best < 0) break;
+			const uint32_t b = cref[best];
+			cref[best] = bchild[2 * b];
+			cref[cnt] = bchild[2 * b + 1];
+			load_ref_box(cref[best], sorted, plo, phi, bn_lo, bn_hi, cb[best]);
+			load_ref_box(cref[cnt], sorted, plo, phi, bn_lo, bn_hi, cb[cnt]);
+			++cnt;
+		}
+		// Child ranges and node bounds
+		uint32_t cfirst[8], ccount[8];
+		float3 nlo = cb[0].lo, nhi = cb[0].hi;
+		uint32_t n_int = 0, n_tri = 0;
+		for (int k = 0; k < cnt; ++k) {
+			if (cref[k] & kLeafFlag) {
+				cfirst[k] = cref[k] & ~kLeafFlag;
+				ccount[k] = 1;
+			} else {
+				const uint2 rg = brange[cref[k]];
+				cfirst[k] = rg.x;
+				ccount[k] = rg.y - rg.x + 1;
+			}
+			if (ccount[k] > leaf_max) ++n_int;
+			else n_tri += ccount[k];
+			nlo = make_float3(fminf(nlo.x, cb[k].lo.x), fminf(nlo.y, cb[k].lo.y), fminf(nlo.z, cb[k].lo.z));
+			nhi = make_float3(fmaxf(nhi.x, cb[k].hi.x), fmaxf(nhi.y, cb[k].hi.y), fmaxf(nhi.z, cb[k].hi.z));
+		}
+		// Slot assignment: slot s takes the child lying furthest against the
+		// direction octant s (sign bit set = negative axis), so a ray of
+		// octant o meets children roughly front to back in slot order j ^ o.
+		int slot_child[8];
+		for (int s = 0; s < 8; ++s) slot_child[s] = -1;
+		{
+			const float3 pc = make_float3(0.5f * (nlo.x + nhi.x), 0.5f * (nlo.y + nhi.y), 0.5f * (nlo.z + nhi.z));
+			float cost[8][8];
+			for (int k = 0; k < cnt; ++k) {
+				const float cx = 0.5f * (cb[k].lo.x + cb[k].hi.x) - pc.x;
+				const float cy = 0.5f * (cb[k].lo.y + cb[k].hi.y) - pc.y;
+				const float cz = 0.5f * (cb[k].lo.z + cb[k].hi.z) - pc.z;
+				for (int s = 0; s < 8; ++s)
+					cost[k][s] = ((s & 1) ? -cx : cx) + ((s & 2) ? -cy : cy) + ((s & 4) ? -cz : cz);
+			}
+			uint32_t kdone = 0, sdone = 0;
+			for (int round = 0; round < cnt; ++round) {
+				float bc = INFINITY;
+				int bk = -1, bs = -1;
+				for (int k = 0; k < cnt; ++k) {
+					if (kdone & (1u << k)) continue;
+					for (int s = 0; s < 8; ++s) {
+						if (sdone & (1u << s)) continue;
+						if (bk < 0 || cost[k][s] < bc) {
+							bc = cost[k][s];
+							bk = k;
+							bs = s;
+						}
+					}
+				}
+				kdone |= 1u << bk;
+				sdone |= 1u << bs;
+				slot_child[bs] = bk;
+			}
+		}
+		// Quantisation grid: origin = node min, per-axis power-of-two scale.
+		const uint32_t ex = quant_exponent(__fsub_ru(nhi.x, nlo.x));
+		const uint32_t ey = quant_exponent(__fsub_ru(nhi.y, nlo.y));
+		const uint32_t ez = quant_exponent(__fsub_ru(nhi.z, nlo.z));
+		const float ix = __uint_as_float((254u - ex) << 23);
+		const float iy = __uint_as_float((254u - ey) << 23);
+		const float iz = __uint_as_float((254u - ez) << 23);
+
+		const uint32_t child_base = n_int ? atomicAdd(&counters[C_NODES], n_int) : 0u;
+		const uint32_t tri_base = n_tri ? atomicAdd(&counters[C_TRIS], n_tri) : 0u;
+
+		uint32_t imask = 0, int_rank = 0, tri_off = 0;
+		uint32_t meta[2] = {0, 0}, qlx[2] = {0, 0}, qly[2] = {0, 0}, qlz[2] = {0, 0};
+		uint32_t qhx[2] = {0, 0}, qhy[2] = {0, 0}, qhz[2] = {0, 0};
+		for (int s = 0; s < 8; ++s) {
+			const int k = slot_child[s];
+			if (k < 0) continue;
+			auto qlo = [](float v, float org, float inv) {
+				const float q = floorf(__fmul_rd(__fsub_rd(v, org), inv));
+				return (uint32_t)fminf(fmaxf(q, 0.f), 255.f);
+			};
+			auto qhi = [](float v, float org, float inv) {
+				const float q = ceilf(__fmul_ru(__fsub_ru(v, org), inv));
+				return (uint32_t)fminf(fmaxf(q, 0.f), 255.f);
+			};
+			const int wsel = s >> 2, sh = (s & 3) * 8;
+			qlx[wsel] |= qlo(cb[k].lo.x, nlo.x, ix) << sh;
+			qly[wsel] |= qlo(cb[k].lo.y, nlo.y, iy) << sh;
+			qlz[wsel] |= qlo(cb[k].lo.z, nlo.z, iz) << sh;
+			qhx[wsel] |= qhi(cb[k].hi.x, nlo.x, ix) << sh;
+			qhy[wsel] |= qhi(cb[k].hi.y, nlo.y, iy) << sh;
+			qhz[wsel] |= qhi(cb[k].hi.z, nlo.z, iz) << sh;
+			if (ccount[k] > leaf_max) {
+				imask |= 1u << s;
+				meta[wsel] |= kInternalMeta << sh;
+				const uint32_t slot = atomicAdd(n_out, 1u);
+				out_items[slot] = make_uint2(cref[k], child_base + int_rank);
+				++int_rank;
+			} else {
+				const uint32_t m = (((1u << ccount[k]) - 1u) << 5) | tri_off;
+				meta[wsel] |= m << sh;
+				for (uint32_t j = 0; j < ccount[k]; ++j)
+					prim_order[tri_base + tri_off + j] = sorted[cfirst[k] + j];
+				tri_off += ccount[k];
+			}
+		}
+		WideNode nd;
+		nd.w[0] = make_uint4(__float_as_uint(nlo.x), __float_as_uint(nlo.y), __float_as_uint(nlo.z),
+				ex | (ey << 8) | (ez << 16) | (imask << 24));
+		nd.w[1] = make_uint4(child_base, tri_base, meta[0], meta[1]);
+		nd.w[2] = make_uint4(qlx[0], qlx[1], qly[0], qly[1]);
+		nd.w[3] = make_uint4(qlz[0], qlz[1], qhx[0], qhx[1]);
+		nd.w[4] = make_uint4(qhy[0], qhy[1], qhz[0], qhz[1]);
+		wnodes[item.y] = nd;
+	}
+}
+
+__global__ void k_init_collapse(uint2 *queue, uint32_t *counters) {
+	queue[0] = make_uint2(counters[C_ROOT], 0u);
+	counters[C_QA] = 1u;
+	counters[C_QB] = 0u;
+	counters[C_NODES] = 1u;
+	counters[C_TRIS] = 0u;
+}
+
+__global__ void k_init_counters(uint32_t *counters) {
+	const int i = threadIdx.x;
+	if (i < C_COUNT) {
+		uint32_t v = 0u;
+		if (i >= C_BMIN && i < C_BMIN + 3) v = 0xffffffffu;
+		if (i >= C_BMAX && i < C_BMAX + 3) v = 0u;
+		counters[i] = v;
+	}
+}
+
+// ---------------------------------------------------------------------------
+// Host orchestration
+// ---------------------------------------------------------------------------
+
+static inline uint32_t blocks_for(uint64_t n, uint32_t bs) { return (uint32_t)((n + bs - 1) / bs); }
+
+lrx_status build_wide_bvh(uint32_t n, const float4 *d_lo, const float4 *d_hi, uint32_t leaf_max,
+		uint32_t treelet_passes, cudaStream_t st, BuildScratch &S, BvhResult *out) {
+	*out = BvhResult();
+	if (n == 0) return LRX_OK;
+	if (leaf_max < 1) leaf_max = 1;
+	if (leaf_max > 3) leaf_max = 3;
+	lrx_status rc;
+	const uint32_t ni = n > 1 ? n - 1 : 1;
+	if ((rc = S.keys.alloc(sizeof(uint64_t) * n)) != LRX_OK) return rc;
+	if ((rc = S.keys_alt.alloc(sizeof(uint64_t) * n)) != LRX_OK) return rc;
+	if ((rc = S.vals.alloc(sizeof(uint32_t) * n)) != LRX_OK) return rc;
+	if ((rc = S.vals_alt.alloc(sizeof(uint32_t) * n)) != LRX_OK) return rc;
+	if ((rc = S.bnodes.alloc((sizeof(float4) * 2 + sizeof(uint32_t) * 2) * ni)) != LRX_OK) return rc;
+	if ((rc = S.branges.alloc(sizeof(uint2) * ni)) != LRX_OK) return rc;
+	if ((rc = S.other_bound.alloc(sizeof(uint32_t) * ni)) != LRX_OK) return rc;
+	if ((rc = S.wide_nodes.alloc(sizeof(WideNode) * (size_t)n)) != LRX_OK) return rc;
+	if ((rc = S.prim_order.alloc(sizeof(uint32_t) * n)) != LRX_OK) return rc;
+	if ((rc = S.queue_a.alloc(sizeof(uint2) * n)) != LRX_OK) return rc;
+	if ((rc = S.queue_b.alloc(sizeof(uint2) * n)) != LRX_OK) return rc;
+	if ((rc = S.counters.alloc(sizeof(uint32_t) * 64)) != LRX_OK) return rc;
+
+	uint32_t *counters = S.counters.as<uint32_t>();
+	float4 *bn_lo = S.bnodes.as<float4>();
+	float4 *bn_hi = bn_lo + ni;
+	uint32_t *bchild = reinterpret_cast<uint32_t *>(bn_hi + ni);
+	uint2 *brange = S.branges.as<uint2>();
+
+	k_init_counters<<<1, 32, 0, st>>>(counters);
+	k_centroid_bounds<<<std::min(blocks_for(n, 256), 1024u), 256, 0, st>>>(n, d_lo, d_hi, counters);
+	k_morton<<<blocks_for(n, 256), 256, 0, st>>>(n, d_lo, d_hi, counters, S.keys.as<uint64_t>(), S.vals.as<uint32_t>());
+	LRX_CUDA(cudaGetLastError());
+
+	cub::DoubleBuffer<uint64_t> dk(S.keys.as<uint64_t>(), S.keys_alt.as<uint64_t>());
+	cub::DoubleBuffer<uint32_t> dv(S.vals.as<uint32_t>(), S.vals_alt.as<uint32_t>());
+	size_t temp_bytes = 0;
+	LRX_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, temp_bytes, dk, dv, (int)n, 0, 63, st));
+	if ((rc = S.cub_temp.alloc(temp_bytes)) != LRX_OK) return rc;
+	LRX_CUDA(cub::DeviceRadixSort::SortPairs(S.cub_temp.ptr, temp_bytes, dk, dv, (int)n, 0, 63, st));
+	const uint64_t *keys = dk.Current();
+	const uint32_t *sorted = dv.Current();
+
+	LRX_CUDA(cudaMemsetAsync(S.other_bound.ptr, 0xff, sizeof(uint32_t) * ni, st));
+	k_hierarchy<<<blocks_for(n, 128), 128, 0, st>>>(n, keys, sorted, d_lo, d_hi, bchild, bn_lo, bn_hi, brange,
+			S.other_bound.as<uint32_t>(), counters);
+	LRX_CUDA(cudaGetLastError());
+
+	(void)treelet_passes;
+
+	// Level-synchronous collapse
+	k_init_collapse<<<1, 1, 0, st>>>(S.queue_a.as<uint2>(), counters);
+	LRX_CUDA(cudaGetLastError());
+	uint2 *qin = S.queue_a.as<uint2>(), *qout = S.queue_b.as<uint2>();
+	int cin = C_QA, cout = C_QB;
+	uint32_t depth = 0;
+	for (;;) {
+		uint32_t n_in = 0;
+		LRX_CUDA(cudaMemcpyAsync(&n_in, counters + cin, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+		LRX_CUDA(cudaStreamSynchronize(st));
+		if (n_in == 0) break;
+		++depth;
+		if (depth > (uint32_t)kMaxTreeDepth) {
+			set_error("BVH deeper than the traversal stack allows");
+			return LRX_ERR_BUILD;
+		}
+		LRX_CUDA(cudaMemsetAsync(counters + cout, 0, sizeof(uint32_t), st));
+		k_collapse<<<std::min(blocks_for(n_in, 128), 152u * 16u), 128, 0, st>>>(qin, counters + cin, qout,
+				counters + cout, bchild, bn_lo, bn_hi, brange, sorted, d_lo, d_hi, leaf_max,
+				S.wide_nodes.as<WideNode>(), S.prim_order.as<uint32_t>(), counters);
+		LRX_CUDA(cudaGetLastError());
+		std::swap(qin, qout);
+		std::swap(cin, cout);
+	}
+	uint32_t host_counters[C_COUNT];
+	LRX_CUDA(cudaMemcpyAsync(host_counters, counters, sizeof(host_counters), cudaMemcpyDeviceToHost, st));
+	LRX_CUDA(cudaStreamSynchronize(st));
+	if (host_counters[C_TRIS] != n) {
+		set_error("BVH collapse lost primitives");
+		return LRX_ERR_BUILD;
+	}
+	out->node_count = host_counters[C_NODES];
+	out->depth = depth;
+	std::memcpy(out->lo, &host_counters[C_BOX], 3 * sizeof(float));
+	std::memcpy(out->hi, &host_counters[C_BOX + 3], 3 * sizeof(float));
+	return LRX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Scene assembly kernels
+// ---------------------------------------------------------------------------
+
+__global__ void k_triangle_boxes(uint32_t n, const float *__restrict__ v, const uint32_t *__restrict__ idx,
+		float4 *__restrict__ lo, float4 *__restrict__ hi) {
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	const uint32_t a = idx[3 * i], b = idx[3 * i + 1], c = idx[3 * i + 2];
+	const float3 p0 = make_float3(v[3 * a], v[3 * a + 1], v[3 * a + 2]);
+	const float3 p1 = make_float3(v[3 * b], v[3 * b + 1], v[3 * b + 2]);
+	const float3 p2 = make_float3(v[3 * c], v[3 * c + 1], v[3 * c + 2]);
+	float3 mn = make_float3(fminf(fminf(p0.x, p1.x), p2.x), fminf(fminf(p0.y, p1.y), p2.y), fminf(fminf(p0.z, p1.z), p2.z));
+	float3 mx = make_float3(fmaxf(fmaxf(p0.x, p1.x), p2.x), fmaxf(fmaxf(p0.y, p1.y), p2.y), fmaxf(fmaxf(p0.z, p1.z), p2.z));
+	// BVHAccel::Init leaf box: Expand(MachineEpsilon::E(bbox)) (bvhaccel.cpp:116-122)
+	const float e = fmaxf(fmaxf(machine_eps(mn.x), fmaxf(machine_eps(mn.y), machine_eps(mn.z))),
+			fmaxf(machine_eps(mx.x), fmaxf(machine_eps(mx.y), machine_eps(mx.z))));
+	lo[i] = make_float4(__fsub_rd(mn.x, e), __fsub_rd(mn.y, e), __fsub_rd(mn.z, e), 0.f);
+	hi[i] = make_float4(__fadd_ru(mx.x, e), __fadd_ru(mx.y, e), __fadd_ru(mx.z, e), 0.f);
+}
+
+lrx_status launch_triangle_boxes(uint32_t n_tris, const float *d_verts, const uint32_t *d_idx, float4 *d_lo,
+		float4 *d_hi, cudaStream_t st) {
+	if (!n_tris) return LRX_OK;
+	k_triangle_boxes<<<blocks_for(n_tris, 256), 256, 0, st>>>(n_tris, d_verts, d_idx, d_lo, d_hi);
+	LRX_CUDA(cudaGetLastError());
+	return LRX_OK;
+}
+
+__global__ void k_relocate(const WideNode *__restrict__ src, WideNode *__restrict__ dst, uint32_t n,
+		uint32_t node_off, uint32_t tri_off) {
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	WideNode nd = src[i];
+	nd.w[1].x += node_off;
+	nd.w[1].y += tri_off;
+	dst[i] = nd;
+}
+
+lrx_status launch_relocate_nodes(const WideNode *src, WideNode *dst, uint32_t n, uint32_t node_offset,
+		uint32_t tri_offset, cudaStream_t st) {
+	if (!n) return LRX_OK;
+	k_relocate<<<blocks_for(n, 256), 256, 0, st>>>(src, dst, n, node_offset, tri_offset);
+	LRX_CUDA(cudaGetLastError());
+	return LRX_OK;
+}
+
+__global__ void k_triangle_records(uint32_t n, const uint32_t *__restrict__ order, const float *__restrict__ v,
+		const uint32_t *__restrict__ idx, const uint32_t *__restrict__ tri_object, uint32_t object_const,
+		TriRecord *__restrict__ dst) {
+	const uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+	if (k >= n) return;
+	const uint32_t t = order[k];
+	const uint32_t a = idx[3 * t], b = idx[3 * t + 1], c = idx[3 * t + 2];
+	const float3 p0 = make_float3(v[3 * a], v[3 * a + 1], v[3 * a + 2]);
+	const float3 p1 = make_float3(v[3 * b], v[3 * b + 1], v[3 * b + 2]);
+	const float3 p2 = make_float3(v[3 * c], v[3 * c + 1], v[3 * c + 2]);
+	const float3 e1 = rn_sub(p1, p0), e2 = rn_sub(p2, p0);
+	uint32_t obj = object_const, tri = t;
+	if (tri_object) {
+		obj = tri_object[2 * t];
+		tri = tri_object[2 * t + 1];
+	}
+	TriRecord r;
+	r.a = make_float4(p0.x, p0.y, p0.z, __uint_as_float(tri));
+	r.b = make_float4(e1.x, e1.y, e1.z, __uint_as_float(obj));
+	r.c = make_float4(e2.x, e2.y, e2.z, 0.f);
+	dst[k] = r;
+}
+
+lrx_status launch_triangle_records(uint32_t n_tris, const uint32_t *d_prim_order, const float *d_verts,
+		const uint32_t *d_idx, const uint32_t *d_tri_object, uint32_t object_const, TriRecord *dst, cudaStream_t st) {
+	if (!n_tris) return LRX_OK;
+	k_triangle_records<<<blocks_for(n_tris, 256), 256, 0, st>>>(n_tris, d_prim_order, d_verts, d_idx, d_tri_object,
+			object_const, dst);
+	LRX_CUDA(cudaGetLastError());
+	return LRX_OK;
+}
+
+}  // namespace lrx

@@ -1,0 +1,114 @@
+// Host-side internals shared by the C-ABI layer, the builder and the
+// traversal launchers.  Not part of the public ABI.
+#pragma once
+
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/lrx.h"
+
+namespace lrx {
+
+struct WideNode;
+struct TriRecord;
+struct InstRecord;
+
+// Error reporting: the thread-local message behind lrx_last_error().
+void set_error(const std::string &msg);
+lrx_status cuda_fail(cudaError_t e, const char *what);
+
+#define LRX_CUDA(call)                                                         \
+	do {                                                                       \
+		cudaError_t _e = (call);                                               \
+		if (_e != cudaSuccess) return ::lrx::cuda_fail(_e, #call);             \
+	} while (0)
+
+// Device buffer owned by the library (freed on destruction).
+struct DevBuf {
+	void *ptr = nullptr;
+	size_t bytes = 0;
+	DevBuf() = default;
+	DevBuf(const DevBuf &) = delete;
+	DevBuf &operator=(const DevBuf &) = delete;
+	DevBuf(DevBuf &&o) noexcept : ptr(o.ptr), bytes(o.bytes) {
+		o.ptr = nullptr;
+		o.bytes = 0;
+	}
+	DevBuf &operator=(DevBuf &&o) noexcept {
+		if (this != &o) {
+			release();
+			ptr = o.ptr;
+			bytes = o.bytes;
+			o.ptr = nullptr;
+			o.bytes = 0;
+		}
+		return *this;
+	}
+	~DevBuf() { release(); }
+	lrx_status alloc(size_t n);   // no-op if already >= n
+	void release();
+	template <class T> T *as() const { return static_cast<T *>(ptr); }
+};
+
+// Scratch memory for one BVH build (grown on demand, reused across builds).
+struct BuildScratch {
+	DevBuf keys, keys_alt, vals, vals_alt, cub_temp;
+	DevBuf bnodes, branges, other_bound;
+	DevBuf wide_nodes, prim_order;
+	DevBuf queue_a, queue_b;
+	DevBuf counters;   // uint32 counters + bounds (small)
+	DevBuf treelet_scratch;
+};
+
+struct BvhResult {
+	uint32_t node_count = 0;  // wide nodes written to scratch.wide_nodes
+	uint32_t depth = 0;       // wide-node levels
+	float lo[3] = {0, 0, 0};  // root box (union of the padded primitive boxes)
+	float hi[3] = {0, 0, 0};
+};
+
+// Builds an 8-wide compressed BVH over n primitive boxes (lo/hi as float4,
+// xyz used).  On return scratch.wide_nodes holds node_count nodes whose
+// child_base / tri_base are relative to 0, and scratch.prim_order holds the
+// n primitive indices in leaf order.  Synchronises `stream`.
+lrx_status build_wide_bvh(uint32_t n, const float4 *d_lo, const float4 *d_hi,
+		uint32_t leaf_max, uint32_t treelet_passes, cudaStream_t stream,
+		BuildScratch &scratch, BvhResult *out);
+
+// Per-triangle padded boxes (Union(BBox(p0,p1),p2) expanded by
+// MachineEpsilon::E, bvhaccel.cpp:116-122) for one mesh.
+lrx_status launch_triangle_boxes(uint32_t n_tris, const float *d_verts, const uint32_t *d_idx,
+		float4 *d_lo, float4 *d_hi, cudaStream_t stream);
+
+// Copies nodes into the scene array, offsetting child/tri bases.
+lrx_status launch_relocate_nodes(const WideNode *src, WideNode *dst, uint32_t n,
+		uint32_t node_offset, uint32_t tri_offset, cudaStream_t stream);
+
+// Writes triangle records for one mesh in leaf order.  d_tri_object, when
+// not null, holds (object index, triangle index) per triangle of a merged
+// mesh; otherwise every record gets object_const and its own index.
+lrx_status launch_triangle_records(uint32_t n_tris, const uint32_t *d_prim_order,
+		const float *d_verts, const uint32_t *d_idx, const uint32_t *d_tri_object,
+		uint32_t object_const, TriRecord *dst, cudaStream_t stream);
+
+struct TraceArgs {
+	const WideNode *nodes;
+	const TriRecord *tris;
+	const InstRecord *insts;
+	uint32_t root;          // root node of the flat BVH or of the TLAS; kNull = empty
+	uint32_t two_level;
+	const void *rays;
+	void *hits;
+	uint32_t count;
+	uint32_t any_hit;
+	uint32_t *status;
+	unsigned long long *counters;  // nullptr unless counting
+};
+
+lrx_status launch_trace(const TraceArgs &a, cudaStream_t stream);
+
+}  // namespace lrx

@@ -1,0 +1,272 @@
+// Ray traversal kernels: closest-hit and any-hit queries of luxrays::Ray
+// buffers against the 8-wide compressed BVH, flat (one BVH over all plain
+// meshes) or two-level (top-level BVH over objects, each leaf an instance
+// record with the world->local transform of an instanced mesh).
+//
+// Replaces the reference's GPU kernels Accelerator_Intersect_RayBuffer of
+// include/luxrays/accelerators/bvh.cl:45-260 and mbvh.cl:61-383 and the CPU
+// walks BVHAccel::Intersect / MBVHAccel::Intersect
+// (src/luxrays/accelerators/bvhaccel.cpp:170-260, mbvhaccel.cpp:252-357).
+// Results follow the CPU semantics: closest hit with t in [mint, maxt] from
+// the same FP32 Triangle::Intersect; at equal t the lowest
+// (meshIndex, triangleIndex) wins, so the answer does not depend on the
+// traversal order.  Masked rays are skipped without writing (bvh.cl:243-244);
+// rays with a NaN or infinite origin/direction component, or a NaN maxt,
+// are misses.
+#include "lrx_common.cuh"
+#include "lrx_internal.h"
+
+namespace lrx {
+
+struct ActiveRay {
+	float3 o, d, idir;
+	uint32_t oct;
+};
+
+__device__ __forceinline__ void make_active(ActiveRay &r, float3 o, float3 d) {
+	r.o = o;
+	r.d = d;
+	r.idir = make_float3(__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z));
+	r.oct = (r.idir.x < 0.f ? 1u : 0u) | (r.idir.y < 0.f ? 2u : 0u) | (r.idir.z < 0.f ? 4u : 0u);
+}
+
+__device__ __forceinline__ float u8_to_float(uint32_t b) {
+	return __uint_as_float(0x4B000000u | b) - 8388608.f;  // exact for b < 2^23
+}
+
+struct NodeHits {
+	uint32_t child_base, tri_base, imask;
+	uint32_t ihits;  // internal children, bit j = slot (j ^ oct)
+	uint32_t tmask;  // leaf triangles, bit k = triangle tri_base + k
+};
+
+// Slab test of the 8 quantised child boxes.  t = q * (scale * idir) +
+// (origin - o) * idir; NaN plane distances (zero direction components) are
+// dropped by fminf/fmaxf, which only ever keeps a child.
+__device__ __forceinline__ NodeHits intersect_node(const WideNode *__restrict__ nodes, uint32_t idx,
+		const ActiveRay &r, float tmin, float tmax) {
+	const uint4 *p = reinterpret_cast<const uint4 *>(nodes + idx);
+	const uint4 w0 = __ldg(p), w1 = __ldg(p + 1), w2 = __ldg(p + 2), w3 = __ldg(p + 3), w4 = __ldg(p + 4);
+	NodeHits h;
+	h.child_base = w1.x;
+	h.tri_base = w1.y;
+	h.imask = w0.w >> 24;
+	const float sx = __uint_as_float((w0.w & 0xffu) << 23);
+	const float sy = __uint_as_float(((w0.w >> 8) & 0xffu) << 23);
+	const float sz = __uint_as_float(((w0.w >> 16) & 0xffu) << 23);
+	const float ax = sx * r.idir.x, ay = sy * r.idir.y, az = sz * r.idir.z;
+	const float bx = (__uint_as_float(w0.x) - r.o.x) * r.idir.x;
+	const float by = (__uint_as_float(w0.y) - r.o.y) * r.idir.y;
+	const float bz = (__uint_as_float(w0.z) - r.o.z) * r.idir.z;
+	const bool px = r.idir.x >= 0.f, py = r.idir.y >= 0.f, pz = r.idir.z >= 0.f;
+	// qlo_x = w2.xy, qlo_y = w2.zw, qlo_z = w3.xy, qhi_x = w3.zw, qhi_y = w4.xy, qhi_z = w4.zw
+	const uint32_t nx0 = px ? w2.x : w3.z, nx1 = px ? w2.y : w3.w;
+	const uint32_t fx0 = px ? w3.z : w2.x, fx1 = px ? w3.w : w2.y;
+	const uint32_t ny0 = py ? w2.z : w4.x, ny1 = py ? w2.w : w4.y;
+	const uint32_t fy0 = py ? w4.x : w2.z, fy1 = py ? w4.y : w2.w;
+	const uint32_t nz0 = pz ? w3.x : w4.z, nz1 = pz ? w3.y : w4.w;
+	const uint32_t fz0 = pz ? w4.z : w3.x, fz1 = pz ? w4.w : w3.y;
+	uint32_t ih = 0, tm = 0;
+#pragma unroll
+	for (int s = 0; s < 8; ++s) {
+		const int sh = (s & 3) * 8;
+		const uint32_t nxw = s < 4 ? nx0 : nx1, fxw = s < 4 ? fx0 : fx1;
+		const uint32_t nyw = s < 4 ? ny0 : ny1, fyw = s < 4 ? fy0 : fy1;
+		const uint32_t nzw = s < 4 ? nz0 : nz1, fzw = s < 4 ? fz0 : fz1;
+		const uint32_t mw = s < 4 ? w1.z : w1.w;
+		const float tnx = fmaf(u8_to_float((nxw >> sh) & 0xffu), ax, bx);
+		const float tny = fmaf(u8_to_float((nyw >> sh) & 0xffu), ay, by);
+		const float tnz = fmaf(u8_to_float((nzw >> sh) & 0xffu), az, bz);
+		const float tfx = fmaf(u8_to_float((fxw >> sh) & 0xffu), ax, bx);
+		const float tfy = fmaf(u8_to_float((fyw >> sh) & 0xffu), ay, by);
+		const float tfz = fmaf(u8_to_float((fzw >> sh) & 0xffu), az, bz);
+		const float tn = fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin));
+		const float tf = fminf(fminf(tfx, tfy), fminf(tfz, tmax));
+		const uint32_t m = (mw >> sh) & 0xffu;
+		if (tn <= tf && m != 0u) {
+			if (h.imask & (1u << s)) ih |= 1u << (s ^ r.oct);
+			else tm |= ((m >> 5) & 7u) << (m & 31u);
+		}
+	}
+	h.ihits = ih;
+	h.tmask = tm;
+	return h;
+}
+
+__device__ __forceinline__ bool finite3(float3 v) {
+	return isfinite(v.x) && isfinite(v.y) && isfinite(v.z);
+}
+
+template <bool ANY, bool TWO_LEVEL, bool COUNT>
+__global__ void __launch_bounds__(128) k_trace(TraceArgs a) {
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (!COUNT && i >= a.count) return;
+	float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0, r2 = r0;
+	bool active = i < a.count;
+	if (active) {
+		const float4 *rp = reinterpret_cast<const float4 *>(a.rays) + 3 * (size_t)i;
+		r0 = __ldg(rp);
+		r1 = __ldg(rp + 1);
+		r2 = __ldg(rp + 2);
+		if (__float_as_uint(r2.y) & LRX_RAY_FLAGS_MASKED) active = false;  // bvh.cl:243-244
+	}
+	if (!COUNT && !active) return;
+
+	const float3 wo = make_float3(r0.x, r0.y, r0.z);
+	const float3 wd = make_float3(r0.w, r1.x, r1.y);
+	const float mint = r1.z, maxt = r1.w;
+
+	float best_t = maxt, best_b1 = 0.f, best_b2 = 0.f;
+	uint32_t best_mesh = kNull, best_tri = kNull;
+	uint32_t n_nodes = 0, n_tris = 0, n_insts = 0;
+
+	if (active && a.root != kNull && finite3(wo) && finite3(wd) && !isnan(maxt)) {
+		ActiveRay ray;
+		make_active(ray, wo, wd);
+		uint2 stack[kStackSize];
+		int sp = 0;
+		int inst_sp = -1;
+		uint32_t inst_obj = kNull;
+		uint2 cur = make_uint2(a.root, (1u << (24 + ray.oct)) | 1u);
+		bool done = false;
+		uint32_t visits = 0;
+		while (!done) {
+			if (TWO_LEVEL && (cur.y & kInstGroup)) {
+				const uint32_t k = __ffs(cur.y & 0xffu) - 1;
+				cur.y &= ~(1u << k);
+				if (cur.y & 0xffu) {
+					if (sp >= kStackSize) {
+						atomicOr(a.status, kStatusStackOverflow);
+						break;
+					}
+					stack[sp++] = cur;
+				}
+				const InstRecord *ir = a.insts + cur.x + k;
+				const uint4 info = __ldg(reinterpret_cast<const uint4 *>(&ir->info));
+				if (COUNT) ++n_insts;
+				inst_obj = info.y;
+				if (info.z & kInstIdentity) {
+					make_active(ray, wo, wd);
+				} else {
+					const float4 m0 = __ldg(&ir->r0), m1 = __ldg(&ir->r1), m2 = __ldg(&ir->r2), m3 = __ldg(&ir->r3);
+					make_active(ray, xform_point(m0, m1, m2, m3, wo), xform_vector(m0, m1, m2, wd));
+				}
+				inst_sp = sp;
+				cur = info.x == kNull ? make_uint2(0u, 0u) : make_uint2(info.x, (1u << (24 + ray.oct)) | 1u);
+				continue;
+			}
+			if ((cur.y >> 24) == 0u) {
+				if (TWO_LEVEL && inst_sp == sp) {  // leaving the instance
+					inst_sp = -1;
+					inst_obj = kNull;
+					make_active(ray, wo, wd);
+				}
+				if (sp == 0) break;
+				cur = stack[--sp];
+				continue;
+			}
+			const uint32_t j = __ffs(cur.y >> 24) - 1;
+			cur.y &= ~(1u << (24 + j));
+			const uint32_t s = j ^ ray.oct;
+			const uint32_t node = cur.x + __popc(cur.y & ((1u << s) - 1u) & 0xffu);
+			if (cur.y >> 24) {
+				if (sp >= kStackSize) {
+					atomicOr(a.status, kStatusStackOverflow);
+					break;
+				}
+				stack[sp++] = cur;
+			}
+			if (++visits > kMaxVisits) {
+				atomicOr(a.status, kStatusVisitLimit);
+				break;
+			}
+			if (COUNT) ++n_nodes;
+			const NodeHits h = intersect_node(a.nodes, node, ray, mint, best_t);
+			cur = make_uint2(h.child_base, (h.ihits << 24) | h.imask);
+			if (h.tmask) {
+				if (TWO_LEVEL && inst_sp < 0) {
+					// top-level leaves: instances, entered one at a time
+					if (cur.y >> 24) {
+						if (sp >= kStackSize) {
+							atomicOr(a.status, kStatusStackOverflow);
+							break;
+						}
+						stack[sp++] = cur;
+					}
+					cur = make_uint2(h.tri_base, kInstGroup | h.tmask);
+					continue;
+				}
+				uint32_t tm = h.tmask;
+				while (tm) {
+					const uint32_t k = __ffs(tm) - 1;
+					tm &= tm - 1;
+					const float4 *tp = reinterpret_cast<const float4 *>(a.tris + h.tri_base + k);
+					const float4 ta = __ldg(tp), tb = __ldg(tp + 1), tc = __ldg(tp + 2);
+					if (COUNT) ++n_tris;
+					float t, b1, b2;
+					if (tri_intersect(ray.o, ray.d, mint, best_t, make_float3(ta.x, ta.y, ta.z),
+							make_float3(tb.x, tb.y, tb.z), make_float3(tc.x, tc.y, tc.z), t, b1, b2)) {
+						const uint32_t tri = __float_as_uint(ta.w);
+						uint32_t mesh = __float_as_uint(tb.w);
+						if (TWO_LEVEL && mesh == kNull) mesh = inst_obj;
+						if (ANY || t < best_t || mesh < best_mesh || (mesh == best_mesh && tri < best_tri)) {
+							best_t = t;
+							best_b1 = b1;
+							best_b2 = b2;
+							best_mesh = mesh;
+							best_tri = tri;
+							if (ANY) {
+								done = true;
+								break;
+							}
+						}
+					}
+				}
+			}
+		}
+	}
+	if (active) {
+		uint32_t *hp = reinterpret_cast<uint32_t *>(a.hits) + 5 * (size_t)i;
+		hp[0] = __float_as_uint(best_t);
+		hp[1] = __float_as_uint(best_b1);
+		hp[2] = __float_as_uint(best_b2);
+		hp[3] = best_mesh;
+		hp[4] = best_tri;
+	}
+
+	if (COUNT) {
+		// every lane of the warp reaches this point in the counting variant
+		unsigned long long v[4] = {n_nodes, n_tris, n_insts, active ? 1ull : 0ull};
+#pragma unroll
+		for (int k = 0; k < 4; ++k) {
+			unsigned long long x = v[k];
+#pragma unroll
+			for (int off = 16; off > 0; off >>= 1) x += __shfl_xor_sync(0xffffffffu, x, off);
+			v[k] = x;
+		}
+		if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+			for (int k = 0; k < 4; ++k) atomicAdd(&a.counters[k], v[k]);
+		}
+	}
+}
+
+lrx_status launch_trace(const TraceArgs &a, cudaStream_t st) {
+	if (a.count == 0) return LRX_OK;
+	const uint32_t bs = 128;
+	const uint32_t grid = (a.count + bs - 1) / bs;
+	const bool cnt = a.counters != nullptr;
+#define LRX_LAUNCH(A, T, C) k_trace<A, T, C><<<grid, bs, 0, st>>>(a)
+	if (a.any_hit) {
+		if (a.two_level) { if (cnt) LRX_LAUNCH(true, true, true); else LRX_LAUNCH(true, true, false); }
+		else { if (cnt) LRX_LAUNCH(true, false, true); else LRX_LAUNCH(true, false, false); }
+	} else {
+		if (a.two_level) { if (cnt) LRX_LAUNCH(false, true, true); else LRX_LAUNCH(false, true, false); }
+		else { if (cnt) LRX_LAUNCH(false, false, true); else LRX_LAUNCH(false, false, false); }
+	}
+#undef LRX_LAUNCH
+	LRX_CUDA(cudaGetLastError());
+	return LRX_OK;
+}
+
+}  // namespace lrx

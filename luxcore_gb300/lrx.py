@@ -1,0 +1,200 @@
+"""ctypes binding of liblrx.so (include/lrx.h).
+
+The library is the product: this module loads it from luxcore_gb300/lib/
+and raises if it is missing -- there is no CPU fallback.  Device buffers are
+passed as raw device addresses (ints), streams as raw cudaStream_t handles;
+PyTorch, when used by callers, only provides that memory and those streams.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+from . import workloads as W
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "liblrx.so")
+
+LRX_TRACE_CLOSEST = 0
+LRX_TRACE_ANY = 1
+LRX_OBJECT_INSTANCE = 0x1
+LRX_OBJECT_HAS_INVERSE = 0x2
+
+STATUS_NAMES = {0: "LRX_OK", 1: "LRX_ERR_INVALID_ARGUMENT", 2: "LRX_ERR_CUDA", 3: "LRX_ERR_OUT_OF_MEMORY",
+                4: "LRX_ERR_BUILD", 5: "LRX_ERR_DEVICE", 6: "LRX_ERR_NOT_SUPPORTED", 7: "LRX_ERR_BUDGET",
+                8: "LRX_ERR_BUSY", 9: "LRX_ERR_TIMEOUT"}
+
+# Every function include/lrx.h declares (checked by the CPU tests).
+EXPORTED = ["lrx_abi_version", "lrx_last_error", "lrx_scene_create", "lrx_scene_destroy",
+            "lrx_scene_update_instances", "lrx_scene_get_info", "lrx_trace", "lrx_trace_host",
+            "lrx_trace_counted", "lrx_scene_device_status"]
+
+
+class LrxError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+class MeshDesc(ctypes.Structure):
+    _fields_ = [("vertices", ctypes.c_void_p), ("triangles", ctypes.c_void_p),
+                ("vertex_count", ctypes.c_uint32), ("triangle_count", ctypes.c_uint32)]
+
+
+class ObjectDesc(ctypes.Structure):
+    _fields_ = [("mesh", ctypes.c_uint32), ("flags", ctypes.c_uint32),
+                ("transform", ctypes.c_float * 16), ("inverse", ctypes.c_float * 16)]
+
+
+class BuildOpts(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_uint32), ("leaf_max", ctypes.c_uint32),
+                ("treelet_passes", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class SceneInfo(ctypes.Structure):
+    _fields_ = [("triangle_count", ctypes.c_uint64), ("unique_triangle_count", ctypes.c_uint64),
+                ("object_count", ctypes.c_uint32), ("instance_count", ctypes.c_uint32),
+                ("blas_count", ctypes.c_uint32), ("two_level", ctypes.c_uint32),
+                ("node_count", ctypes.c_uint64), ("device_bytes", ctypes.c_uint64),
+                ("max_depth", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("build_ms", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def load(path: str | None = None):
+    """Loads liblrx.so; raises if it has not been built."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise RuntimeError(f"liblrx.so not found at {p}: run luxcore_gb300/build.py "
+                               "(there is no CPU fallback)")
+        L = ctypes.CDLL(p)
+        vp, u32, u64 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64
+        st = ctypes.c_int
+        L.lrx_abi_version.restype = u32
+        L.lrx_last_error.restype = ctypes.c_char_p
+        L.lrx_scene_create.restype = st
+        L.lrx_scene_create.argtypes = [vp, u32, vp, u32, vp, vp, ctypes.POINTER(vp)]
+        L.lrx_scene_destroy.restype = st
+        L.lrx_scene_destroy.argtypes = [vp]
+        L.lrx_scene_update_instances.restype = st
+        L.lrx_scene_update_instances.argtypes = [vp, vp, u32, vp]
+        L.lrx_scene_get_info.restype = st
+        L.lrx_scene_get_info.argtypes = [vp, ctypes.POINTER(SceneInfo)]
+        L.lrx_trace.restype = st
+        L.lrx_trace.argtypes = [vp, vp, vp, u32, u32, vp]
+        L.lrx_trace_host.restype = st
+        L.lrx_trace_host.argtypes = [vp, vp, vp, u32, u32, vp]
+        L.lrx_trace_counted.restype = st
+        L.lrx_trace_counted.argtypes = [vp, vp, vp, u32, u32, vp, vp]
+        L.lrx_scene_device_status.restype = st
+        L.lrx_scene_device_status.argtypes = [vp, ctypes.POINTER(u32), vp]
+        _lib = L
+        return L
+
+
+def check(status: int):
+    if status != 0:
+        raise LrxError(status, load().lrx_last_error().decode(errors="replace"))
+
+
+def _object_array(scene: W.SceneDesc):
+    objs = (ObjectDesc * max(1, len(scene.objects)))()
+    for i, (mi, m) in enumerate(scene.objects):
+        objs[i].mesh = mi
+        if m is not None:
+            objs[i].flags = LRX_OBJECT_INSTANCE
+            flat = np.asarray(m, np.float32).reshape(16)
+            for k in range(16):
+                objs[i].transform[k] = float(flat[k])
+    return objs
+
+
+class Scene:
+    """A device-resident scene (lrx_scene): meshes + objects of a SceneDesc."""
+
+    def __init__(self, scene: W.SceneDesc, stream: int = 0, leaf_max: int = 3, treelet_passes: int = 0):
+        L = load()
+        self._keep = []
+        meshes = (MeshDesc * max(1, len(scene.meshes)))()
+        for i, m in enumerate(scene.meshes):
+            v = np.ascontiguousarray(m.vertices, np.float32)
+            t = np.ascontiguousarray(m.triangles, np.uint32)
+            self._keep += [v, t]
+            meshes[i].vertices = v.ctypes.data
+            meshes[i].triangles = t.ctypes.data
+            meshes[i].vertex_count = v.shape[0]
+            meshes[i].triangle_count = t.shape[0]
+        objs = _object_array(scene)
+        opts = BuildOpts(ctypes.sizeof(BuildOpts), leaf_max, treelet_passes, 0)
+        h = ctypes.c_void_p()
+        check(L.lrx_scene_create(meshes, len(scene.meshes), objs, len(scene.objects), ctypes.byref(opts),
+                                 ctypes.c_void_p(stream), ctypes.byref(h)))
+        self._keep = None  # the library copied the geometry
+        self.handle = h
+        self.desc = scene
+
+    def close(self):
+        if getattr(self, "handle", None):
+            load().lrx_scene_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self) -> dict:
+        inf = SceneInfo()
+        check(load().lrx_scene_get_info(self.handle, ctypes.byref(inf)))
+        return inf.as_dict()
+
+    def update_instances(self, scene: W.SceneDesc, stream: int = 0):
+        objs = _object_array(scene)
+        check(load().lrx_scene_update_instances(self.handle, objs, len(scene.objects), ctypes.c_void_p(stream)))
+        self.desc = scene
+
+    def trace(self, d_rays: int, d_hits: int, count: int, mode: int = LRX_TRACE_CLOSEST, stream: int = 0):
+        """Device buffers (raw addresses); asynchronous on `stream`."""
+        check(load().lrx_trace(self.handle, ctypes.c_void_p(d_rays), ctypes.c_void_p(d_hits), count, mode,
+                               ctypes.c_void_p(stream)))
+
+    def trace_counted(self, d_rays: int, d_hits: int, count: int, mode: int, d_counters: int, stream: int = 0):
+        check(load().lrx_trace_counted(self.handle, ctypes.c_void_p(d_rays), ctypes.c_void_p(d_hits), count, mode,
+                                       ctypes.c_void_p(d_counters), ctypes.c_void_p(stream)))
+
+    def trace_host(self, rays: np.ndarray, hits: np.ndarray | None = None, mode: int = LRX_TRACE_CLOSEST,
+                   stream: int = 0) -> np.ndarray:
+        """Host rays in, host hits out (copies inside the call)."""
+        rays = np.ascontiguousarray(rays, W.RAY_DTYPE)
+        if hits is None:
+            hits = np.zeros(rays.shape[0], W.HIT_DTYPE)
+        check(load().lrx_trace_host(self.handle, rays.ctypes.data, hits.ctypes.data, rays.shape[0], mode,
+                                    ctypes.c_void_p(stream)))
+        return hits
+
+    def trace_host_ptr(self, h_rays: int, h_hits: int, count: int, mode: int = LRX_TRACE_CLOSEST,
+                       stream: int = 0):
+        """lrx_trace_host on raw host addresses (e.g. pinned buffers)."""
+        check(load().lrx_trace_host(self.handle, ctypes.c_void_p(h_rays), ctypes.c_void_p(h_hits), count, mode,
+                                    ctypes.c_void_p(stream)))
+
+    def device_status(self, stream: int = 0) -> int:
+        v = ctypes.c_uint32()
+        rc = load().lrx_scene_device_status(self.handle, ctypes.byref(v), ctypes.c_void_p(stream))
+        if rc not in (0, 5):
+            check(rc)
+        return v.value

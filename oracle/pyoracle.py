@@ -1,0 +1,160 @@
+"""ctypes wrapper of the CPU oracle -- TEST INFRASTRUCTURE.
+
+Only tests/, the smoke check and bench.py's CPU-baseline / reference legs
+import this module.  The oracle restates LuxRays' BVHAccel / MBVHAccel
+(src/luxrays/accelerators/bvhaccel.cpp:72-260, mbvhaccel.cpp:58-357); see
+lrx_oracle.h for the full list of restated functions.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liblrx_oracle.so")
+REF_LIB_PATH = os.path.join(HERE, "_ref", "liblrx_refcl.so")
+
+ACCEL_BVH, ACCEL_MBVH = 0, 1
+
+_lib = None
+_lock = threading.Lock()
+
+
+class OrcObject(ctypes.Structure):
+    _fields_ = [("mesh", ctypes.c_uint32), ("has_transform", ctypes.c_uint32),
+                ("m", ctypes.c_float * 16)]
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with g++ (-O2 -ffp-contract=off, no fast math)."""
+    src = os.path.join(HERE, "lrx_oracle.cpp")
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= max(
+            os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "lrx_oracle.h"))):
+        return LIB_PATH
+    os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
+    tmp = LIB_PATH + f".tmp{os.getpid()}"
+    subprocess.check_call(["g++", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+                           "-std=c++17", "-pthread", src, "-o", tmp])
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    with _lock:
+        if _lib is None:
+            build()
+            L = ctypes.CDLL(LIB_PATH)
+            vp, u32, u64 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64
+            L.orc_scene_create.restype = vp
+            L.orc_scene_create.argtypes = [vp, vp, vp, vp, u32, vp, u32, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_char_p, u64]
+            L.orc_scene_destroy.argtypes = [vp]
+            L.orc_intersect.restype = ctypes.c_double
+            L.orc_intersect.argtypes = [vp, vp, vp, u64, ctypes.c_int]
+            L.orc_brute_force.argtypes = [vp, vp, vp, u64, ctypes.c_int]
+            L.orc_triangle_hit.restype = ctypes.c_int
+            L.orc_triangle_hit.argtypes = [vp, vp, u32, u32, vp, vp, vp]
+            L.orc_bvh_node_count.restype = u64
+            L.orc_bvh_node_count.argtypes = [vp]
+            L.orc_bvh_nodes.argtypes = [vp, vp]
+            L.orc_visit_stats.argtypes = [vp, vp, u64, vp, vp]
+            L.orc_matrix_inverse.restype = ctypes.c_int
+            L.orc_matrix_inverse.argtypes = [vp, vp]
+            L.orc_machine_epsilon.restype = ctypes.c_float
+            L.orc_machine_epsilon.argtypes = [ctypes.c_float]
+            _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class OracleScene:
+    """LuxRays DataSet + BVHAccel (accel=ACCEL_BVH) or MBVHAccel (ACCEL_MBVH),
+    built with the classic builder (tree type 4 by default)."""
+
+    def __init__(self, scene, accel: int | None = None, tree_type: int = 4):
+        L = lib()
+        if accel is None:
+            accel = ACCEL_MBVH if scene.has_instances else ACCEL_BVH
+        verts = [np.ascontiguousarray(m.vertices, np.float32).reshape(-1, 3) for m in scene.meshes]
+        tris = [np.ascontiguousarray(m.triangles, np.uint32).reshape(-1, 3) for m in scene.meshes]
+        self._verts = np.concatenate(verts) if verts else np.zeros((0, 3), np.float32)
+        self._tris = np.concatenate(tris) if tris else np.zeros((0, 3), np.uint32)
+        self._vo = np.zeros(len(verts) + 1, np.uint64)
+        self._to = np.zeros(len(tris) + 1, np.uint64)
+        self._vo[1:] = np.cumsum([v.shape[0] for v in verts])
+        self._to[1:] = np.cumsum([t.shape[0] for t in tris])
+        objs = (OrcObject * max(1, len(scene.objects)))()
+        for i, (mi, m) in enumerate(scene.objects):
+            objs[i].mesh = mi
+            objs[i].has_transform = 0 if m is None else 1
+            if m is not None:
+                flat = np.asarray(m, np.float32).reshape(16)
+                for k in range(16):
+                    objs[i].m[k] = float(flat[k])
+        err = ctypes.create_string_buffer(512)
+        self.handle = L.orc_scene_create(_ptr(self._verts), _ptr(self._vo), _ptr(self._tris), _ptr(self._to),
+                                         len(scene.meshes), objs, len(scene.objects), accel, tree_type,
+                                         err, 512)
+        if not self.handle:
+            raise RuntimeError("oracle scene build failed: " + err.value.decode())
+        self.accel = accel
+
+    def __del__(self):
+        if getattr(self, "handle", None) and _lib is not None:
+            _lib.orc_scene_destroy(self.handle)
+            self.handle = None
+
+    def intersect(self, rays: np.ndarray, n_threads: int = 0):
+        """Accelerator::Intersect per ray; returns (hits, seconds)."""
+        from luxcore_gb300.workloads import HIT_DTYPE
+        rays = np.ascontiguousarray(rays)
+        hits = np.zeros(rays.shape[0], HIT_DTYPE)
+        secs = lib().orc_intersect(self.handle, _ptr(rays), _ptr(hits), rays.shape[0], n_threads)
+        return hits, secs
+
+    def brute_force(self, rays: np.ndarray, n_threads: int = 0) -> np.ndarray:
+        from luxcore_gb300.workloads import HIT_DTYPE
+        rays = np.ascontiguousarray(rays)
+        hits = np.zeros(rays.shape[0], HIT_DTYPE)
+        lib().orc_brute_force(self.handle, _ptr(rays), _ptr(hits), rays.shape[0], n_threads)
+        return hits
+
+    def triangle_hit(self, ray: np.ndarray, mesh_index: int, tri_index: int):
+        """(hit, t, b1, b2) of Triangle::Intersect against one triangle."""
+        t, b1, b2 = ctypes.c_float(), ctypes.c_float(), ctypes.c_float()
+        r = np.ascontiguousarray(ray.reshape(1))
+        ok = lib().orc_triangle_hit(self.handle, _ptr(r), mesh_index, tri_index,
+                                    ctypes.byref(t), ctypes.byref(b1), ctypes.byref(b2))
+        return bool(ok), t.value, b1.value, b2.value
+
+    def bvh_nodes(self) -> np.ndarray:
+        n = lib().orc_bvh_node_count(self.handle)
+        out = np.zeros((n, 8), np.uint32)
+        if n:
+            lib().orc_bvh_nodes(self.handle, _ptr(out))
+        return out
+
+    def visit_stats(self, rays: np.ndarray):
+        rays = np.ascontiguousarray(rays)
+        a, b = ctypes.c_double(), ctypes.c_double()
+        lib().orc_visit_stats(self.handle, _ptr(rays), rays.shape[0], ctypes.byref(a), ctypes.byref(b))
+        return a.value, b.value
+
+
+def matrix_inverse(m: np.ndarray):
+    m = np.ascontiguousarray(m, np.float32).reshape(16)
+    out = np.zeros(16, np.float32)
+    ok = lib().orc_matrix_inverse(_ptr(m), _ptr(out))
+    return out.reshape(4, 4) if ok else None
+
+
+def machine_epsilon(v: float) -> float:
+    return lib().orc_machine_epsilon(v)

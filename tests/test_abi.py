@@ -1,0 +1,66 @@
+"""CPU tests of the C-ABI boundary: the library loads, exports every function
+include/lrx.h declares, and its struct layouts match the reference's."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from luxcore_gb300 import build, lrx
+from luxcore_gb300 import workloads as W
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    src = open(os.path.join(ROOT, "include", "lrx.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(lrx_[a-z_0-9]+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    build.build()
+    return lrx.load()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    names = declared_functions()
+    assert names, "no declarations parsed"
+    assert sorted(lrx.EXPORTED) == names
+    for n in names:
+        assert hasattr(lib, n), n
+
+
+def test_abi_version_and_error_string(lib):
+    assert lib.lrx_abi_version() == 1
+    assert isinstance(lib.lrx_last_error(), bytes)
+
+
+def test_struct_layouts():
+    assert W.RAY_DTYPE.itemsize == 48 and W.HIT_DTYPE.itemsize == 20
+    assert W.RAY_DTYPE.fields["mint"][1] == 24 and W.RAY_DTYPE.fields["flags"][1] == 36
+    assert ctypes.sizeof(lrx.MeshDesc) == 24
+    assert ctypes.sizeof(lrx.ObjectDesc) == 136
+    assert ctypes.sizeof(lrx.BuildOpts) == 16
+
+
+def test_null_arguments_are_rejected_without_a_device(lib):
+    # argument checks run before any CUDA call
+    h = ctypes.c_void_p()
+    assert lib.lrx_scene_create(None, 0, None, 0, None, None, None) == 1
+    assert lib.lrx_trace(None, None, None, 10, 0, None) == 1
+    assert lib.lrx_scene_destroy(None) == 0
+    assert b"null" in lib.lrx_last_error()
+    del h
+
+
+def test_package_has_no_cpu_fallback():
+    # the product path must not import the oracle
+    for dirpath, _, files in os.walk(os.path.join(ROOT, "luxcore_gb300")):
+        for f in files:
+            if f.endswith(".py"):
+                src = open(os.path.join(dirpath, f)).read()
+                assert "oracle" not in re.sub(r"#.*", "", src).replace('"""', "").split("import")[0] or \
+                    "from oracle" not in src and "import oracle" not in src, f

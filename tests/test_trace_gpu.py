@@ -1,0 +1,268 @@
+"""GPU parity tests: the CUDA engine through the C ABI against the oracle
+(BVHAccel / MBVHAccel restated) and against golden hits of the reference's
+own kernel code.  Bar: parity.compare (>= 99.99 % index agreement, every
+disagreement an exact-t tie re-tested on the oracle, t/b1/b2 within 1e-5
+relative -- in practice bit-exact)."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+sys.path.insert(0, os.path.dirname(__file__))
+sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+
+from luxcore_gb300 import lrx  # noqa: E402
+from luxcore_gb300 import workloads as W  # noqa: E402
+from oracle import pyoracle as po  # noqa: E402
+from adversarial import adversarial_rays  # noqa: E402
+from parity import check_anyhit, compare  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+SENT = 0xDEADBEEF
+
+
+@pytest.fixture(scope="module")
+def torch_cuda(cuda_ready):
+    import torch
+    return torch
+
+
+def gpu_trace(torch, scene, rays, mode=lrx.LRX_TRACE_CLOSEST, prefill=SENT, chunks=1):
+    n = rays.shape[0]
+    d_r = torch.from_numpy(np.ascontiguousarray(rays).view(np.uint8).reshape(-1).copy()).cuda()
+    d_h = torch.empty(n * 20, dtype=torch.uint8, device="cuda")
+    d_h.view(torch.int32).fill_(np.int32(np.uint32(prefill).view(np.int32)).item())
+    st = torch.cuda.current_stream().cuda_stream
+    bounds = np.linspace(0, n, chunks + 1).astype(np.int64)
+    for a, b in zip(bounds[:-1], bounds[1:]):
+        if b > a:
+            scene.trace(d_r.data_ptr() + 48 * int(a), d_h.data_ptr() + 20 * int(a), int(b - a), mode, st)
+    torch.cuda.synchronize()
+    assert scene.device_status(st) == 0
+    return d_h.cpu().numpy().view(W.HIT_DTYPE).copy()
+
+
+def assert_parity(gpu, ref, oracle, rays, min_hit_rate=0.0):
+    st = compare(gpu, ref, oracle, rays)
+    assert st["ok"], st
+    assert st["hit_rate"] >= min_hit_rate, st
+    return st
+
+
+# ---------------------------------------------------------------------------
+
+
+@pytest.mark.parametrize("name", ["golden_random", "golden_heightfield", "golden_multimesh"])
+def test_golden_fixtures(torch_cuda, name):
+    from make_golden import load
+    scene, rays, ref = load(name)
+    s = lrx.Scene(scene)
+    gpu = gpu_trace(torch_cuda, s, rays)
+    masked = (rays["flags"] & W.RAY_FLAGS_MASKED) != 0
+    # masked rays: hit left untouched (bvh.cl:243-244)
+    assert (gpu.view(np.uint32).reshape(-1, 5)[masked] == SENT).all()
+    nan_ray = np.isnan(rays["o"]).any(1) | np.isnan(rays["d"]).any(1) | np.isnan(rays["maxt"])
+    # NaN rays: misses, as BVHAccel::Intersect returns them
+    assert (gpu["meshIndex"][nan_ray] == W.NULL_INDEX).all()
+    keep = ~masked & ~nan_ray
+    oracle = po.OracleScene(scene, po.ACCEL_BVH)
+    g, r, rr = gpu[keep], ref[keep], rays[keep]
+    st = compare(g, r, oracle, rr)
+    assert st["bad_disagreements"] == 0 and st["values_ok"] and st["ties_valid"], st
+    # and against the oracle itself, ties included
+    oh, _ = oracle.intersect(rays)
+    assert_parity(gpu[keep], oh[keep], oracle, rr)
+
+
+def test_config1_full_scene(torch_cuda):
+    """65,536 random triangles (config 1's scene), 262,144 of its rays."""
+    scene, rays = W.config1(n_rays=1 << 18)
+    s = lrx.Scene(scene)
+    oracle = po.OracleScene(scene)
+    ref, _ = oracle.intersect(rays)
+    gpu = gpu_trace(torch_cuda, s, rays)
+    st = assert_parity(gpu, ref, oracle, rays, min_hit_rate=0.3)
+    assert st["bitexact_t"] == 1.0
+    anyh = gpu_trace(torch_cuda, s, rays, lrx.LRX_TRACE_ANY)
+    a = check_anyhit(anyh, ref, oracle, rays)
+    assert a["ok"], a
+
+
+def test_heightfield_primary_bounce_shadow(torch_cuda):
+    """Config 2's three ray sets on a 256x256 heightfield."""
+    mesh = W.heightfield_mesh(256, 21)
+    scene = W.SceneDesc([mesh])
+    s = lrx.Scene(scene)
+    oracle = po.OracleScene(scene)
+    prim = W.pinhole_rays(256, 256)
+    ref_p, _ = oracle.intersect(prim)
+    gpu_p = gpu_trace(torch_cuda, s, prim)
+    assert_parity(gpu_p, ref_p, oracle, prim, min_hit_rate=0.2)
+    bounce = W.bounce_rays(scene, prim, gpu_p, 1 << 16, 22)
+    ref_b, _ = oracle.intersect(bounce)
+    gpu_b = gpu_trace(torch_cuda, s, bounce)
+    assert_parity(gpu_b, ref_b, oracle, bounce, min_hit_rate=0.05)
+    shadow = W.shadow_rays(bounce, 4, 23)
+    ref_s, _ = oracle.intersect(shadow)
+    any_s = gpu_trace(torch_cuda, s, shadow, lrx.LRX_TRACE_ANY)
+    a = check_anyhit(any_s, ref_s, oracle, shadow)
+    assert a["ok"], a
+
+
+def test_instanced_two_level(torch_cuda):
+    """Config 3 in small: displaced icospheres under random affine instances."""
+    scene, closest, anyr = W.config3(n_rays=1 << 15, n_meshes=4, freq=12, n_inst=300, extent=3.0,
+                                     scale=(0.1, 0.4))
+    s = lrx.Scene(scene)
+    info = s.info()
+    assert info["two_level"] == 1 and info["instance_count"] == 300 and info["blas_count"] == 4
+    oracle = po.OracleScene(scene)
+    ref, _ = oracle.intersect(closest)
+    gpu = gpu_trace(torch_cuda, s, closest)
+    st = assert_parity(gpu, ref, oracle, closest, min_hit_rate=0.1)
+    assert st["bitexact_t"] == 1.0
+    ref_a, _ = oracle.intersect(anyr)
+    gpu_a = gpu_trace(torch_cuda, s, anyr, lrx.LRX_TRACE_ANY)
+    a = check_anyhit(gpu_a, ref_a, oracle, anyr)
+    assert a["ok"], a
+
+
+def test_plain_and_instanced_objects_mixed(torch_cuda):
+    base = W.displaced_icosphere(8, 31)
+    objs = [(1, None), (0, None)]
+    rng = np.random.default_rng(4)
+    for k in range(20):
+        m = np.eye(4, dtype=np.float32)
+        m[:3, :3] *= rng.uniform(0.05, 0.2)
+        m[:3, 3] = rng.uniform(0, 1, 3)
+        objs.append((2, m))
+    scene = W.SceneDesc([W.random_triangles(500, 32), W.random_triangles(300, 33), base], objs)
+    s = lrx.Scene(scene)
+    rays = W.random_rays(20000, 34)
+    oracle = po.OracleScene(scene)
+    ref, _ = oracle.intersect(rays)
+    gpu = gpu_trace(torch_cuda, s, rays)
+    assert_parity(gpu, ref, oracle, rays, min_hit_rate=0.05)
+    meshes_hit = set(np.unique(gpu["meshIndex"]).tolist())
+    assert {0, 1} <= meshes_hit and any(m >= 2 and m != W.NULL_INDEX for m in meshes_hit)
+
+
+def test_adversarial_rays(torch_cuda):
+    mesh = W.heightfield_mesh(64, 41)
+    scene = W.SceneDesc([mesh])
+    rays = adversarial_rays(mesh, 42, 64)
+    s = lrx.Scene(scene)
+    gpu = gpu_trace(torch_cuda, s, rays)
+    oracle = po.OracleScene(scene)
+    ref, _ = oracle.intersect(rays)
+    masked = (rays["flags"] & W.RAY_FLAGS_MASKED) != 0
+    assert (gpu.view(np.uint32).reshape(-1, 5)[masked] == SENT).all()
+    st = compare(gpu[~masked], ref[~masked], oracle, rays[~masked])
+    assert st["bad_disagreements"] == 0 and st["values_ok"] and st["ties_valid"], st
+    anyh = gpu_trace(torch_cuda, s, rays, lrx.LRX_TRACE_ANY)
+    a = check_anyhit(anyh[~masked], ref[~masked], oracle, rays[~masked])
+    assert a["ok"], a
+
+
+@pytest.mark.parametrize("n_tris", [0, 1, 2, 3, 4, 9, 25])
+def test_tiny_and_empty_scenes(torch_cuda, n_tris):
+    mesh = W.random_triangles(n_tris, 50 + n_tris, size=0.3) if n_tris else W.Mesh(
+        np.zeros((0, 3), np.float32), np.zeros((0, 3), np.uint32))
+    scene = W.SceneDesc([mesh])
+    s = lrx.Scene(scene)
+    rays = W.random_rays(4096, 51)
+    gpu = gpu_trace(torch_cuda, s, rays)
+    oracle = po.OracleScene(scene)
+    ref, _ = oracle.intersect(rays)
+    assert_parity(gpu, ref, oracle, rays)
+    if n_tris == 0:
+        assert np.array_equal(gpu["t"], rays["maxt"])
+
+
+def test_degenerate_coincident_triangles(torch_cuda):
+    """Many identical triangles: equal Morton codes, equal t -> lowest index."""
+    v = np.array([[0.2, 0.2, 0.5], [0.8, 0.2, 0.5], [0.5, 0.8, 0.5]], np.float32)
+    n = 3000
+    mesh = W.Mesh(np.tile(v, (n, 1)), np.arange(3 * n, dtype=np.uint32).reshape(n, 3))
+    scene = W.SceneDesc([mesh])
+    s = lrx.Scene(scene)
+    rng = np.random.default_rng(3)
+    o = np.concatenate([rng.uniform(0.3, 0.6, (512, 2)), np.zeros((512, 1))], 1).astype(np.float32)
+    rays = W.make_rays(o, np.tile(np.array([[0, 0, 1]], np.float32), (512, 1)), 1e-4, 1e30)
+    gpu = gpu_trace(torch_cuda, s, rays)
+    hit = gpu["meshIndex"] != W.NULL_INDEX
+    assert hit.mean() > 0.5
+    assert (gpu["triangleIndex"][hit] == 0).all()
+    assert s.info()["max_depth"] <= 30
+
+
+def test_host_entry_point_matches_device(torch_cuda):
+    scene, rays = W.config1(n_tris=20000, n_rays=50000, seed=61)
+    rays["flags"][::7] = W.RAY_FLAGS_MASKED
+    s = lrx.Scene(scene)
+    d = gpu_trace(torch_cuda, s, rays)
+    hits = np.zeros(rays.shape[0], W.HIT_DTYPE)
+    hits.view(np.uint32)[:] = SENT
+    h = s.trace_host(rays, hits)
+    assert np.array_equal(h.view(np.uint8), d.view(np.uint8))
+
+
+def test_deterministic_and_batch_independent(torch_cuda):
+    scene, rays = W.config1(n_tris=30000, n_rays=100000, seed=71)
+    s = lrx.Scene(scene)
+    a = gpu_trace(torch_cuda, s, rays)
+    b = gpu_trace(torch_cuda, s, rays, chunks=7)
+    assert np.array_equal(a.view(np.uint8), b.view(np.uint8))
+
+
+def test_instance_update_matches_rebuilt_oracle(torch_cuda):
+    scene, closest, _ = W.config3(n_rays=20000, n_meshes=2, freq=8, n_inst=64, extent=2.0, scale=(0.1, 0.3))
+    s = lrx.Scene(scene)
+    rng = np.random.default_rng(9)
+    moved = []
+    for mi, m in scene.objects:
+        m2 = np.array(m, np.float32).copy()
+        m2[:3, 3] += rng.uniform(-0.3, 0.3, 3).astype(np.float32)
+        moved.append((mi, m2))
+    scene2 = W.SceneDesc(scene.meshes, moved)
+    s.update_instances(scene2)
+    oracle = po.OracleScene(scene2)
+    ref, _ = oracle.intersect(closest)
+    gpu = gpu_trace(torch_cuda, s, closest)
+    assert_parity(gpu, ref, oracle, closest, min_hit_rate=0.02)
+
+
+def test_counted_trace(torch_cuda):
+    scene, rays = W.config1(n_tris=20000, n_rays=40000, seed=81)
+    s = lrx.Scene(scene)
+    torch = torch_cuda
+    d_r = torch.from_numpy(rays.view(np.uint8).copy()).cuda()
+    d_h = torch.empty(rays.shape[0] * 20, dtype=torch.uint8, device="cuda")
+    c = torch.zeros(4, dtype=torch.int64, device="cuda")
+    s.trace_counted(d_r.data_ptr(), d_h.data_ptr(), rays.shape[0], 0, c.data_ptr(),
+                    torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    nodes, tris, insts, n = c.cpu().tolist()
+    assert n == rays.shape[0] and insts == 0
+    assert nodes >= n and tris > 0
+    plain = gpu_trace(torch, s, rays)
+    assert np.array_equal(d_h.cpu().numpy().view(W.HIT_DTYPE).view(np.uint8), plain.view(np.uint8))
+
+
+def test_rejects_bad_arguments(torch_cuda):
+    scene, rays = W.config1(n_tris=100, n_rays=64, seed=91)
+    s = lrx.Scene(scene)
+    torch = torch_cuda
+    buf = torch.empty(64 * 48 + 16, dtype=torch.uint8, device="cuda")
+    with pytest.raises(lrx.LrxError):
+        s.trace(buf.data_ptr() + 4, buf.data_ptr(), 8, 0)      # misaligned rays
+    with pytest.raises(lrx.LrxError):
+        s.trace(buf.data_ptr(), buf.data_ptr(), 8, 7)          # unknown mode
+    bad = W.SceneDesc([W.Mesh(np.zeros((3, 3), np.float32), np.array([[0, 1, 5]], np.uint32))])
+    with pytest.raises(lrx.LrxError):
+        lrx.Scene(bad)                                         # vertex index out of range
+    sing = W.SceneDesc([W.random_triangles(10, 1)], [(0, np.zeros((4, 4), np.float32))])
+    with pytest.raises(lrx.LrxError):
+        lrx.Scene(sing)                                        # singular instance transform
