@@ -407,8 +407,8 @@ def run_lrx(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="lrx", choices=["lrx", "reference"])
     ap.add_argument("--ref-fraction", type=int, default=4,
                     help="CPU legs trace every Nth ray of each set")

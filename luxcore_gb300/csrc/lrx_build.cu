@@ -31,6 +31,7 @@ enum : int {
 	C_TRIS = 8,    // leaf-primitive allocation counter
 	C_QA = 9,      // queue A item count
 	C_QB = 10,     // queue B item count
+	C_ERR = 11,    // nonzero: a capacity guard fired (never expected)
 	C_BOX = 12,    // 6 floats: root box lo.xyz, hi.xyz
 	C_COUNT = 20
 };
@@ -208,8 +209,10 @@ __global__ void __launch_bounds__(128) k_collapse(const uint2 *__restrict__ item
 		uint2 *__restrict__ out_items, uint32_t *n_out, const uint32_t *__restrict__ bchild,
 		const float4 *__restrict__ bn_lo, const float4 *__restrict__ bn_hi, const uint2 *__restrict__ brange,
 		const uint32_t *__restrict__ sorted, const float4 *__restrict__ plo, const float4 *__restrict__ phi,
-		uint32_t leaf_max, WideNode *__restrict__ wnodes, uint32_t *__restrict__ prim_order, uint32_t *counters) {
-	const uint32_t n_items = *n_items_ptr;
+		uint32_t leaf_max, WideNode *__restrict__ wnodes, uint32_t *__restrict__ prim_order, uint32_t *counters,
+		uint32_t cap) {
+	// cap = primitive count: bounds the node array, the leaf order and each queue
+	const uint32_t n_items = min(*n_items_ptr, cap);
 	for (uint32_t it = blockIdx.x * blockDim.x + threadIdx.x; it < n_items; it += gridDim.x * blockDim.x) {
 		const uint2 item = items[it];
 		uint32_t cref[8];
@@ -309,6 +312,10 @@ __global__ void __launch_bounds__(128) k_collapse(const uint2 *__restrict__ item
 
 		const uint32_t child_base = n_int ? atomicAdd(&counters[C_NODES], n_int) : 0u;
 		const uint32_t tri_base = n_tri ? atomicAdd(&counters[C_TRIS], n_tri) : 0u;
+		if (child_base + n_int > cap || tri_base + n_tri > cap || item.y >= cap) {
+			atomicOr(&counters[C_ERR], 1u);
+			continue;
+		}
 
 		uint32_t imask = 0, int_rank = 0, tri_off = 0;
 		uint32_t meta[2] = {0, 0}, qlx[2] = {0, 0}, qly[2] = {0, 0}, qlz[2] = {0, 0};
@@ -335,7 +342,8 @@ __global__ void __launch_bounds__(128) k_collapse(const uint2 *__restrict__ item
 				imask |= 1u << s;
 				meta[wsel] |= kInternalMeta << sh;
 				const uint32_t slot = atomicAdd(n_out, 1u);
-				out_items[slot] = make_uint2(cref[k], child_base + int_rank);
+				if (slot < cap) out_items[slot] = make_uint2(cref[k], child_base + int_rank);
+				else atomicOr(&counters[C_ERR], 2u);
 				++int_rank;
 			} else {
 				const uint32_t m = (((1u << ccount[k]) - 1u) << 5) | tri_off;
@@ -439,6 +447,10 @@ lrx_status build_wide_bvh(uint32_t n, const float4 *d_lo, const float4 *d_hi, ui
 		LRX_CUDA(cudaMemcpyAsync(&n_in, counters + cin, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
 		LRX_CUDA(cudaStreamSynchronize(st));
 		if (n_in == 0) break;
+		if (n_in > n) {
+			set_error("BVH collapse queue overflow");
+			return LRX_ERR_BUILD;
+		}
 		++depth;
 		if (depth > (uint32_t)kMaxTreeDepth) {
 			set_error("BVH deeper than the traversal stack allows");
@@ -447,7 +459,7 @@ lrx_status build_wide_bvh(uint32_t n, const float4 *d_lo, const float4 *d_hi, ui
 		LRX_CUDA(cudaMemsetAsync(counters + cout, 0, sizeof(uint32_t), st));
 		k_collapse<<<std::min(blocks_for(n_in, 128), 152u * 16u), 128, 0, st>>>(qin, counters + cin, qout,
 				counters + cout, bchild, bn_lo, bn_hi, brange, sorted, d_lo, d_hi, leaf_max,
-				S.wide_nodes.as<WideNode>(), S.prim_order.as<uint32_t>(), counters);
+				S.wide_nodes.as<WideNode>(), S.prim_order.as<uint32_t>(), counters, n);
 		LRX_CUDA(cudaGetLastError());
 		std::swap(qin, qout);
 		std::swap(cin, cout);
@@ -455,7 +467,7 @@ lrx_status build_wide_bvh(uint32_t n, const float4 *d_lo, const float4 *d_hi, ui
 	uint32_t host_counters[C_COUNT];
 	LRX_CUDA(cudaMemcpyAsync(host_counters, counters, sizeof(host_counters), cudaMemcpyDeviceToHost, st));
 	LRX_CUDA(cudaStreamSynchronize(st));
-	if (host_counters[C_TRIS] != n) {
+	if (host_counters[C_ERR] != 0 || host_counters[C_TRIS] != n) {
 		set_error("BVH collapse lost primitives");
 		return LRX_ERR_BUILD;
 	}

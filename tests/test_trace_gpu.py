@@ -71,9 +71,13 @@ def test_golden_fixtures(torch_cuda, name):
     g, r, rr = gpu[keep], ref[keep], rays[keep]
     st = compare(g, r, oracle, rr)
     assert st["bad_disagreements"] == 0 and st["values_ok"] and st["ties_valid"], st
-    # and against the oracle itself, ties included
+    # and against the oracle itself: these fixtures aim rays at shared
+    # vertices and edges, so the rate bar does not apply -- every
+    # disagreement must be an exact-t tie that re-tests as a hit
     oh, _ = oracle.intersect(rays)
-    assert_parity(gpu[keep], oh[keep], oracle, rr)
+    st = compare(gpu[keep], oh[keep], oracle, rr)
+    assert st["bad_disagreements"] == 0 and st["values_ok"] and st["ties_valid"], st
+    assert st["agree"] >= 0.99, st
 
 
 def test_config1_full_scene(torch_cuda):
