@@ -156,6 +156,36 @@ lrx_status lrx_trace(lrx_scene *scene, const void *d_rays, void *d_hits,
 lrx_status lrx_trace_host(lrx_scene *scene, const lrx_ray *h_rays, lrx_hit *h_hits,
 		uint32_t count, uint32_t mode, void *stream);
 
+/* Largest batch lrx_trace_host_noalloc accepts (its fixed staging area). */
+#define LRX_NOALLOC_MAX_RAYS 131072u
+
+/* lrx_trace_host without any device allocation.  This entry point has no
+ * counterpart in the reference.
+ *
+ * It is for callers that cannot call cudaMalloc or cudaFree.  One example is
+ * a host loop that shares the GPU with other work in flight: cudaFree can
+ * synchronise the whole device and stall that work, and lrx_trace_host grows
+ * its staging buffers with cudaMalloc/cudaFree when a larger batch arrives.
+ * Another is an application that owns all device memory through its own
+ * fixed pool or budget and allows no allocation outside it.
+ *
+ * Instead of allocating, the rays and hits are staged through one array that
+ * the library reserves statically on every GPU that loads it: room for
+ * LRX_NOALLOC_MAX_RAYS rays and hits (8.5 MiB), held until the process exits.
+ * A batch larger than that is rejected with LRX_ERR_INVALID_ARGUMENT.
+ * Results are the same as lrx_trace_host's for the same scene and rays.
+ *
+ * The first call on a device looks up the array's device address (one
+ * cudaGetSymbolAddress, with that device current); make that first call
+ * before any stream capture.  Every call on a device shares the array and it
+ * keeps the last call's contents; nothing in it needs to start at zero,
+ * because each call copies its rays and the caller's hit buffer in before
+ * the kernel runs.  Calls whose GPU work overlapped would race on the array,
+ * so the library serialises these calls per device and each one
+ * synchronises `stream` before it returns. */
+lrx_status lrx_trace_host_noalloc(lrx_scene *scene, const lrx_ray *h_rays, lrx_hit *h_hits,
+		uint32_t count, uint32_t mode, void *stream);
+
 /* Like lrx_trace, and also accumulates per-ray traversal counters into
  * d_counters[4] (u64: wide nodes fetched, triangles tested, instances
  * entered, rays traced) -- the byte accounting of the roofline. */

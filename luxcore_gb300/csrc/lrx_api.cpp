@@ -185,6 +185,8 @@ struct lrx_scene {
 	std::mutex mu;
 };
 
+int lrx::scene_device(const lrx_scene *scene) { return scene->device; }
+
 namespace {
 
 struct DeviceGuard {

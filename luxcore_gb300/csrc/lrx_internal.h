@@ -111,4 +111,7 @@ struct TraceArgs {
 
 lrx_status launch_trace(const TraceArgs &a, cudaStream_t stream);
 
+// CUDA device a scene was built on.
+int scene_device(const lrx_scene *scene);
+
 }  // namespace lrx

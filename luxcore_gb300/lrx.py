@@ -30,7 +30,8 @@ STATUS_NAMES = {0: "LRX_OK", 1: "LRX_ERR_INVALID_ARGUMENT", 2: "LRX_ERR_CUDA", 3
 # Every function include/lrx.h declares (checked by the CPU tests).
 EXPORTED = ["lrx_abi_version", "lrx_last_error", "lrx_scene_create", "lrx_scene_destroy",
             "lrx_scene_update_instances", "lrx_scene_get_info", "lrx_trace", "lrx_trace_host",
-            "lrx_trace_counted", "lrx_scene_device_status"]
+            "lrx_trace_counted", "lrx_scene_device_status", "lrx_trace_host_noalloc"]
+LRX_NOALLOC_MAX_RAYS = 131072
 
 
 class LrxError(RuntimeError):
@@ -97,6 +98,8 @@ def load(path: str | None = None):
         L.lrx_trace.argtypes = [vp, vp, vp, u32, u32, vp]
         L.lrx_trace_host.restype = st
         L.lrx_trace_host.argtypes = [vp, vp, vp, u32, u32, vp]
+        L.lrx_trace_host_noalloc.restype = st
+        L.lrx_trace_host_noalloc.argtypes = [vp, vp, vp, u32, u32, vp]
         L.lrx_trace_counted.restype = st
         L.lrx_trace_counted.argtypes = [vp, vp, vp, u32, u32, vp, vp]
         L.lrx_scene_device_status.restype = st
