@@ -342,8 +342,9 @@ def run_lrx(args):
     traffic = None if tpr is None else tpr * rays_per_step / len(dev)
 
     # end to end: host rays in pinned memory -> lrx_trace_host -> host hits
+    e2e_value = None
     pinned = []
-    for name, r, mode in sets:
+    for name, r, mode in (sets if not args.no_e2e else []):
         hr = torch.from_numpy(np.ascontiguousarray(r).view(np.uint8).reshape(-1).copy()).pin_memory()
         hh = torch.empty(r.shape[0] * HIT_BYTES, dtype=torch.uint8).pin_memory()
         pinned.append((hr, hh, r.shape[0], mode))
@@ -352,14 +353,15 @@ def run_lrx(args):
         for hr, hh, n, mode in pinned:
             scene.trace_host_ptr(hr.data_ptr(), hh.data_ptr(), n, mode, st)
 
-    for _ in range(max(1, args.warmup)):
-        e2e_step()
-    d.barrier()
-    t1 = time.perf_counter()
-    for _ in range(args.steps):
-        e2e_step()
-    e2e_s = d.max(time.perf_counter() - t1)
-    e2e_value = rays_per_step * args.steps * ws / e2e_s / 1e6
+    if not args.no_e2e:
+        for _ in range(max(1, args.warmup)):
+            e2e_step()
+        d.barrier()
+        t1 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        e2e_s = d.max(time.perf_counter() - t1)
+        e2e_value = round(rays_per_step * args.steps * ws / e2e_s / 1e6, 3)
     h2d = rays_per_step * (RAY_BYTES + HIT_BYTES)
     d2h = rays_per_step * HIT_BYTES
 
@@ -393,7 +395,7 @@ def run_lrx(args):
                          "peak_kind": peak_kind,
                          "bytes_per_ray": round(tot_alg / rays_per_step, 1)},
             "cpu_baseline": cpu,
-            "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "api": "lrx_trace_host (pinned host buffers)"},
             "gpu_launches": len(dev) * args.steps,
             "clocks": clk,
@@ -413,6 +415,7 @@ def main():
     ap.add_argument("--ref-fraction", type=int, default=4,
                     help="CPU legs trace every Nth ray of each set")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (lrx_trace_host) leg")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3 (timing rule)")
