@@ -156,6 +156,22 @@ lrx_status lrx_trace(lrx_scene *scene, const void *d_rays, void *d_hits,
 lrx_status lrx_trace_host(lrx_scene *scene, const lrx_ray *h_rays, lrx_hit *h_hits,
 		uint32_t count, uint32_t mode, void *stream);
 
+/* Traversal launch configuration of a scene (what the autotuner chooses). */
+#define LRX_KERNEL_SIMPLE 0u      /* one thread per ray, as the reference's kernel */
+#define LRX_KERNEL_PERSISTENT 1u  /* persistent blocks, warp-level dynamic ray fetch (default) */
+typedef struct lrx_trace_config {
+	uint32_t struct_size;     /* sizeof(lrx_trace_config) */
+	uint32_t kernel;          /* LRX_KERNEL_* */
+	uint32_t blocks_per_sm;   /* persistent: resident blocks per SM (0 = default 8) */
+	uint32_t refill_min;      /* persistent: idle lanes in a warp before it fetches rays (0 = default 1) */
+} lrx_trace_config;
+
+/* Sets / reads the launch configuration lrx_trace uses for this scene.
+ * No reference counterpart (the reference fixes 32-thread blocks,
+ * bvhaccelhw.cpp:259-268). */
+lrx_status lrx_scene_set_trace_config(lrx_scene *scene, const lrx_trace_config *config);
+lrx_status lrx_scene_get_trace_config(const lrx_scene *scene, lrx_trace_config *config);
+
 /* Largest batch lrx_trace_host_noalloc accepts (its fixed staging area). */
 #define LRX_NOALLOC_MAX_RAYS 131072u
 

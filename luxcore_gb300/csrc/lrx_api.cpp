@@ -180,6 +180,7 @@ struct lrx_scene {
 	uint32_t tlas_capacity = 0;
 	uint32_t blas_node_total = 0;
 	lrx_build_opts opts{};
+	lrx_trace_config tcfg{sizeof(lrx_trace_config), LRX_KERNEL_PERSISTENT, 0, 0};
 	lrx_scene_info info{};
 	BuildScratch scratch;
 	std::mutex mu;
@@ -645,7 +646,33 @@ static lrx_status trace_common(lrx_scene *s, const void *d_rays, void *d_hits, u
 	a.any_hit = mode == LRX_TRACE_ANY;
 	a.status = s->status.as<uint32_t>();
 	a.counters = reinterpret_cast<unsigned long long *>(d_counters);
+	a.kernel = s->tcfg.kernel;
+	a.blocks_per_sm = s->tcfg.blocks_per_sm;
+	a.refill_min = s->tcfg.refill_min;
 	return launch_trace(a, st);
+}
+
+lrx_status lrx_scene_set_trace_config(lrx_scene *s, const lrx_trace_config *c) {
+	if (!s || !c || c->struct_size < sizeof(lrx_trace_config)) {
+		set_error("lrx_scene_set_trace_config: null argument or old struct");
+		return LRX_ERR_INVALID_ARGUMENT;
+	}
+	if (c->kernel > LRX_KERNEL_PERSISTENT || c->blocks_per_sm > 32 || c->refill_min > 32) {
+		set_error("lrx_scene_set_trace_config: value out of range");
+		return LRX_ERR_INVALID_ARGUMENT;
+	}
+	s->tcfg = *c;
+	s->tcfg.struct_size = sizeof(lrx_trace_config);
+	return LRX_OK;
+}
+
+lrx_status lrx_scene_get_trace_config(const lrx_scene *s, lrx_trace_config *c) {
+	if (!s || !c) {
+		set_error("lrx_scene_get_trace_config: null argument");
+		return LRX_ERR_INVALID_ARGUMENT;
+	}
+	*c = s->tcfg;
+	return LRX_OK;
 }
 
 lrx_status lrx_trace(lrx_scene *s, const void *d_rays, void *d_hits, uint32_t count, uint32_t mode, void *stream) {

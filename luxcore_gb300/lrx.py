@@ -30,7 +30,10 @@ STATUS_NAMES = {0: "LRX_OK", 1: "LRX_ERR_INVALID_ARGUMENT", 2: "LRX_ERR_CUDA", 3
 # Every function include/lrx.h declares (checked by the CPU tests).
 EXPORTED = ["lrx_abi_version", "lrx_last_error", "lrx_scene_create", "lrx_scene_destroy",
             "lrx_scene_update_instances", "lrx_scene_get_info", "lrx_trace", "lrx_trace_host",
-            "lrx_trace_counted", "lrx_scene_device_status", "lrx_trace_host_noalloc"]
+            "lrx_trace_counted", "lrx_scene_device_status", "lrx_trace_host_noalloc",
+            "lrx_scene_set_trace_config", "lrx_scene_get_trace_config"]
+LRX_KERNEL_SIMPLE = 0
+LRX_KERNEL_PERSISTENT = 1
 LRX_NOALLOC_MAX_RAYS = 131072
 
 
@@ -53,6 +56,11 @@ class ObjectDesc(ctypes.Structure):
 class BuildOpts(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_uint32), ("leaf_max", ctypes.c_uint32),
                 ("treelet_passes", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+
+class TraceConfig(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_uint32), ("kernel", ctypes.c_uint32),
+                ("blocks_per_sm", ctypes.c_uint32), ("refill_min", ctypes.c_uint32)]
 
 
 class SceneInfo(ctypes.Structure):
@@ -98,6 +106,10 @@ def load(path: str | None = None):
         L.lrx_trace.argtypes = [vp, vp, vp, u32, u32, vp]
         L.lrx_trace_host.restype = st
         L.lrx_trace_host.argtypes = [vp, vp, vp, u32, u32, vp]
+        L.lrx_scene_set_trace_config.restype = st
+        L.lrx_scene_set_trace_config.argtypes = [vp, ctypes.POINTER(TraceConfig)]
+        L.lrx_scene_get_trace_config.restype = st
+        L.lrx_scene_get_trace_config.argtypes = [vp, ctypes.POINTER(TraceConfig)]
         L.lrx_trace_host_noalloc.restype = st
         L.lrx_trace_host_noalloc.argtypes = [vp, vp, vp, u32, u32, vp]
         L.lrx_trace_counted.restype = st
@@ -164,6 +176,15 @@ class Scene:
         inf = SceneInfo()
         check(load().lrx_scene_get_info(self.handle, ctypes.byref(inf)))
         return inf.as_dict()
+
+    def set_trace_config(self, kernel: int = LRX_KERNEL_PERSISTENT, blocks_per_sm: int = 0, refill_min: int = 0):
+        c = TraceConfig(ctypes.sizeof(TraceConfig), kernel, blocks_per_sm, refill_min)
+        check(load().lrx_scene_set_trace_config(self.handle, ctypes.byref(c)))
+
+    def trace_config(self) -> dict:
+        c = TraceConfig()
+        check(load().lrx_scene_get_trace_config(self.handle, ctypes.byref(c)))
+        return {"kernel": c.kernel, "blocks_per_sm": c.blocks_per_sm, "refill_min": c.refill_min}
 
     def update_instances(self, scene: W.SceneDesc, stream: int = 0):
         objs = _object_array(scene)

@@ -21,6 +21,15 @@ from parity import check_anyhit, compare  # noqa: E402
 pytestmark = pytest.mark.gpu
 
 SENT = 0xDEADBEEF
+KERNELS = pytest.mark.parametrize("kernel", [lrx.LRX_KERNEL_SIMPLE, lrx.LRX_KERNEL_PERSISTENT],
+                                  ids=["simple", "persistent"])
+
+
+def make_scene(desc, kernel=lrx.LRX_KERNEL_PERSISTENT, **kw):
+    s = lrx.Scene(desc, **kw)
+    s.set_trace_config(kernel)
+    assert s.trace_config()["kernel"] == kernel
+    return s
 
 
 @pytest.fixture(scope="module")
@@ -55,10 +64,11 @@ def assert_parity(gpu, ref, oracle, rays, min_hit_rate=0.0):
 
 
 @pytest.mark.parametrize("name", ["golden_random", "golden_heightfield", "golden_multimesh"])
-def test_golden_fixtures(torch_cuda, name):
+@KERNELS
+def test_golden_fixtures(torch_cuda, kernel, name):
     from make_golden import load
     scene, rays, ref = load(name)
-    s = lrx.Scene(scene)
+    s = make_scene(scene, kernel)
     gpu = gpu_trace(torch_cuda, s, rays)
     masked = (rays["flags"] & W.RAY_FLAGS_MASKED) != 0
     # masked rays: hit left untouched (bvh.cl:243-244)
@@ -80,10 +90,11 @@ def test_golden_fixtures(torch_cuda, name):
     assert st["agree"] >= 0.99, st
 
 
-def test_config1_full_scene(torch_cuda):
+@KERNELS
+def test_config1_full_scene(torch_cuda, kernel):
     """65,536 random triangles (config 1's scene), 262,144 of its rays."""
     scene, rays = W.config1(n_rays=1 << 18)
-    s = lrx.Scene(scene)
+    s = make_scene(scene, kernel)
     oracle = po.OracleScene(scene)
     ref, _ = oracle.intersect(rays)
     gpu = gpu_trace(torch_cuda, s, rays)
@@ -94,11 +105,12 @@ def test_config1_full_scene(torch_cuda):
     assert a["ok"], a
 
 
-def test_heightfield_primary_bounce_shadow(torch_cuda):
+@KERNELS
+def test_heightfield_primary_bounce_shadow(torch_cuda, kernel):
     """Config 2's three ray sets on a 256x256 heightfield."""
     mesh = W.heightfield_mesh(256, 21)
     scene = W.SceneDesc([mesh])
-    s = lrx.Scene(scene)
+    s = make_scene(scene, kernel)
     oracle = po.OracleScene(scene)
     prim = W.pinhole_rays(256, 256)
     ref_p, _ = oracle.intersect(prim)
@@ -115,11 +127,12 @@ def test_heightfield_primary_bounce_shadow(torch_cuda):
     assert a["ok"], a
 
 
-def test_instanced_two_level(torch_cuda):
+@KERNELS
+def test_instanced_two_level(torch_cuda, kernel):
     """Config 3 in small: displaced icospheres under random affine instances."""
     scene, closest, anyr = W.config3(n_rays=1 << 15, n_meshes=4, freq=12, n_inst=300, extent=3.0,
                                      scale=(0.1, 0.4))
-    s = lrx.Scene(scene)
+    s = make_scene(scene, kernel)
     info = s.info()
     assert info["two_level"] == 1 and info["instance_count"] == 300 and info["blas_count"] == 4
     oracle = po.OracleScene(scene)
@@ -133,7 +146,8 @@ def test_instanced_two_level(torch_cuda):
     assert a["ok"], a
 
 
-def test_plain_and_instanced_objects_mixed(torch_cuda):
+@KERNELS
+def test_plain_and_instanced_objects_mixed(torch_cuda, kernel):
     base = W.displaced_icosphere(8, 31)
     objs = [(1, None), (0, None)]
     rng = np.random.default_rng(4)
@@ -143,7 +157,7 @@ def test_plain_and_instanced_objects_mixed(torch_cuda):
         m[:3, 3] = rng.uniform(0, 1, 3)
         objs.append((2, m))
     scene = W.SceneDesc([W.random_triangles(500, 32), W.random_triangles(300, 33), base], objs)
-    s = lrx.Scene(scene)
+    s = make_scene(scene, kernel)
     rays = W.random_rays(20000, 34)
     oracle = po.OracleScene(scene)
     ref, _ = oracle.intersect(rays)
@@ -153,11 +167,12 @@ def test_plain_and_instanced_objects_mixed(torch_cuda):
     assert {0, 1} <= meshes_hit and any(m >= 2 and m != W.NULL_INDEX for m in meshes_hit)
 
 
-def test_adversarial_rays(torch_cuda):
+@KERNELS
+def test_adversarial_rays(torch_cuda, kernel):
     mesh = W.heightfield_mesh(64, 41)
     scene = W.SceneDesc([mesh])
     rays = adversarial_rays(mesh, 42, 64)
-    s = lrx.Scene(scene)
+    s = make_scene(scene, kernel)
     gpu = gpu_trace(torch_cuda, s, rays)
     oracle = po.OracleScene(scene)
     ref, _ = oracle.intersect(rays)
@@ -171,11 +186,12 @@ def test_adversarial_rays(torch_cuda):
 
 
 @pytest.mark.parametrize("n_tris", [0, 1, 2, 3, 4, 9, 25])
-def test_tiny_and_empty_scenes(torch_cuda, n_tris):
+@KERNELS
+def test_tiny_and_empty_scenes(torch_cuda, kernel, n_tris):
     mesh = W.random_triangles(n_tris, 50 + n_tris, size=0.3) if n_tris else W.Mesh(
         np.zeros((0, 3), np.float32), np.zeros((0, 3), np.uint32))
     scene = W.SceneDesc([mesh])
-    s = lrx.Scene(scene)
+    s = make_scene(scene, kernel)
     rays = W.random_rays(4096, 51)
     gpu = gpu_trace(torch_cuda, s, rays)
     oracle = po.OracleScene(scene)
@@ -213,9 +229,10 @@ def test_host_entry_point_matches_device(torch_cuda):
     assert np.array_equal(h.view(np.uint8), d.view(np.uint8))
 
 
-def test_deterministic_and_batch_independent(torch_cuda):
+@KERNELS
+def test_deterministic_and_batch_independent(torch_cuda, kernel):
     scene, rays = W.config1(n_tris=30000, n_rays=100000, seed=71)
-    s = lrx.Scene(scene)
+    s = make_scene(scene, kernel)
     a = gpu_trace(torch_cuda, s, rays)
     b = gpu_trace(torch_cuda, s, rays, chunks=7)
     assert np.array_equal(a.view(np.uint8), b.view(np.uint8))
@@ -238,9 +255,10 @@ def test_instance_update_matches_rebuilt_oracle(torch_cuda):
     assert_parity(gpu, ref, oracle, closest, min_hit_rate=0.02)
 
 
-def test_counted_trace(torch_cuda):
+@KERNELS
+def test_counted_trace(torch_cuda, kernel):
     scene, rays = W.config1(n_tris=20000, n_rays=40000, seed=81)
-    s = lrx.Scene(scene)
+    s = make_scene(scene, kernel)
     torch = torch_cuda
     d_r = torch.from_numpy(rays.view(np.uint8).copy()).cuda()
     d_h = torch.empty(rays.shape[0] * 20, dtype=torch.uint8, device="cuda")
