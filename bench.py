@@ -271,10 +271,13 @@ def run_lrx(args):
     def up(a):
         return torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).reshape(-1).copy()).cuda(local)
 
+    log(f"[bench] {time.strftime('%H:%M:%S')} scene built {info}")
     d_prim = up(primary)
     d_ph = torch.empty(primary.shape[0] * HIT_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
+    torch.cuda.synchronize()
     scene.trace(d_prim.data_ptr(), d_ph.data_ptr(), primary.shape[0], lrx.LRX_TRACE_CLOSEST, st)
     stream.synchronize()
+    log(f"[bench] {time.strftime('%H:%M:%S')} primary hits traced")
     ph = d_ph.cpu().numpy().view(W.HIT_DTYPE)
     bounce, shadow = derived_rays(scene_desc, primary, ph, W.BASE_SEED + 100)
     sets = [("primary", primary, lrx.LRX_TRACE_CLOSEST), ("bounce", bounce, lrx.LRX_TRACE_CLOSEST),
@@ -289,12 +292,17 @@ def run_lrx(args):
     # traversal counters (untimed): nodes / triangles fetched per ray
     counts = {}
     cbuf = torch.zeros(4, dtype=torch.int64, device=f"cuda:{local}")
+    log(f"[bench] {time.strftime('%H:%M:%S')} rays ready, counting pass")
     for name, dr, dh, n, mode in dev:
         cbuf.zero_()
+        torch.cuda.synchronize()  # the zeroing ran on torch's stream, the trace runs on `st`
         scene.trace_counted(dr.data_ptr(), dh.data_ptr(), n, mode, cbuf.data_ptr(), st)
         stream.synchronize()
         nodes, tris, insts, rays = cbuf.cpu().tolist()
         counts[name] = (nodes / n, tris / n, insts / n)
+    if scene.device_status(st) != 0:
+        raise RuntimeError("device status word set during the counting pass")
+    log(f"[bench] {time.strftime('%H:%M:%S')} counting done {counts}")
     alg_bytes = {}
     for name, dr, dh, n, mode in dev:
         nn, nt, ni = counts[name]
@@ -313,6 +321,7 @@ def run_lrx(args):
     stream.synchronize()
     if scene.device_status(st) != 0:
         raise RuntimeError("device status word set during warm-up")
+    log(f"[bench] {time.strftime('%H:%M:%S')} warm-up done, timing {args.steps} steps")
 
     ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in dev]
           for _ in range(args.steps)]
@@ -327,6 +336,9 @@ def run_lrx(args):
     end.record(stream)
     torch.cuda.synchronize()
     clk = clocks.stop()
+    log(f"[bench] {time.strftime('%H:%M:%S')} timed region done")
+    if scene.device_status(st) != 0:
+        raise RuntimeError("device status word set during the timed steps")
     d.barrier()
     elapsed_ms = start.elapsed_time(end)
     elapsed_ms = d.max(elapsed_ms)

@@ -646,6 +646,12 @@ static lrx_status trace_common(lrx_scene *s, const void *d_rays, void *d_hits, u
 	a.any_hit = mode == LRX_TRACE_ANY;
 	a.status = s->status.as<uint32_t>();
 	a.counters = reinterpret_cast<unsigned long long *>(d_counters);
+	// A correct walk visits each node at most once per BLAS entry, so a ray
+	// never needs more than (instances + 1) x nodes visits.
+	{
+		const uint64_t lim = (uint64_t)(s->info.instance_count + 1) * (s->info.node_count + 1) + 64;
+		a.visit_limit = (uint32_t)std::min<uint64_t>(lim, kMaxVisits);
+	}
 	a.kernel = s->tcfg.kernel;
 	a.blocks_per_sm = s->tcfg.blocks_per_sm;
 	a.refill_min = s->tcfg.refill_min;

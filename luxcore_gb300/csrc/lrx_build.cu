@@ -364,6 +364,42 @@ __global__ void __launch_bounds__(128) k_collapse(const uint2 *__restrict__ item
 	}
 }
 
+// Structural check of a finished wide BVH: every node but the root is the
+// child of exactly one node, every leaf-order slot is referenced by exactly
+// one leaf, and every index is in range.  Counts go to refs[0..n_nodes) and
+// refs[n_nodes..n_nodes+n_prims); bad indices set counters[C_ERR].
+__global__ void k_validate_refs(const WideNode *__restrict__ nodes, uint32_t n_nodes, uint32_t n_prims,
+		uint32_t *refs, uint32_t *counters) {
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n_nodes) return;
+	const WideNode nd = nodes[i];
+	const uint32_t imask = nd.w[0].w >> 24;
+	const uint32_t child_base = nd.w[1].x, tri_base = nd.w[1].y;
+	uint32_t rank = 0;
+	for (int s = 0; s < 8; ++s) {
+		const uint32_t m = ((s < 4 ? nd.w[1].z : nd.w[1].w) >> ((s & 3) * 8)) & 0xffu;
+		if (imask & (1u << s)) {
+			const uint32_t c = child_base + rank++;
+			if (c == 0 || c >= n_nodes) atomicOr(&counters[C_ERR], 4u);
+			else atomicAdd(&refs[c], 1u);
+		} else if (m) {
+			const uint32_t cnt = __popc((m >> 5) & 7u), off = m & 31u;
+			for (uint32_t k = 0; k < cnt; ++k) {
+				const uint32_t t = tri_base + off + k;
+				if (t >= n_prims) atomicOr(&counters[C_ERR], 8u);
+				else atomicAdd(&refs[n_nodes + t], 1u);
+			}
+		}
+	}
+}
+
+__global__ void k_validate_counts(const uint32_t *refs, uint32_t n_nodes, uint32_t n_prims, uint32_t *counters) {
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n_nodes + n_prims) return;
+	const uint32_t want = i == 0 ? 0u : 1u;
+	if (refs[i] != want) atomicOr(&counters[C_ERR], 16u);
+}
+
 __global__ void k_init_collapse(uint2 *queue, uint32_t *counters) {
 	queue[0] = make_uint2(counters[C_ROOT], 0u);
 	counters[C_QA] = 1u;
@@ -470,6 +506,29 @@ lrx_status build_wide_bvh(uint32_t n, const float4 *d_lo, const float4 *d_hi, ui
 	if (host_counters[C_ERR] != 0 || host_counters[C_TRIS] != n) {
 		set_error("BVH collapse lost primitives");
 		return LRX_ERR_BUILD;
+	}
+	// Validate the structure before anyone traverses it.  The reference
+	// counts reuse the (now idle) Morton key buffer.
+	{
+		const uint32_t n_nodes = host_counters[C_NODES];
+		const size_t ref_bytes = sizeof(uint32_t) * ((size_t)n_nodes + n);
+		if (ref_bytes > S.keys.bytes) {
+			set_error("BVH validation scratch too small");
+			return LRX_ERR_BUILD;
+		}
+		uint32_t *refs = S.keys.as<uint32_t>();
+		LRX_CUDA(cudaMemsetAsync(refs, 0, ref_bytes, st));
+		k_validate_refs<<<blocks_for(n_nodes, 256), 256, 0, st>>>(S.wide_nodes.as<WideNode>(), n_nodes, n, refs,
+				counters);
+		k_validate_counts<<<blocks_for((uint64_t)n_nodes + n, 256), 256, 0, st>>>(refs, n_nodes, n, counters);
+		LRX_CUDA(cudaGetLastError());
+		uint32_t err = 0;
+		LRX_CUDA(cudaMemcpyAsync(&err, counters + C_ERR, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+		LRX_CUDA(cudaStreamSynchronize(st));
+		if (err != 0) {
+			set_error("BVH validation failed (code " + std::to_string(err) + ")");
+			return LRX_ERR_BUILD;
+		}
 	}
 	out->node_count = host_counters[C_NODES];
 	out->depth = depth;

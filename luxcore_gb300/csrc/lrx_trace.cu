@@ -197,7 +197,7 @@ __device__ __forceinline__ bool trav_step(Traversal &T, const TraceArgs &a, Coun
 	const uint32_t s = j ^ T.ray.oct;
 	const uint32_t node = T.cur.x + __popc(T.cur.y & ((1u << s) - 1u) & 0xffu);
 	if ((T.cur.y >> 24) && !push(T, a, T.cur)) return true;
-	if (++T.visits > kMaxVisits) {
+	if (++T.visits > a.visit_limit) {
 		atomicOr(a.status, kStatusVisitLimit);
 		return true;
 	}
