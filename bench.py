@@ -263,7 +263,7 @@ def run_lrx(args):
     with torch.cuda.stream(stream):
         scene = lrx.Scene(scene_desc, stream=st)
     build_s = time.perf_counter() - t0
-    scene.set_trace_config(args.kernel, args.blocks_per_sm, args.refill_min)
+    scene.set_trace_config(args.block_size, args.postpone)
     info = scene.info()
 
     primary = W.pinhole_rays(1024, 1024)
@@ -346,21 +346,24 @@ def run_lrx(args):
                for j, (name, *_rest) in enumerate(dev)}
     value = rays_per_step * args.steps * ws / (elapsed_ms / 1e3) / 1e6
 
-    # the same sets with the one-thread-per-ray kernel (the reference's work
-    # layout), for comparison; untimed by the step clock
+    # the same sets under other launch configurations (block size, postpone),
+    # for comparison; outside the timed region
     alt = {}
-    if not args.no_alt_kernel:
-        scene.set_trace_config(lrx.LRX_KERNEL_SIMPLE)
-        for name, dr, dh, n, mode in dev:
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            scene.trace(dr.data_ptr(), dh.data_ptr(), n, mode, st)
-            e0.record(stream)
-            for _ in range(5):
+    if args.sweep:
+        for bs, pp in [(32, 0), (64, 0), (128, 0), (256, 0), (64, 8), (128, 8), (128, 16), (256, 8)]:
+            scene.set_trace_config(bs, pp)
+            key = f"b{bs}-p{pp}"
+            alt[key] = {}
+            for name, dr, dh, n, mode in dev:
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 scene.trace(dr.data_ptr(), dh.data_ptr(), n, mode, st)
-            e1.record(stream)
-            e1.synchronize()
-            alt[name] = round(n * 5 / (e0.elapsed_time(e1) / 1e3) / 1e6, 1)
-        scene.set_trace_config(args.kernel, args.blocks_per_sm, args.refill_min)
+                e0.record(stream)
+                for _ in range(5):
+                    scene.trace(dr.data_ptr(), dh.data_ptr(), n, mode, st)
+                e1.record(stream)
+                e1.synchronize()
+                alt[key][name] = round(n * 5 / (e0.elapsed_time(e1) / 1e3) / 1e6, 1)
+        scene.set_trace_config(args.block_size, args.postpone)
 
     # roofline of the traversal kernel: algorithmic bytes / kernel time
     peak, peak_kind = load_peaks()
@@ -419,7 +422,7 @@ def run_lrx(args):
                 "per_set_Mrays": {name: round(n / (kern_ms[name] / 1e3) / 1e6, 1) for name, _, _, n, _ in dev},
                 "nodes_tris_per_ray": {k: [round(v[0], 2), round(v[1], 2)] for k, v in counts.items()},
                 "trace_config": scene.trace_config(),
-                "simple_kernel_per_set_Mrays": alt,
+                "config_sweep_Mrays": alt,
             },
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": traffic,
@@ -447,10 +450,9 @@ def main():
                     help="CPU legs trace every Nth ray of each set")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (lrx_trace_host) leg")
-    ap.add_argument("--no-alt-kernel", action="store_true", help="skip the one-thread-per-ray comparison")
-    ap.add_argument("--kernel", type=int, default=1, help="0 = one thread per ray, 1 = persistent (default)")
-    ap.add_argument("--blocks-per-sm", type=int, default=0)
-    ap.add_argument("--refill-min", type=int, default=0)
+    ap.add_argument("--sweep", action="store_true", help="also time other launch configurations")
+    ap.add_argument("--block-size", type=int, default=128)
+    ap.add_argument("--postpone", type=int, default=0)
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3 (timing rule)")

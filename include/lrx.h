@@ -157,13 +157,13 @@ lrx_status lrx_trace_host(lrx_scene *scene, const lrx_ray *h_rays, lrx_hit *h_hi
 		uint32_t count, uint32_t mode, void *stream);
 
 /* Traversal launch configuration of a scene (what the autotuner chooses). */
-#define LRX_KERNEL_SIMPLE 0u      /* one thread per ray, as the reference's kernel */
-#define LRX_KERNEL_PERSISTENT 1u  /* persistent blocks, warp-level dynamic ray fetch (default) */
 typedef struct lrx_trace_config {
 	uint32_t struct_size;     /* sizeof(lrx_trace_config) */
-	uint32_t kernel;          /* LRX_KERNEL_* */
-	uint32_t blocks_per_sm;   /* persistent: resident blocks per SM (0 = default 8) */
-	uint32_t refill_min;      /* persistent: idle lanes in a warp before it fetches rays (0 = default 1) */
+	uint32_t block_size;      /* threads per block: a multiple of 32 in [32, 512] (0 = 128) */
+	uint32_t postpone;        /* leaf triangles are tested only while at least this many lanes
+	                             of the warp test triangles; otherwise they are deferred while
+	                             node work remains (0 = never defer) */
+	uint32_t reserved;
 } lrx_trace_config;
 
 /* Sets / reads the launch configuration lrx_trace uses for this scene.

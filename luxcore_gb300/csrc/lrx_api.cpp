@@ -180,7 +180,7 @@ struct lrx_scene {
 	uint32_t tlas_capacity = 0;
 	uint32_t blas_node_total = 0;
 	lrx_build_opts opts{};
-	lrx_trace_config tcfg{sizeof(lrx_trace_config), LRX_KERNEL_PERSISTENT, 0, 0};
+	lrx_trace_config tcfg{sizeof(lrx_trace_config), kTraceBlock, 0, 0};
 	lrx_scene_info info{};
 	BuildScratch scratch;
 	std::mutex mu;
@@ -652,9 +652,8 @@ static lrx_status trace_common(lrx_scene *s, const void *d_rays, void *d_hits, u
 		const uint64_t lim = (uint64_t)(s->info.instance_count + 1) * (s->info.node_count + 1) + 64;
 		a.visit_limit = (uint32_t)std::min<uint64_t>(lim, kMaxVisits);
 	}
-	a.kernel = s->tcfg.kernel;
-	a.blocks_per_sm = s->tcfg.blocks_per_sm;
-	a.refill_min = s->tcfg.refill_min;
+	a.block_size = s->tcfg.block_size;
+	a.postpone = s->tcfg.postpone;
 	return launch_trace(a, st);
 }
 
@@ -663,12 +662,14 @@ lrx_status lrx_scene_set_trace_config(lrx_scene *s, const lrx_trace_config *c) {
 		set_error("lrx_scene_set_trace_config: null argument or old struct");
 		return LRX_ERR_INVALID_ARGUMENT;
 	}
-	if (c->kernel > LRX_KERNEL_PERSISTENT || c->blocks_per_sm > 32 || c->refill_min > 32) {
+	const uint32_t bs = c->block_size ? c->block_size : kTraceBlock;
+	if (bs < 32 || bs > 512 || (bs & 31) || c->postpone > 32) {
 		set_error("lrx_scene_set_trace_config: value out of range");
 		return LRX_ERR_INVALID_ARGUMENT;
 	}
 	s->tcfg = *c;
 	s->tcfg.struct_size = sizeof(lrx_trace_config);
+	s->tcfg.block_size = bs;
 	return LRX_OK;
 }
 

@@ -107,13 +107,10 @@ struct TraceArgs {
 	uint32_t any_hit;
 	uint32_t *status;
 	unsigned long long *counters;  // nullptr unless counting
-	uint32_t kernel = 1;           // kKernelSimple or kKernelPersistent
-	uint32_t blocks_per_sm = 0;    // persistent kernel: resident blocks per SM (0 = default)
-	uint32_t refill_min = 0;       // persistent kernel: idle lanes before a refill (0 = default)
+	uint32_t block_size = 0;       // threads per block (0 = kTraceBlock)
+	uint32_t postpone = 0;         // min lanes testing triangles before deferring (0 = never)
 	uint32_t visit_limit = 1u << 24;  // node visits after which a ray is abandoned (status bit 1)
 };
-constexpr uint32_t kKernelSimple = 0;
-constexpr uint32_t kKernelPersistent = 1;
 constexpr uint32_t kTraceBlock = 128;
 
 lrx_status launch_trace(const TraceArgs &a, cudaStream_t stream);

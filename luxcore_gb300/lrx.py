@@ -32,8 +32,6 @@ EXPORTED = ["lrx_abi_version", "lrx_last_error", "lrx_scene_create", "lrx_scene_
             "lrx_scene_update_instances", "lrx_scene_get_info", "lrx_trace", "lrx_trace_host",
             "lrx_trace_counted", "lrx_scene_device_status", "lrx_trace_host_noalloc",
             "lrx_scene_set_trace_config", "lrx_scene_get_trace_config"]
-LRX_KERNEL_SIMPLE = 0
-LRX_KERNEL_PERSISTENT = 1
 LRX_NOALLOC_MAX_RAYS = 131072
 
 
@@ -59,8 +57,8 @@ class BuildOpts(ctypes.Structure):
 
 
 class TraceConfig(ctypes.Structure):
-    _fields_ = [("struct_size", ctypes.c_uint32), ("kernel", ctypes.c_uint32),
-                ("blocks_per_sm", ctypes.c_uint32), ("refill_min", ctypes.c_uint32)]
+    _fields_ = [("struct_size", ctypes.c_uint32), ("block_size", ctypes.c_uint32),
+                ("postpone", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
 
 
 class SceneInfo(ctypes.Structure):
@@ -177,14 +175,14 @@ class Scene:
         check(load().lrx_scene_get_info(self.handle, ctypes.byref(inf)))
         return inf.as_dict()
 
-    def set_trace_config(self, kernel: int = LRX_KERNEL_PERSISTENT, blocks_per_sm: int = 0, refill_min: int = 0):
-        c = TraceConfig(ctypes.sizeof(TraceConfig), kernel, blocks_per_sm, refill_min)
+    def set_trace_config(self, block_size: int = 128, postpone: int = 0):
+        c = TraceConfig(ctypes.sizeof(TraceConfig), block_size, postpone, 0)
         check(load().lrx_scene_set_trace_config(self.handle, ctypes.byref(c)))
 
     def trace_config(self) -> dict:
         c = TraceConfig()
         check(load().lrx_scene_get_trace_config(self.handle, ctypes.byref(c)))
-        return {"kernel": c.kernel, "blocks_per_sm": c.blocks_per_sm, "refill_min": c.refill_min}
+        return {"block_size": c.block_size, "postpone": c.postpone}
 
     def update_instances(self, scene: W.SceneDesc, stream: int = 0):
         objs = _object_array(scene)

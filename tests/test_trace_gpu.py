@@ -21,14 +21,14 @@ from parity import check_anyhit, compare  # noqa: E402
 pytestmark = pytest.mark.gpu
 
 SENT = 0xDEADBEEF
-KERNELS = pytest.mark.parametrize("kernel", [lrx.LRX_KERNEL_SIMPLE, lrx.LRX_KERNEL_PERSISTENT],
-                                  ids=["simple", "persistent"])
+# launch configurations every parity test runs under: (block size, postpone)
+KERNELS = pytest.mark.parametrize("kernel", [(128, 0), (64, 8), (256, 24)], ids=["b128", "b64-p8", "b256-p24"])
 
 
-def make_scene(desc, kernel=lrx.LRX_KERNEL_PERSISTENT, **kw):
+def make_scene(desc, kernel=(128, 0), **kw):
     s = lrx.Scene(desc, **kw)
-    s.set_trace_config(kernel)
-    assert s.trace_config()["kernel"] == kernel
+    s.set_trace_config(*kernel)
+    assert s.trace_config() == {"block_size": kernel[0], "postpone": kernel[1]}
     return s
 
 
