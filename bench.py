@@ -451,8 +451,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (lrx_trace_host) leg")
     ap.add_argument("--sweep", action="store_true", help="also time other launch configurations")
-    ap.add_argument("--block-size", type=int, default=128)
-    ap.add_argument("--postpone", type=int, default=0)
+    ap.add_argument("--block-size", type=int, default=64)
+    ap.add_argument("--postpone", type=int, default=8)
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3 (timing rule)")

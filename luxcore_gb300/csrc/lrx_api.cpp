@@ -180,7 +180,9 @@ struct lrx_scene {
 	uint32_t tlas_capacity = 0;
 	uint32_t blas_node_total = 0;
 	lrx_build_opts opts{};
-	lrx_trace_config tcfg{sizeof(lrx_trace_config), kTraceBlock, 0, 0};
+	// default launch: 64-thread blocks, triangles deferred below 8 lanes
+	// (best of a block-size x postpone sweep on the heightfield ray sets)
+	lrx_trace_config tcfg{sizeof(lrx_trace_config), 64, 8, 0};
 	lrx_scene_info info{};
 	BuildScratch scratch;
 	std::mutex mu;
