@@ -263,7 +263,7 @@ def run_lrx(args):
     with torch.cuda.stream(stream):
         scene = lrx.Scene(scene_desc, stream=st)
     build_s = time.perf_counter() - t0
-    scene.set_trace_config(args.block_size, args.postpone)
+    scene.set_trace_config(args.block_size, args.postpone, args.variant)
     info = scene.info()
 
     primary = W.pinhole_rays(1024, 1024)
@@ -350,9 +350,10 @@ def run_lrx(args):
     # for comparison; outside the timed region
     alt = {}
     if args.sweep:
-        for bs, pp in [(32, 0), (64, 0), (128, 0), (256, 0), (64, 8), (128, 8), (128, 16), (256, 8)]:
-            scene.set_trace_config(bs, pp)
-            key = f"b{bs}-p{pp}"
+        for bs, pp, var in [(64, 8, 0), (64, 8, 1), (64, 8, 2), (64, 8, 4), (64, 8, 6), (64, 8, 8), (64, 8, 9),
+                            (64, 8, 15), (32, 8, 9), (64, 16, 9), (128, 8, 1), (64, 4, 9)]:
+            scene.set_trace_config(bs, pp, var)
+            key = f"b{bs}-p{pp}-v{var}"
             alt[key] = {}
             for name, dr, dh, n, mode in dev:
                 e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -363,7 +364,7 @@ def run_lrx(args):
                 e1.record(stream)
                 e1.synchronize()
                 alt[key][name] = round(n * 5 / (e0.elapsed_time(e1) / 1e3) / 1e6, 1)
-        scene.set_trace_config(args.block_size, args.postpone)
+        scene.set_trace_config(args.block_size, args.postpone, args.variant)
 
     # roofline of the traversal kernel: algorithmic bytes / kernel time
     peak, peak_kind = load_peaks()
@@ -453,6 +454,7 @@ def main():
     ap.add_argument("--sweep", action="store_true", help="also time other launch configurations")
     ap.add_argument("--block-size", type=int, default=64)
     ap.add_argument("--postpone", type=int, default=8)
+    ap.add_argument("--variant", type=int, default=0, help="LRX_VARIANT_* bits")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3 (timing rule)")

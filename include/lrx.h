@@ -163,8 +163,12 @@ typedef struct lrx_trace_config {
 	uint32_t postpone;        /* leaf triangles are tested only while at least this many lanes
 	                             of the warp test triangles; otherwise they are deferred while
 	                             node work remains (0 = never defer) */
-	uint32_t reserved;
+	uint32_t variant;         /* LRX_VARIANT_* bits */
 } lrx_trace_config;
+#define LRX_VARIANT_MINMAX3 0x1u       /* 3-input min/max in the slab tests */
+#define LRX_VARIANT_SCENE_L2_KEEP 0x2u /* node/triangle loads marked evict-last in L2 */
+#define LRX_VARIANT_STREAM_RAYS 0x4u   /* ray loads / hit stores marked evict-first */
+#define LRX_VARIANT_OCCUPANCY 0x8u     /* register budget for 20 blocks of 64 threads per SM (blocks <= 64) */
 
 /* Sets / reads the launch configuration lrx_trace uses for this scene.
  * No reference counterpart (the reference fixes 32-thread blocks,

@@ -656,6 +656,7 @@ static lrx_status trace_common(lrx_scene *s, const void *d_rays, void *d_hits, u
 	}
 	a.block_size = s->tcfg.block_size;
 	a.postpone = s->tcfg.postpone;
+	a.variant = s->tcfg.variant;
 	return launch_trace(a, st);
 }
 
@@ -665,7 +666,7 @@ lrx_status lrx_scene_set_trace_config(lrx_scene *s, const lrx_trace_config *c) {
 		return LRX_ERR_INVALID_ARGUMENT;
 	}
 	const uint32_t bs = c->block_size ? c->block_size : kTraceBlock;
-	if (bs < 32 || bs > 512 || (bs & 31) || c->postpone > 32) {
+	if (bs < 32 || bs > 512 || (bs & 31) || c->postpone > 32 || c->variant > 0xfu) {
 		set_error("lrx_scene_set_trace_config: value out of range");
 		return LRX_ERR_INVALID_ARGUMENT;
 	}

@@ -109,6 +109,7 @@ struct TraceArgs {
 	unsigned long long *counters;  // nullptr unless counting
 	uint32_t block_size = 0;       // threads per block (0 = kTraceBlock)
 	uint32_t postpone = 0;         // min lanes testing triangles before deferring (0 = never)
+	uint32_t variant = 0;          // lrx_trace_config.variant bits
 	uint32_t visit_limit = 1u << 24;  // node visits after which a ray is abandoned (status bit 1)
 };
 constexpr uint32_t kTraceBlock = 128;

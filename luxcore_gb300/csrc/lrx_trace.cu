@@ -50,13 +50,54 @@ struct NodeHits {
 	uint32_t tmask;  // leaf triangles, bit k = triangle tri_base + k
 };
 
+// Variant bits (lrx_trace_config.variant):
+constexpr uint32_t kVarMinMax3 = 1u;      // compile time: 3-input min/max for the slab tests
+constexpr uint32_t kVarSceneEvictLast = 2u;  // runtime: node/triangle loads keep L2 lines (evict_last)
+constexpr uint32_t kVarStreamRays = 4u;   // runtime: ray loads / hit stores stream past L2 (evict_first)
+constexpr uint32_t kVarOccupancy = 8u;    // compile time: register budget for 20 blocks of 64 per SM
+
+// 3-input max / min (max.f32 d, a, b, c on sm_100+): a NaN input is
+// dropped like fmaxf/fminf drop it.
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+	float d;
+	asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+	return d;
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+	float d;
+	asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+	return d;
+}
+
+__device__ __forceinline__ uint64_t evict_last_policy() {
+	uint64_t pol;
+	asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+	return pol;
+}
+
+// Read-only 16-B scene load, optionally with an L2 evict_last policy.
+__device__ __forceinline__ uint4 ld_scene(const uint4 *p, bool keep, uint64_t pol) {
+	if (!keep) return __ldg(p);
+	uint4 v;
+	asm volatile("ld.global.nc.L2::cache_hint.v4.u32 {%0,%1,%2,%3}, [%4], %5;"
+			: "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p), "l"(pol));
+	return v;
+}
+
+__device__ __forceinline__ float4 ld_scene_f4(const float4 *p, bool keep, uint64_t pol) {
+	const uint4 v = ld_scene(reinterpret_cast<const uint4 *>(p), keep, pol);
+	return make_float4(__uint_as_float(v.x), __uint_as_float(v.y), __uint_as_float(v.z), __uint_as_float(v.w));
+}
+
 // Slab test of the 8 quantised child boxes.  t = q * (scale * idir) +
 // (origin - o) * idir; NaN plane distances (zero direction components) are
 // dropped by fminf/fmaxf, which only ever keeps a child.
+template <bool MM3>
 __device__ __forceinline__ NodeHits intersect_node(const WideNode *__restrict__ nodes, uint32_t idx,
-		const ActiveRay &r, float tmin, float tmax) {
+		const ActiveRay &r, float tmin, float tmax, bool keep, uint64_t pol) {
 	const uint4 *p = reinterpret_cast<const uint4 *>(nodes + idx);
-	const uint4 w0 = __ldg(p), w1 = __ldg(p + 1), w2 = __ldg(p + 2), w3 = __ldg(p + 3), w4 = __ldg(p + 4);
+	const uint4 w0 = ld_scene(p, keep, pol), w1 = ld_scene(p + 1, keep, pol), w2 = ld_scene(p + 2, keep, pol),
+			w3 = ld_scene(p + 3, keep, pol), w4 = ld_scene(p + 4, keep, pol);
 	NodeHits h;
 	h.child_base = w1.x;
 	h.tri_base = w1.y;
@@ -81,10 +122,12 @@ __device__ __forceinline__ NodeHits intersect_node(const WideNode *__restrict__ 
 #define LRX_CHILD(S)                                                                                      \
 	{                                                                                                     \
 		constexpr int H = (S) >> 2, K = (S) & 3;                                                          \
-		const float tn = fmaxf(fmaxf(fmaf(byte_as_float<K>(nx[H]), ax, bx), fmaf(byte_as_float<K>(ny[H]), ay, by)), \
-				fmaxf(fmaf(byte_as_float<K>(nz[H]), az, bz), tmin));                                      \
-		const float tf = fminf(fminf(fmaf(byte_as_float<K>(fx[H]), ax, bx), fmaf(byte_as_float<K>(fy[H]), ay, by)), \
-				fminf(fmaf(byte_as_float<K>(fz[H]), az, bz), tmax));                                      \
+		const float tnx = fmaf(byte_as_float<K>(nx[H]), ax, bx), tny = fmaf(byte_as_float<K>(ny[H]), ay, by); \
+		const float tnz = fmaf(byte_as_float<K>(nz[H]), az, bz);                                          \
+		const float tfx = fmaf(byte_as_float<K>(fx[H]), ax, bx), tfy = fmaf(byte_as_float<K>(fy[H]), ay, by); \
+		const float tfz = fmaf(byte_as_float<K>(fz[H]), az, bz);                                          \
+		const float tn = MM3 ? fmaxf(max3f(tnx, tny, tnz), tmin) : fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin)); \
+		const float tf = MM3 ? fminf(min3f(tfx, tfy, tfz), tmax) : fminf(fminf(tfx, tfy), fminf(tfz, tmax)); \
 		const uint32_t m = (mw[H] >> (8 * K)) & 0xffu;                                                    \
 		if (tn <= tf && m != 0u) {                                                                        \
 			if (h.imask & (1u << (S))) ih |= 1u << ((S) ^ r.oct);                                         \
@@ -102,17 +145,28 @@ __device__ __forceinline__ bool finite3(float3 v) {
 	return isfinite(v.x) && isfinite(v.y) && isfinite(v.z);
 }
 
-template <bool ANY, bool TWO_LEVEL, bool COUNT>
-__global__ void k_trace(TraceArgs a) {
+template <bool ANY, bool TWO_LEVEL, bool COUNT, uint32_t CV>
+__global__ void __launch_bounds__((CV & kVarOccupancy) ? 64 : 1024, (CV & kVarOccupancy) ? 20 : 0)
+k_trace(TraceArgs a) {
+	constexpr bool MM3 = (CV & kVarMinMax3) != 0;
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	bool active = i < a.count;
 	if (!COUNT && !active) return;
+	const bool keep = (a.variant & kVarSceneEvictLast) != 0;
+	const bool stream = (a.variant & kVarStreamRays) != 0;
+	const uint64_t pol = keep ? evict_last_policy() : 0ull;
 	float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0, r2 = r0;
 	if (active) {
 		const float4 *rp = reinterpret_cast<const float4 *>(a.rays) + 3 * (size_t)i;
-		r0 = __ldg(rp);
-		r1 = __ldg(rp + 1);
-		r2 = __ldg(rp + 2);
+		if (stream) {
+			r0 = __ldcs(rp);
+			r1 = __ldcs(rp + 1);
+			r2 = __ldcs(rp + 2);
+		} else {
+			r0 = __ldg(rp);
+			r1 = __ldg(rp + 1);
+			r2 = __ldg(rp + 2);
+		}
 		if (__float_as_uint(r2.y) & LRX_RAY_FLAGS_MASKED) active = false;  // bvh.cl:243-244
 	}
 	if (!COUNT && !active) return;
@@ -154,7 +208,7 @@ __global__ void k_trace(TraceArgs a) {
 					break;
 				}
 				if (COUNT) ++n_nodes;
-				const NodeHits h = intersect_node(a.nodes, node, ray, mint, best_t);
+				const NodeHits h = intersect_node<MM3>(a.nodes, node, ray, mint, best_t, keep, pol);
 				ng = make_uint2(h.child_base, (h.ihits << 24) | h.imask);
 				tg = make_uint2(h.tri_base, h.tmask);
 			} else {
@@ -194,7 +248,8 @@ __global__ void k_trace(TraceArgs a) {
 					const uint32_t k = __ffs(tg.y) - 1;
 					tg.y &= tg.y - 1;
 					const float4 *tp = reinterpret_cast<const float4 *>(a.tris + tg.x + k);
-					const float4 ta = __ldg(tp), tb = __ldg(tp + 1), tc = __ldg(tp + 2);
+					const float4 ta = ld_scene_f4(tp, keep, pol), tb = ld_scene_f4(tp + 1, keep, pol),
+							tc = ld_scene_f4(tp + 2, keep, pol);
 					if (COUNT) ++n_tris;
 					float t, b1, b2;
 					if (tri_intersect(ray.o, ray.d, mint, best_t, make_float3(ta.x, ta.y, ta.z),
@@ -231,11 +286,19 @@ __global__ void k_trace(TraceArgs a) {
 	}
 	if (active) {
 		uint32_t *hp = reinterpret_cast<uint32_t *>(a.hits) + 5 * (size_t)i;
-		hp[0] = __float_as_uint(best_t);
-		hp[1] = __float_as_uint(best_b1);
-		hp[2] = __float_as_uint(best_b2);
-		hp[3] = best_mesh;
-		hp[4] = best_tri;
+		if (stream) {
+			__stcs(hp, __float_as_uint(best_t));
+			__stcs(hp + 1, __float_as_uint(best_b1));
+			__stcs(hp + 2, __float_as_uint(best_b2));
+			__stcs(hp + 3, best_mesh);
+			__stcs(hp + 4, best_tri);
+		} else {
+			hp[0] = __float_as_uint(best_t);
+			hp[1] = __float_as_uint(best_b1);
+			hp[2] = __float_as_uint(best_b2);
+			hp[3] = best_mesh;
+			hp[4] = best_tri;
+		}
 	}
 	if (COUNT) {
 		// every lane of the block reaches this point in the counting variant
@@ -263,14 +326,26 @@ lrx_status launch_trace(const TraceArgs &a, cudaStream_t st) {
 	}
 	const uint32_t grid = (a.count + bs - 1) / bs;
 	const bool cnt = a.counters != nullptr;
-#define LRX_LAUNCH(A, T, C) k_trace<A, T, C><<<grid, bs, 0, st>>>(a)
-	if (a.any_hit) {
-		if (a.two_level) { if (cnt) LRX_LAUNCH(true, true, true); else LRX_LAUNCH(true, true, false); }
-		else { if (cnt) LRX_LAUNCH(true, false, true); else LRX_LAUNCH(true, false, false); }
-	} else {
-		if (a.two_level) { if (cnt) LRX_LAUNCH(false, true, true); else LRX_LAUNCH(false, true, false); }
-		else { if (cnt) LRX_LAUNCH(false, false, true); else LRX_LAUNCH(false, false, false); }
+	// compile-time variants; the occupancy-bounded build only takes <= 64-thread blocks
+	uint32_t cv = a.variant & (kVarMinMax3 | kVarOccupancy);
+	if (bs > 64) cv &= ~kVarOccupancy;
+	if (cnt) cv = 0;
+#define LRX_LAUNCH(A, T, C, V) k_trace<A, T, C, V><<<grid, bs, 0, st>>>(a)
+#define LRX_LAUNCH_V(A, T)                                         \
+	switch (cv) {                                                  \
+	case kVarMinMax3: LRX_LAUNCH(A, T, false, kVarMinMax3); break; \
+	case kVarOccupancy: LRX_LAUNCH(A, T, false, kVarOccupancy); break; \
+	case kVarMinMax3 | kVarOccupancy: LRX_LAUNCH(A, T, false, kVarMinMax3 | kVarOccupancy); break; \
+	default: LRX_LAUNCH(A, T, false, 0u); break;                   \
 	}
+	if (a.any_hit) {
+		if (a.two_level) { if (cnt) LRX_LAUNCH(true, true, true, 0u); else LRX_LAUNCH_V(true, true); }
+		else { if (cnt) LRX_LAUNCH(true, false, true, 0u); else LRX_LAUNCH_V(true, false); }
+	} else {
+		if (a.two_level) { if (cnt) LRX_LAUNCH(false, true, true, 0u); else LRX_LAUNCH_V(false, true); }
+		else { if (cnt) LRX_LAUNCH(false, false, true, 0u); else LRX_LAUNCH_V(false, false); }
+	}
+#undef LRX_LAUNCH_V
 #undef LRX_LAUNCH
 	LRX_CUDA(cudaGetLastError());
 	return LRX_OK;

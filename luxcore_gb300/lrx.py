@@ -58,7 +58,7 @@ class BuildOpts(ctypes.Structure):
 
 class TraceConfig(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_uint32), ("block_size", ctypes.c_uint32),
-                ("postpone", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("postpone", ctypes.c_uint32), ("variant", ctypes.c_uint32)]
 
 
 class SceneInfo(ctypes.Structure):
@@ -175,14 +175,14 @@ class Scene:
         check(load().lrx_scene_get_info(self.handle, ctypes.byref(inf)))
         return inf.as_dict()
 
-    def set_trace_config(self, block_size: int = 128, postpone: int = 0):
-        c = TraceConfig(ctypes.sizeof(TraceConfig), block_size, postpone, 0)
+    def set_trace_config(self, block_size: int = 64, postpone: int = 8, variant: int = 0):
+        c = TraceConfig(ctypes.sizeof(TraceConfig), block_size, postpone, variant)
         check(load().lrx_scene_set_trace_config(self.handle, ctypes.byref(c)))
 
     def trace_config(self) -> dict:
         c = TraceConfig()
         check(load().lrx_scene_get_trace_config(self.handle, ctypes.byref(c)))
-        return {"block_size": c.block_size, "postpone": c.postpone}
+        return {"block_size": c.block_size, "postpone": c.postpone, "variant": c.variant}
 
     def update_instances(self, scene: W.SceneDesc, stream: int = 0):
         objs = _object_array(scene)

@@ -21,14 +21,15 @@ from parity import check_anyhit, compare  # noqa: E402
 pytestmark = pytest.mark.gpu
 
 SENT = 0xDEADBEEF
-# launch configurations every parity test runs under: (block size, postpone)
-KERNELS = pytest.mark.parametrize("kernel", [(128, 0), (64, 8), (256, 24)], ids=["b128", "b64-p8", "b256-p24"])
+# launch configurations every parity test runs under: (block size, postpone, variant bits)
+KERNELS = pytest.mark.parametrize("kernel", [(128, 0, 0), (64, 8, 0), (256, 24, 0), (64, 8, 0xF), (128, 8, 0x7)],
+                                  ids=["b128", "b64-p8", "b256-p24", "b64-p8-allvariants", "b128-p8-mm3-hints"])
 
 
-def make_scene(desc, kernel=(128, 0), **kw):
+def make_scene(desc, kernel=(64, 8, 0), **kw):
     s = lrx.Scene(desc, **kw)
     s.set_trace_config(*kernel)
-    assert s.trace_config() == {"block_size": kernel[0], "postpone": kernel[1]}
+    assert s.trace_config() == {"block_size": kernel[0], "postpone": kernel[1], "variant": kernel[2]}
     return s
 
 
