@@ -350,8 +350,8 @@ def run_lrx(args):
     # for comparison; outside the timed region
     alt = {}
     if args.sweep:
-        for bs, pp, var in [(64, 8, 0), (64, 8, 1), (64, 8, 2), (64, 8, 4), (64, 8, 6), (64, 8, 8), (64, 8, 9),
-                            (64, 8, 15), (32, 8, 9), (64, 16, 9), (128, 8, 1), (64, 4, 9)]:
+        for bs, pp, var in [(64, 8, 0), (64, 8, 16), (64, 8, 17), (64, 8, 20), (64, 8, 24), (64, 8, 25), (32, 8, 16),
+                            (128, 8, 16), (64, 0, 16), (64, 16, 16), (64, 8, 1), (64, 8, 4)]:
             scene.set_trace_config(bs, pp, var)
             key = f"b{bs}-p{pp}-v{var}"
             alt[key] = {}

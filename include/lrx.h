@@ -169,6 +169,8 @@ typedef struct lrx_trace_config {
 #define LRX_VARIANT_SCENE_L2_KEEP 0x2u /* node/triangle loads marked evict-last in L2 */
 #define LRX_VARIANT_STREAM_RAYS 0x4u   /* ray loads / hit stores marked evict-first */
 #define LRX_VARIANT_OCCUPANCY 0x8u     /* register budget for 20 blocks of 64 threads per SM (blocks <= 64) */
+#define LRX_VARIANT_SORT_RAYS 0x10u    /* reorder batches of >= 32768 rays by direction octant and
+                                          origin before tracing (hits stay in caller order) */
 
 /* Sets / reads the launch configuration lrx_trace uses for this scene.
  * No reference counterpart (the reference fixes 32-thread blocks,

@@ -186,6 +186,7 @@ struct lrx_scene {
 	lrx_scene_info info{};
 	BuildScratch scratch;
 	std::mutex mu;
+	float bounds_lo[3] = {0, 0, 0}, bounds_hi[3] = {0, 0, 0};  // world box of the root
 };
 
 int lrx::scene_device(const lrx_scene *scene) { return scene->device; }
@@ -348,6 +349,8 @@ lrx_status build_tlas(lrx_scene *s, const lrx_object_desc *objects, uint32_t n_o
 		return rc;
 	LRX_CUDA(cudaStreamSynchronize(st));
 	s->root = s->tlas_node_offset;
+	std::memcpy(s->bounds_lo, r.lo, sizeof(r.lo));
+	std::memcpy(s->bounds_hi, r.hi, sizeof(r.hi));
 	s->info.node_count = s->blas_node_total + r.node_count;
 	s->info.max_depth = std::max(s->info.max_depth, r.depth);
 	return LRX_OK;
@@ -555,6 +558,10 @@ lrx_status lrx_scene_create(const lrx_mesh_desc *meshes, uint32_t mesh_count, co
 			if ((rc = build_tlas(s, objs.data(), n_obj, st)) != LRX_OK) return rc;
 		} else {
 			s->root = s->blas.empty() ? kNull : 0u;
+			if (!s->blas.empty()) {
+				std::memcpy(s->bounds_lo, s->blas[0].lo, sizeof(s->bounds_lo));
+				std::memcpy(s->bounds_hi, s->blas[0].hi, sizeof(s->bounds_hi));
+			}
 		}
 		// scratch is kept only where instance updates need it
 		if (!s->two_level) s->scratch = BuildScratch();
@@ -657,6 +664,8 @@ static lrx_status trace_common(lrx_scene *s, const void *d_rays, void *d_hits, u
 	a.block_size = s->tcfg.block_size;
 	a.postpone = s->tcfg.postpone;
 	a.variant = s->tcfg.variant;
+	if ((a.variant & kVarSortRays) && count >= kSortMinRays && s->root != kNull)
+		return launch_trace_sorted(a, s->bounds_lo, s->bounds_hi, st);
 	return launch_trace(a, st);
 }
 
@@ -666,7 +675,7 @@ lrx_status lrx_scene_set_trace_config(lrx_scene *s, const lrx_trace_config *c) {
 		return LRX_ERR_INVALID_ARGUMENT;
 	}
 	const uint32_t bs = c->block_size ? c->block_size : kTraceBlock;
-	if (bs < 32 || bs > 512 || (bs & 31) || c->postpone > 32 || c->variant > 0xfu) {
+	if (bs < 32 || bs > 512 || (bs & 31) || c->postpone > 32 || c->variant > 0x1fu) {
 		set_error("lrx_scene_set_trace_config: value out of range");
 		return LRX_ERR_INVALID_ARGUMENT;
 	}

@@ -111,10 +111,17 @@ struct TraceArgs {
 	uint32_t postpone = 0;         // min lanes testing triangles before deferring (0 = never)
 	uint32_t variant = 0;          // lrx_trace_config.variant bits
 	uint32_t visit_limit = 1u << 24;  // node visits after which a ray is abandoned (status bit 1)
+	const uint32_t *order = nullptr;  // thread i traces ray order[i] (sorted launches)
 };
 constexpr uint32_t kTraceBlock = 128;
+constexpr uint32_t kVarSortRays = 0x10u;   // reorder rays by octant + origin before tracing
+constexpr uint32_t kSortMinRays = 32768;   // smaller batches are traced in caller order
 
 lrx_status launch_trace(const TraceArgs &a, cudaStream_t stream);
+
+// Sorts the rays (octant, origin Morton code in [lo, hi]) and traces them in
+// that order; scratch from a stream-ordered pool.  Hits land in caller order.
+lrx_status launch_trace_sorted(const TraceArgs &a, const float lo[3], const float hi[3], cudaStream_t stream);
 
 // CUDA device a scene was built on.
 int scene_device(const lrx_scene *scene);

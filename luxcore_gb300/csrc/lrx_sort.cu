@@ -1,0 +1,116 @@
+// Ray reordering before traversal.  Rays are keyed by direction octant and
+// the Morton code of their origin inside the scene box, radix-sorted (stable),
+// and traced through the resulting index list; hits are written back to each
+// ray's own slot, so the caller sees the same order as without sorting.
+// Rays in one warp then share a direction octant (the same child order in
+// every node) and start close together, which keeps lanes on similar paths.
+//
+// Scratch (keys, indices, sort temp) comes from a library-owned stream-ordered
+// memory pool: allocation and release are ordered on the caller's stream, so
+// concurrent calls on one scene do not share scratch and nothing synchronises
+// the device.
+#include <cstdint>
+#include <mutex>
+
+#include <cub/device/device_radix_sort.cuh>
+
+#include "lrx_common.cuh"
+#include "lrx_internal.h"
+
+namespace lrx {
+
+namespace {
+
+constexpr int kMaxDevices = 64;
+std::mutex g_pool_mu;
+cudaMemPool_t g_pool[kMaxDevices] = {};
+
+lrx_status pool_for(int dev, cudaMemPool_t *out) {
+	std::lock_guard<std::mutex> lk(g_pool_mu);
+	if (!g_pool[dev]) {
+		cudaMemPoolProps props = {};
+		props.allocType = cudaMemAllocationTypePinned;
+		props.location.type = cudaMemLocationTypeDevice;
+		props.location.id = dev;
+		cudaMemPool_t p;
+		LRX_CUDA(cudaMemPoolCreate(&p, &props));
+		uint64_t keep = UINT64_MAX;  // keep freed blocks for the next call
+		LRX_CUDA(cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep));
+		g_pool[dev] = p;
+	}
+	*out = g_pool[dev];
+	return LRX_OK;
+}
+
+__device__ __forceinline__ uint32_t spread10(uint32_t v) {
+	v &= 0x3ffu;
+	v = (v | (v << 16)) & 0x030000ffu;
+	v = (v | (v << 8)) & 0x0300f00fu;
+	v = (v | (v << 4)) & 0x030c30c3u;
+	v = (v | (v << 2)) & 0x09249249u;
+	return v;
+}
+
+// key = octant (3 bits) << 27 | Morton code of the origin (9 bits per axis)
+__global__ void k_ray_keys(const float4 *__restrict__ rays, uint32_t n, float3 lo, float3 inv_ext,
+		uint32_t *__restrict__ keys, uint32_t *__restrict__ idx) {
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	const float4 r0 = __ldcs(rays + 3 * (size_t)i), r1 = __ldcs(rays + 3 * (size_t)i + 1);
+	const uint32_t oct = (__float_as_uint(r0.w) >> 31) | ((__float_as_uint(r1.x) >> 31) << 1) |
+			((__float_as_uint(r1.y) >> 31) << 2);
+	auto q = [](float v, float l, float s) {
+		const float u = (v - l) * s;
+		return u > 0.f ? (u < 511.f ? (uint32_t)u : 511u) : 0u;  // NaN -> 0
+	};
+	const uint32_t m = (spread10(q(r0.x, lo.x, inv_ext.x)) << 2) | (spread10(q(r0.y, lo.y, inv_ext.y)) << 1) |
+			spread10(q(r0.z, lo.z, inv_ext.z));
+	keys[i] = (oct << 27) | (m & 0x07ffffffu);
+	idx[i] = i;
+}
+
+}  // namespace
+
+lrx_status launch_trace_sorted(const TraceArgs &a_in, const float lo[3], const float hi[3], cudaStream_t st) {
+	TraceArgs a = a_in;
+	const uint32_t n = a.count;
+	int dev = 0;
+	LRX_CUDA(cudaGetDevice(&dev));
+	if (dev < 0 || dev >= kMaxDevices) return launch_trace(a, st);
+	cudaMemPool_t pool;
+	lrx_status rc = pool_for(dev, &pool);
+	if (rc != LRX_OK) return rc;
+
+	size_t temp_bytes = 0;
+	{
+		cub::DoubleBuffer<uint32_t> dk(nullptr, nullptr), dv(nullptr, nullptr);
+		LRX_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, temp_bytes, dk, dv, (int)n, 0, 30, st));
+	}
+	const size_t arr = ((sizeof(uint32_t) * (size_t)n + 255) / 256) * 256;
+	const size_t total = 4 * arr + temp_bytes;
+	void *base = nullptr;
+	LRX_CUDA(cudaMallocFromPoolAsync(&base, total, pool, st));
+	unsigned char *p = static_cast<unsigned char *>(base);
+	uint32_t *k0 = reinterpret_cast<uint32_t *>(p), *k1 = reinterpret_cast<uint32_t *>(p + arr);
+	uint32_t *v0 = reinterpret_cast<uint32_t *>(p + 2 * arr), *v1 = reinterpret_cast<uint32_t *>(p + 3 * arr);
+	void *temp = p + 4 * arr;
+
+	float3 l = make_float3(lo[0], lo[1], lo[2]);
+	float3 s = make_float3(hi[0] > lo[0] ? 512.f / (hi[0] - lo[0]) : 0.f, hi[1] > lo[1] ? 512.f / (hi[1] - lo[1]) : 0.f,
+			hi[2] > lo[2] ? 512.f / (hi[2] - lo[2]) : 0.f);
+	k_ray_keys<<<(n + 255) / 256, 256, 0, st>>>(reinterpret_cast<const float4 *>(a.rays), n, l, s, k0, v0);
+	cudaError_t e = cudaGetLastError();
+	if (e == cudaSuccess) {
+		cub::DoubleBuffer<uint32_t> dk(k0, k1), dv(v0, v1);
+		e = cub::DeviceRadixSort::SortPairs(temp, temp_bytes, dk, dv, (int)n, 0, 30, st);
+		if (e == cudaSuccess) {
+			a.order = dv.Current();
+			rc = launch_trace(a, st);
+		}
+	}
+	cudaFreeAsync(base, st);  // ordered after the trace on the same stream
+	if (e != cudaSuccess) return cuda_fail(e, "ray sort");
+	return rc;
+}
+
+}  // namespace lrx

@@ -149,9 +149,10 @@ template <bool ANY, bool TWO_LEVEL, bool COUNT, uint32_t CV>
 __global__ void __launch_bounds__((CV & kVarOccupancy) ? 64 : 1024, (CV & kVarOccupancy) ? 20 : 0)
 k_trace(TraceArgs a) {
 	constexpr bool MM3 = (CV & kVarMinMax3) != 0;
-	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-	bool active = i < a.count;
+	const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+	bool active = tid < a.count;
 	if (!COUNT && !active) return;
+	const uint32_t i = (a.order && active) ? a.order[tid] : tid;  // the ray this thread traces
 	const bool keep = (a.variant & kVarSceneEvictLast) != 0;
 	const bool stream = (a.variant & kVarStreamRays) != 0;
 	const uint64_t pol = keep ? evict_last_policy() : 0ull;
