@@ -350,8 +350,8 @@ def run_lrx(args):
     # for comparison; outside the timed region
     alt = {}
     if args.sweep:
-        for bs, pp, var in [(64, 8, 0), (64, 8, 16), (64, 8, 17), (64, 8, 20), (64, 8, 24), (64, 8, 25), (32, 8, 16),
-                            (128, 8, 16), (64, 0, 16), (64, 16, 16), (64, 8, 1), (64, 8, 4)]:
+        for bs, pp, var in [(64, 8, 0), (64, 8, 16), (64, 8, 48), (64, 8, 52), (32, 8, 48), (128, 8, 48),
+                            (64, 4, 48), (64, 16, 48), (64, 8, 4)]:
             scene.set_trace_config(bs, pp, var)
             key = f"b{bs}-p{pp}-v{var}"
             alt[key] = {}
@@ -422,7 +422,8 @@ def run_lrx(args):
                 "per_set_ms": {k: round(v, 4) for k, v in kern_ms.items()},
                 "per_set_Mrays": {name: round(n / (kern_ms[name] / 1e3) / 1e6, 1) for name, _, _, n, _ in dev},
                 "nodes_tris_per_ray": {k: [round(v[0], 2), round(v[1], 2)] for k, v in counts.items()},
-                "trace_config": scene.trace_config(),
+                "trace_config": {"closest": scene.trace_config(lrx.LRX_TRACE_CLOSEST),
+                                 "any": scene.trace_config(lrx.LRX_TRACE_ANY)},
                 "config_sweep_Mrays": alt,
             },
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",

@@ -164,6 +164,8 @@ typedef struct lrx_trace_config {
 	                             of the warp test triangles; otherwise they are deferred while
 	                             node work remains (0 = never defer) */
 	uint32_t variant;         /* LRX_VARIANT_* bits */
+	uint32_t modes;           /* set: which trace modes take this config (bit 0 closest,
+	                             bit 1 any-hit; 0 = both).  get: bit 1 set reads the any-hit one */
 } lrx_trace_config;
 #define LRX_VARIANT_MINMAX3 0x1u       /* 3-input min/max in the slab tests */
 #define LRX_VARIANT_SCENE_L2_KEEP 0x2u /* node/triangle loads marked evict-last in L2 */
@@ -171,6 +173,8 @@ typedef struct lrx_trace_config {
 #define LRX_VARIANT_OCCUPANCY 0x8u     /* register budget for 20 blocks of 64 threads per SM (blocks <= 64) */
 #define LRX_VARIANT_SORT_RAYS 0x10u    /* reorder batches of >= 32768 rays by direction octant and
                                           origin before tracing (hits stay in caller order) */
+#define LRX_VARIANT_SORT_OCTANT 0x20u  /* with SORT_RAYS: key on the direction octant only
+                                          (one radix pass, caller order kept within an octant) */
 
 /* Sets / reads the launch configuration lrx_trace uses for this scene.
  * No reference counterpart (the reference fixes 32-thread blocks,

@@ -180,9 +180,11 @@ struct lrx_scene {
 	uint32_t tlas_capacity = 0;
 	uint32_t blas_node_total = 0;
 	lrx_build_opts opts{};
-	// default launch: 64-thread blocks, triangles deferred below 8 lanes
-	// (best of a block-size x postpone sweep on the heightfield ray sets)
-	lrx_trace_config tcfg{sizeof(lrx_trace_config), 64, 8, 0};
+	// default launch per mode (closest, any-hit): 64-thread blocks, triangles
+	// deferred below 8 lanes (best of a block-size x postpone sweep on the
+	// heightfield ray sets); any-hit batches are reordered by direction octant
+	lrx_trace_config tcfg[2] = {{sizeof(lrx_trace_config), 64, 8, 0, 1},
+			{sizeof(lrx_trace_config), 64, 8, 0, 2}};
 	lrx_scene_info info{};
 	BuildScratch scratch;
 	std::mutex mu;
@@ -661,9 +663,10 @@ static lrx_status trace_common(lrx_scene *s, const void *d_rays, void *d_hits, u
 		const uint64_t lim = (uint64_t)(s->info.instance_count + 1) * (s->info.node_count + 1) + 64;
 		a.visit_limit = (uint32_t)std::min<uint64_t>(lim, kMaxVisits);
 	}
-	a.block_size = s->tcfg.block_size;
-	a.postpone = s->tcfg.postpone;
-	a.variant = s->tcfg.variant;
+	const lrx_trace_config &cfg = s->tcfg[mode == LRX_TRACE_ANY ? 1 : 0];
+	a.block_size = cfg.block_size;
+	a.postpone = cfg.postpone;
+	a.variant = cfg.variant;
 	if ((a.variant & kVarSortRays) && count >= kSortMinRays && s->root != kNull)
 		return launch_trace_sorted(a, s->bounds_lo, s->bounds_hi, st);
 	return launch_trace(a, st);
@@ -675,13 +678,18 @@ lrx_status lrx_scene_set_trace_config(lrx_scene *s, const lrx_trace_config *c) {
 		return LRX_ERR_INVALID_ARGUMENT;
 	}
 	const uint32_t bs = c->block_size ? c->block_size : kTraceBlock;
-	if (bs < 32 || bs > 512 || (bs & 31) || c->postpone > 32 || c->variant > 0x1fu) {
+	if (bs < 32 || bs > 512 || (bs & 31) || c->postpone > 32 || c->variant > 0x3fu || c->modes > 3u) {
 		set_error("lrx_scene_set_trace_config: value out of range");
 		return LRX_ERR_INVALID_ARGUMENT;
 	}
-	s->tcfg = *c;
-	s->tcfg.struct_size = sizeof(lrx_trace_config);
-	s->tcfg.block_size = bs;
+	const uint32_t modes = c->modes ? c->modes : 3u;
+	for (int m = 0; m < 2; ++m) {
+		if (!(modes & (1u << m))) continue;
+		s->tcfg[m] = *c;
+		s->tcfg[m].struct_size = sizeof(lrx_trace_config);
+		s->tcfg[m].block_size = bs;
+		s->tcfg[m].modes = 1u << m;
+	}
 	return LRX_OK;
 }
 
@@ -690,7 +698,7 @@ lrx_status lrx_scene_get_trace_config(const lrx_scene *s, lrx_trace_config *c) {
 		set_error("lrx_scene_get_trace_config: null argument");
 		return LRX_ERR_INVALID_ARGUMENT;
 	}
-	*c = s->tcfg;
+	*c = s->tcfg[(c->modes & 2u) ? 1 : 0];
 	return LRX_OK;
 }
 

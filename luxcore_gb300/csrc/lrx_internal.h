@@ -115,6 +115,7 @@ struct TraceArgs {
 };
 constexpr uint32_t kTraceBlock = 128;
 constexpr uint32_t kVarSortRays = 0x10u;   // reorder rays by octant + origin before tracing
+constexpr uint32_t kVarSortOctantOnly = 0x20u;  // ... by direction octant only (one radix pass)
 constexpr uint32_t kSortMinRays = 32768;   // smaller batches are traced in caller order
 
 lrx_status launch_trace(const TraceArgs &a, cudaStream_t stream);

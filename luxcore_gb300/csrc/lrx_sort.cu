@@ -81,10 +81,12 @@ lrx_status launch_trace_sorted(const TraceArgs &a_in, const float lo[3], const f
 	lrx_status rc = pool_for(dev, &pool);
 	if (rc != LRX_OK) return rc;
 
+	// octant-only keys sort in one pass and keep caller order inside an octant
+	const int begin_bit = (a.variant & kVarSortOctantOnly) ? 27 : 0;
 	size_t temp_bytes = 0;
 	{
 		cub::DoubleBuffer<uint32_t> dk(nullptr, nullptr), dv(nullptr, nullptr);
-		LRX_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, temp_bytes, dk, dv, (int)n, 0, 30, st));
+		LRX_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, temp_bytes, dk, dv, (int)n, begin_bit, 30, st));
 	}
 	const size_t arr = ((sizeof(uint32_t) * (size_t)n + 255) / 256) * 256;
 	const size_t total = 4 * arr + temp_bytes;
@@ -102,7 +104,7 @@ lrx_status launch_trace_sorted(const TraceArgs &a_in, const float lo[3], const f
 	cudaError_t e = cudaGetLastError();
 	if (e == cudaSuccess) {
 		cub::DoubleBuffer<uint32_t> dk(k0, k1), dv(v0, v1);
-		e = cub::DeviceRadixSort::SortPairs(temp, temp_bytes, dk, dv, (int)n, 0, 30, st);
+		e = cub::DeviceRadixSort::SortPairs(temp, temp_bytes, dk, dv, (int)n, begin_bit, 30, st);
 		if (e == cudaSuccess) {
 			a.order = dv.Current();
 			rc = launch_trace(a, st);

@@ -58,7 +58,7 @@ class BuildOpts(ctypes.Structure):
 
 class TraceConfig(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_uint32), ("block_size", ctypes.c_uint32),
-                ("postpone", ctypes.c_uint32), ("variant", ctypes.c_uint32)]
+                ("postpone", ctypes.c_uint32), ("variant", ctypes.c_uint32), ("modes", ctypes.c_uint32)]
 
 
 class SceneInfo(ctypes.Structure):
@@ -175,12 +175,14 @@ class Scene:
         check(load().lrx_scene_get_info(self.handle, ctypes.byref(inf)))
         return inf.as_dict()
 
-    def set_trace_config(self, block_size: int = 64, postpone: int = 8, variant: int = 0):
-        c = TraceConfig(ctypes.sizeof(TraceConfig), block_size, postpone, variant)
+    def set_trace_config(self, block_size: int = 64, postpone: int = 8, variant: int = 0, modes: int = 0):
+        """modes: 1 = closest-hit launches, 2 = any-hit launches, 0 = both."""
+        c = TraceConfig(ctypes.sizeof(TraceConfig), block_size, postpone, variant, modes)
         check(load().lrx_scene_set_trace_config(self.handle, ctypes.byref(c)))
 
-    def trace_config(self) -> dict:
+    def trace_config(self, mode: int = LRX_TRACE_CLOSEST) -> dict:
         c = TraceConfig()
+        c.modes = 2 if mode == LRX_TRACE_ANY else 1
         check(load().lrx_scene_get_trace_config(self.handle, ctypes.byref(c)))
         return {"block_size": c.block_size, "postpone": c.postpone, "variant": c.variant}
 

@@ -23,9 +23,9 @@ pytestmark = pytest.mark.gpu
 SENT = 0xDEADBEEF
 # launch configurations every parity test runs under: (block size, postpone, variant bits)
 KERNELS = pytest.mark.parametrize("kernel", [(128, 0, 0), (64, 8, 0), (256, 24, 0), (64, 8, 0xF), (128, 8, 0x7),
-                                             (64, 8, 0x10), (32, 8, 0x1F)],
+                                             (64, 8, 0x10), (32, 8, 0x1F), (64, 8, 0x30)],
                                   ids=["b128", "b64-p8", "b256-p24", "b64-p8-allvariants", "b128-p8-mm3-hints",
-                                       "b64-p8-sorted", "b32-p8-sorted-all"])
+                                       "b64-p8-sorted", "b32-p8-sorted-all", "b64-p8-octsort"])
 
 
 def make_scene(desc, kernel=(64, 8, 0), **kw):
