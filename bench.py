@@ -263,7 +263,10 @@ def run_lrx(args):
     with torch.cuda.stream(stream):
         scene = lrx.Scene(scene_desc, stream=st)
     build_s = time.perf_counter() - t0
-    scene.set_trace_config(args.block_size, args.postpone, args.variant)
+    if args.block_size is not None or args.postpone is not None or args.variant is not None:
+        scene.set_trace_config(args.block_size or 64, 8 if args.postpone is None else args.postpone,
+                               args.variant or 0)
+    saved_cfg = {m: scene.trace_config(m) for m in (lrx.LRX_TRACE_CLOSEST, lrx.LRX_TRACE_ANY)}
     info = scene.info()
 
     primary = W.pinhole_rays(1024, 1024)
@@ -364,7 +367,8 @@ def run_lrx(args):
                 e1.record(stream)
                 e1.synchronize()
                 alt[key][name] = round(n * 5 / (e0.elapsed_time(e1) / 1e3) / 1e6, 1)
-        scene.set_trace_config(args.block_size, args.postpone, args.variant)
+        for m, c in saved_cfg.items():
+            scene.set_trace_config(c["block_size"], c["postpone"], c["variant"], modes=2 if m == lrx.LRX_TRACE_ANY else 1)
 
     # roofline of the traversal kernel: algorithmic bytes / kernel time
     peak, peak_kind = load_peaks()
@@ -453,9 +457,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (lrx_trace_host) leg")
     ap.add_argument("--sweep", action="store_true", help="also time other launch configurations")
-    ap.add_argument("--block-size", type=int, default=64)
-    ap.add_argument("--postpone", type=int, default=8)
-    ap.add_argument("--variant", type=int, default=0, help="LRX_VARIANT_* bits")
+    ap.add_argument("--block-size", type=int, default=None, help="override the per-mode defaults")
+    ap.add_argument("--postpone", type=int, default=None)
+    ap.add_argument("--variant", type=int, default=None, help="LRX_VARIANT_* bits")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3 (timing rule)")
