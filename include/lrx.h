@@ -182,6 +182,25 @@ typedef struct lrx_trace_config {
 lrx_status lrx_scene_set_trace_config(lrx_scene *scene, const lrx_trace_config *config);
 lrx_status lrx_scene_get_trace_config(const lrx_scene *scene, lrx_trace_config *config);
 
+/* One ray batch of a multi-batch call (device buffers, as for lrx_trace). */
+typedef struct lrx_batch {
+	lrx_scene *scene;
+	const void *d_rays;
+	void *d_hits;
+	uint32_t count;
+	uint32_t mode;     /* LRX_TRACE_CLOSEST or LRX_TRACE_ANY */
+} lrx_batch;
+
+/* Traces many ray batches -- any mix of scenes (on one device) and modes --
+ * with one launch of a persistent queue kernel per 384 batches: 64-thread
+ * blocks claim 64-ray tiles from a device work queue until every batch is
+ * done, so small and uneven batches share the GPU instead of each paying a
+ * launch and a tail.  Results equal lrx_trace on each batch.  Asynchronous
+ * on `stream`; graph-capturable (no allocation, no host synchronisation).
+ * Replaces: a sequence of HardwareIntersectionKernel::EnqueueTraceRayBuffer
+ * calls (hardwareintersectiondevice.h:67-68), one per RayBuffer. */
+lrx_status lrx_trace_batches(const lrx_batch *batches, uint32_t batch_count, void *stream);
+
 /* Largest batch lrx_trace_host_noalloc accepts (its fixed staging area). */
 #define LRX_NOALLOC_MAX_RAYS 131072u
 

@@ -5,6 +5,7 @@
 // Compiled with -ffp-contract=off so the host-side FP32 arithmetic below
 // (Matrix4x4::Inverse, instance boxes) rounds exactly as the reference's.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -627,6 +628,13 @@ lrx_status lrx_scene_get_info(const lrx_scene *s, lrx_scene_info *info) {
 	return LRX_OK;
 }
 
+// A correct walk visits each node at most once per BLAS entry, so a ray never
+// needs more than (instances + 1) x nodes visits.
+static uint32_t scene_visit_limit(const lrx_scene *s) {
+	const uint64_t lim = (uint64_t)(s->info.instance_count + 1) * (s->info.node_count + 1) + 64;
+	return (uint32_t)std::min<uint64_t>(lim, kMaxVisits);
+}
+
 static lrx_status trace_common(lrx_scene *s, const void *d_rays, void *d_hits, uint32_t count, uint32_t mode,
 		uint64_t *d_counters, cudaStream_t st) {
 	if (!s) {
@@ -659,12 +667,7 @@ static lrx_status trace_common(lrx_scene *s, const void *d_rays, void *d_hits, u
 	a.any_hit = mode == LRX_TRACE_ANY;
 	a.status = s->status.as<uint32_t>();
 	a.counters = reinterpret_cast<unsigned long long *>(d_counters);
-	// A correct walk visits each node at most once per BLAS entry, so a ray
-	// never needs more than (instances + 1) x nodes visits.
-	{
-		const uint64_t lim = (uint64_t)(s->info.instance_count + 1) * (s->info.node_count + 1) + 64;
-		a.visit_limit = (uint32_t)std::min<uint64_t>(lim, kMaxVisits);
-	}
+	a.visit_limit = scene_visit_limit(s);
 	const lrx_trace_config &cfg = s->tcfg[mode == LRX_TRACE_ANY ? 1 : 0];
 	a.block_size = cfg.block_size;
 	a.postpone = cfg.postpone;
@@ -706,6 +709,76 @@ lrx_status lrx_scene_get_trace_config(const lrx_scene *s, lrx_trace_config *c) {
 
 lrx_status lrx_trace(lrx_scene *s, const void *d_rays, void *d_hits, uint32_t count, uint32_t mode, void *stream) {
 	return trace_common(s, d_rays, d_hits, count, mode, nullptr, (cudaStream_t)stream);
+}
+
+lrx_status lrx_trace_batches(const lrx_batch *batches, uint32_t n_batches, void *stream) {
+	if (n_batches && !batches) {
+		set_error("lrx_trace_batches: null batch array");
+		return LRX_ERR_INVALID_ARGUMENT;
+	}
+	int dev = 0;
+	for (uint32_t k = 0; k < n_batches; ++k) {
+		const lrx_batch &b = batches[k];
+		if (!b.scene || b.mode > LRX_TRACE_ANY) {
+			set_error("lrx_trace_batches: batch " + std::to_string(k) + ": null scene or unknown mode");
+			return LRX_ERR_INVALID_ARGUMENT;
+		}
+		if (b.count && (!b.d_rays || !b.d_hits || ((uintptr_t)b.d_rays & 15u) || ((uintptr_t)b.d_hits & 3u))) {
+			set_error("lrx_trace_batches: batch " + std::to_string(k) + ": null or misaligned ray/hit buffer");
+			return LRX_ERR_INVALID_ARGUMENT;
+		}
+		if (k == 0) dev = b.scene->device;
+		if (b.scene->device != dev) {
+			set_error("lrx_trace_batches: all scenes of one call must live on one device");
+			return LRX_ERR_INVALID_ARGUMENT;
+		}
+	}
+	if (n_batches == 0) return LRX_OK;
+	DeviceGuard g(dev);
+	static std::atomic<uint32_t> next_slot{0};
+	thread_local std::unique_ptr<QueueParams> params;
+	if (!params) params.reset(new QueueParams());
+	QueueParams &p = *params;
+	cudaStream_t st = (cudaStream_t)stream;
+	p.n = 0;
+	p.total_tiles = 0;
+	auto flush = [&]() -> lrx_status {
+		if (p.n == 0) return LRX_OK;
+		p.slot = next_slot.fetch_add(1u) % kQueueSlots;
+		lrx_status rc = launch_trace_queue(p, st);
+		p.n = 0;
+		p.total_tiles = 0;
+		return rc;
+	};
+	for (uint32_t k = 0; k < n_batches; ++k) {
+		const lrx_batch &b = batches[k];
+		if (b.count == 0) continue;
+		lrx_scene *s = b.scene;
+		const uint32_t tiles = (b.count + kTileRays - 1) / kTileRays;
+		if (p.n == kMaxQueueBatches || (uint64_t)p.total_tiles + tiles > 0xffffffffull) {
+			lrx_status rc = flush();
+			if (rc != LRX_OK) return rc;
+		}
+		const lrx_trace_config &cfg = s->tcfg[b.mode == LRX_TRACE_ANY ? 1 : 0];
+		QueueBatch &q = p.b[p.n++];
+		q.nodes = s->nodes.as<WideNode>();
+		q.tris = s->tris.as<TriRecord>();
+		q.insts = s->insts.as<InstRecord>();
+		q.rays = b.d_rays;
+		q.hits = b.d_hits;
+		q.status = s->status.as<uint32_t>();
+		q.root = s->root;
+		q.count = b.count;
+		q.tile_begin = p.total_tiles;
+		// runtime-selectable variants only (cache hints); the queue kernel does not sort
+		const uint32_t var = cfg.variant & (LRX_VARIANT_SCENE_L2_KEEP | LRX_VARIANT_STREAM_RAYS);
+		q.flags = (b.mode == LRX_TRACE_ANY ? 1u : 0u) | (s->two_level ? 2u : 0u) | ((cfg.postpone & 0xffu) << 8) |
+				(var << 16);
+		q.visit_limit = scene_visit_limit(s);
+		q.pad = 0;
+		p.total_tiles += tiles;
+	}
+	return flush();
 }
 
 lrx_status lrx_trace_counted(lrx_scene *s, const void *d_rays, void *d_hits, uint32_t count, uint32_t mode,

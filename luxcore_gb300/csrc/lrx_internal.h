@@ -120,6 +120,31 @@ constexpr uint32_t kSortMinRays = 32768;   // smaller batches are traced in call
 
 lrx_status launch_trace(const TraceArgs &a, cudaStream_t stream);
 
+// One batch of a multi-batch queue launch (kernel parameter space).
+struct QueueBatch {
+	const WideNode *nodes;
+	const TriRecord *tris;
+	const InstRecord *insts;
+	const void *rays;
+	void *hits;
+	uint32_t *status;
+	uint32_t root, count;
+	uint32_t tile_begin;   // first 64-ray tile of this batch in the launch
+	uint32_t flags;        // bit 0 any-hit, bit 1 two-level, bits 8-15 postpone, bits 16-23 variant
+	uint32_t visit_limit, pad;
+};
+constexpr uint32_t kTileRays = 64;
+constexpr uint32_t kMaxQueueBatches = 384;  // keeps the parameter block under 32 KB
+constexpr uint32_t kQueueSlots = 4096;      // concurrent queue launches per device
+struct QueueParams {
+	uint32_t n, total_tiles, slot, pad;
+	QueueBatch b[kMaxQueueBatches];
+};
+static_assert(sizeof(QueueParams) <= 32000, "kernel parameter limit");
+
+// One launch of the persistent queue kernel over p.n batches.
+lrx_status launch_trace_queue(const QueueParams &p, cudaStream_t stream);
+
 // Sorts the rays (octant, origin Morton code in [lo, hi]) and traces them in
 // that order; scratch from a stream-ordered pool.  Hits land in caller order.
 lrx_status launch_trace_sorted(const TraceArgs &a, const float lo[3], const float hi[3], cudaStream_t stream);

@@ -21,6 +21,8 @@
 // unless fewer than `postpone` lanes of the warp are testing triangles at
 // that moment (__activemask, no waiting) while node work remains -- then the
 // group is pushed and tested later, which keeps lanes in step.
+#include <algorithm>
+
 #include "lrx_common.cuh"
 #include "lrx_internal.h"
 
@@ -145,14 +147,17 @@ __device__ __forceinline__ bool finite3(float3 v) {
 	return isfinite(v.x) && isfinite(v.y) && isfinite(v.z);
 }
 
+struct Counts {
+	uint32_t nodes, tris, insts, rays;
+};
+
+// Traces ray `tid` of the batch `a` (through a.order when set) and writes its
+// hit.  Shared by the one-batch kernel and the multi-batch queue kernel.
 template <bool ANY, bool TWO_LEVEL, bool COUNT, uint32_t CV>
-__global__ void __launch_bounds__((CV & kVarOccupancy) ? 64 : 1024, (CV & kVarOccupancy) ? 20 : 0)
-k_trace(TraceArgs a) {
+__device__ __forceinline__ void trace_ray(const TraceArgs &a, uint32_t tid, bool active, Counts &cnt) {
 	constexpr bool MM3 = (CV & kVarMinMax3) != 0;
-	const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-	bool active = tid < a.count;
-	if (!COUNT && !active) return;
-	const uint32_t i = (a.order && active) ? a.order[tid] : tid;  // the ray this thread traces
+	if (!active) return;
+	const uint32_t i = a.order ? a.order[tid] : tid;  // the ray this thread traces
 	const bool keep = (a.variant & kVarSceneEvictLast) != 0;
 	const bool stream = (a.variant & kVarStreamRays) != 0;
 	const uint64_t pol = keep ? evict_last_policy() : 0ull;
@@ -168,9 +173,8 @@ k_trace(TraceArgs a) {
 			r1 = __ldg(rp + 1);
 			r2 = __ldg(rp + 2);
 		}
-		if (__float_as_uint(r2.y) & LRX_RAY_FLAGS_MASKED) active = false;  // bvh.cl:243-244
+		if (__float_as_uint(r2.y) & LRX_RAY_FLAGS_MASKED) return;  // bvh.cl:243-244
 	}
-	if (!COUNT && !active) return;
 
 	const float3 wo = make_float3(r0.x, r0.y, r0.z);
 	const float3 wd = make_float3(r0.w, r1.x, r1.y);
@@ -302,8 +306,23 @@ k_trace(TraceArgs a) {
 		}
 	}
 	if (COUNT) {
+		cnt.nodes += n_nodes;
+		cnt.tris += n_tris;
+		cnt.insts += n_insts;
+		cnt.rays += 1;
+	}
+}
+
+template <bool ANY, bool TWO_LEVEL, bool COUNT, uint32_t CV>
+__global__ void __launch_bounds__((CV & kVarOccupancy) ? 64 : 1024, (CV & kVarOccupancy) ? 20 : 0)
+k_trace(TraceArgs a) {
+	const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+	if (!COUNT && tid >= a.count) return;
+	Counts cnt{0, 0, 0, 0};
+	trace_ray<ANY, TWO_LEVEL, COUNT, CV>(a, tid, tid < a.count, cnt);
+	if (COUNT) {
 		// every lane of the block reaches this point in the counting variant
-		unsigned long long v[4] = {n_nodes, n_tris, n_insts, active ? 1ull : 0ull};
+		unsigned long long v[4] = {cnt.nodes, cnt.tris, cnt.insts, cnt.rays};
 #pragma unroll
 		for (int k = 0; k < 4; ++k) {
 			unsigned long long x = v[k];
@@ -316,6 +335,85 @@ k_trace(TraceArgs a) {
 			for (int k = 0; k < 4; ++k) atomicAdd(&a.counters[k], v[k]);
 		}
 	}
+}
+
+// ---------------------------------------------------------------------------
+// Multi-batch queue kernel: one launch drains many ray batches (any mix of
+// scenes and modes).  Persistent 64-thread blocks claim 64-ray tiles from a
+// device work queue -- a counter in a slot of g_queue -- and trace them; the
+// last block to leave resets the slot for its next use.  Every loop trip and
+// barrier is block-uniform (the tile index is broadcast through shared
+// memory), and the loop ends when the tiles run out.
+// ---------------------------------------------------------------------------
+
+__device__ uint32_t g_queue[kQueueSlots][2];  // (next tile, blocks finished) per slot
+
+template <uint32_t CV>
+__global__ void __launch_bounds__(kTileRays) k_trace_queue(const __grid_constant__ QueueParams p) {
+	__shared__ uint32_t s_tile;
+	uint32_t *slot = g_queue[p.slot];
+	Counts cnt{0, 0, 0, 0};
+	for (;;) {
+		if (threadIdx.x == 0) s_tile = atomicAdd(&slot[0], 1u);
+		__syncthreads();
+		const uint32_t tile = s_tile;
+		__syncthreads();
+		if (tile >= p.total_tiles) break;
+		uint32_t lo = 0, hi = p.n;  // last batch whose first tile is <= tile
+		while (hi - lo > 1) {
+			const uint32_t mid = (lo + hi) >> 1;
+			if (p.b[mid].tile_begin <= tile) lo = mid;
+			else hi = mid;
+		}
+		const QueueBatch &qb = p.b[lo];
+		TraceArgs a{};
+		a.nodes = qb.nodes;
+		a.tris = qb.tris;
+		a.insts = qb.insts;
+		a.root = qb.root;
+		a.two_level = (qb.flags >> 1) & 1u;
+		a.rays = qb.rays;
+		a.hits = qb.hits;
+		a.count = qb.count;
+		a.any_hit = qb.flags & 1u;
+		a.status = qb.status;
+		a.postpone = (qb.flags >> 8) & 0xffu;
+		a.variant = (qb.flags >> 16) & 0xffu;
+		a.visit_limit = qb.visit_limit;
+		const uint32_t tid = (tile - qb.tile_begin) * kTileRays + threadIdx.x;
+		const bool active = tid < a.count;
+		if (a.any_hit) {
+			if (a.two_level) trace_ray<true, true, false, CV>(a, tid, active, cnt);
+			else trace_ray<true, false, false, CV>(a, tid, active, cnt);
+		} else {
+			if (a.two_level) trace_ray<false, true, false, CV>(a, tid, active, cnt);
+			else trace_ray<false, false, false, CV>(a, tid, active, cnt);
+		}
+	}
+	if (threadIdx.x == 0) {
+		__threadfence();
+		if (atomicAdd(&slot[1], 1u) == gridDim.x - 1) {  // every block has stopped claiming tiles
+			slot[0] = 0u;
+			slot[1] = 0u;
+			__threadfence();
+		}
+	}
+}
+
+lrx_status launch_trace_queue(const QueueParams &p, cudaStream_t st) {
+	if (p.total_tiles == 0) return LRX_OK;
+	static int resident = 0;  // 64-thread blocks resident per GB300 at this kernel's occupancy
+	if (resident == 0) {
+		int dev = 0, sms = 0, per_sm = 0;
+		LRX_CUDA(cudaGetDevice(&dev));
+		LRX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+		LRX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_queue<0u>, kTileRays, 0));
+		resident = std::max(1, sms * std::max(1, per_sm));
+	}
+	const uint32_t grid = std::min<uint32_t>(p.total_tiles, (uint32_t)resident);
+	k_trace_queue<0u><<<grid, kTileRays, 0, st>>>(p);
+	LRX_CUDA(cudaGetLastError());
+	return LRX_OK;
 }
 
 lrx_status launch_trace(const TraceArgs &a, cudaStream_t st) {

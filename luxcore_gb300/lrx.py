@@ -31,7 +31,7 @@ STATUS_NAMES = {0: "LRX_OK", 1: "LRX_ERR_INVALID_ARGUMENT", 2: "LRX_ERR_CUDA", 3
 EXPORTED = ["lrx_abi_version", "lrx_last_error", "lrx_scene_create", "lrx_scene_destroy",
             "lrx_scene_update_instances", "lrx_scene_get_info", "lrx_trace", "lrx_trace_host",
             "lrx_trace_counted", "lrx_scene_device_status", "lrx_trace_host_noalloc",
-            "lrx_scene_set_trace_config", "lrx_scene_get_trace_config"]
+            "lrx_scene_set_trace_config", "lrx_scene_get_trace_config", "lrx_trace_batches"]
 LRX_NOALLOC_MAX_RAYS = 131072
 
 
@@ -108,6 +108,8 @@ def load(path: str | None = None):
         L.lrx_scene_set_trace_config.argtypes = [vp, ctypes.POINTER(TraceConfig)]
         L.lrx_scene_get_trace_config.restype = st
         L.lrx_scene_get_trace_config.argtypes = [vp, ctypes.POINTER(TraceConfig)]
+        L.lrx_trace_batches.restype = st
+        L.lrx_trace_batches.argtypes = [vp, u32, vp]
         L.lrx_trace_host_noalloc.restype = st
         L.lrx_trace_host_noalloc.argtypes = [vp, vp, vp, u32, u32, vp]
         L.lrx_trace_counted.restype = st
@@ -121,6 +123,31 @@ def load(path: str | None = None):
 def check(status: int):
     if status != 0:
         raise LrxError(status, load().lrx_last_error().decode(errors="replace"))
+
+
+class Batch(ctypes.Structure):
+    _fields_ = [("scene", ctypes.c_void_p), ("d_rays", ctypes.c_void_p), ("d_hits", ctypes.c_void_p),
+                ("count", ctypes.c_uint32), ("mode", ctypes.c_uint32)]
+
+
+def batch_array(batches):
+    """ctypes array of lrx_batch from (Scene, d_rays, d_hits, count, mode) tuples."""
+    arr = (Batch * max(1, len(batches)))()
+    for k, (s, r, h, n, m) in enumerate(batches):
+        arr[k].scene = s.handle.value if isinstance(s.handle, ctypes.c_void_p) else s.handle
+        arr[k].d_rays = r
+        arr[k].d_hits = h
+        arr[k].count = n
+        arr[k].mode = m
+    return arr
+
+
+def trace_batches(batches, stream: int = 0, arr=None):
+    """lrx_trace_batches over (Scene, d_rays, d_hits, count, mode) tuples (or a
+    prebuilt batch_array)."""
+    if arr is None:
+        arr = batch_array(batches)
+    check(load().lrx_trace_batches(arr, len(batches), ctypes.c_void_p(stream)))
 
 
 def _object_array(scene: W.SceneDesc):

@@ -291,3 +291,37 @@ def test_rejects_bad_arguments(torch_cuda):
     sing = W.SceneDesc([W.random_triangles(10, 1)], [(0, np.zeros((4, 4), np.float32))])
     with pytest.raises(lrx.LrxError):
         lrx.Scene(sing)                                        # singular instance transform
+
+
+def test_trace_batches_equals_per_batch_traces(torch_cuda):
+    """lrx_trace_batches over a ragged mix of scenes, modes and sizes
+    (including empty, single-ray and tile-boundary batches, and more batches
+    than one queue launch holds) returns exactly what lrx_trace returns."""
+    torch = torch_cuda
+    flat_desc, _ = W.config1(n_tris=20000, n_rays=1, seed=301)
+    inst_desc, _, _ = W.config3(n_rays=1, n_meshes=2, freq=8, n_inst=50, extent=1.0, scale=(0.05, 0.2))
+    scenes = [lrx.Scene(flat_desc), lrx.Scene(inst_desc)]
+    rng = np.random.default_rng(302)
+    sizes = [0, 1, 63, 64, 65, 1000, 100_000] + rng.integers(1, 3000, 400).tolist()
+    st = torch.cuda.current_stream().cuda_stream
+    items, refs = [], []
+    for k, n in enumerate(sizes):
+        s = scenes[k % 2]
+        mode = lrx.LRX_TRACE_ANY if k % 3 == 0 else lrx.LRX_TRACE_CLOSEST
+        rays = W.random_rays(max(n, 1), 400 + k)[:n]
+        rays["flags"][::17] = W.RAY_FLAGS_MASKED
+        d_r = torch.from_numpy(rays.view(np.uint8).reshape(-1).copy()).cuda() if n else \
+            torch.empty(48, dtype=torch.uint8, device="cuda")
+        d_h = torch.empty(max(n, 1) * 20, dtype=torch.uint8, device="cuda")
+        d_h.view(torch.int32).fill_(np.int32(np.uint32(SENT).view(np.int32)).item())
+        items.append((s, d_r, d_h, n, mode))
+        refs.append(gpu_trace(torch, s, rays, mode) if n else None)
+    lrx.trace_batches([(s, r.data_ptr(), h.data_ptr(), n, m) for s, r, h, n, m in items], st)
+    torch.cuda.synchronize()
+    for s in scenes:
+        assert s.device_status(st) == 0
+    for (s, r, h, n, m), ref in zip(items, refs):
+        if n == 0:
+            continue
+        got = h.cpu().numpy().view(W.HIT_DTYPE)[:n]
+        assert np.array_equal(got.view(np.uint8), ref.view(np.uint8))
