@@ -446,12 +446,124 @@ def run_lrx(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# Uneven batches over several resident scenes: plain vs queue kernel
+# ---------------------------------------------------------------------------
+
+def device_random_rays(torch, n, extent, seed, device):
+    """Rays on the device: origins ~ U[0,extent]^3, directions uniform on the
+    sphere, mint 1e-4, maxt 1e30 (48-byte luxrays::Ray records)."""
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    rec = torch.zeros((n, 12), dtype=torch.float32, device=device)
+    rec[:, 0:3] = torch.rand((n, 3), generator=g, device=device) * extent
+    d = torch.randn((n, 3), generator=g, device=device)
+    rec[:, 3:6] = d / d.norm(dim=1, keepdim=True).clamp_min(1e-20)
+    rec[:, 6] = 1e-4
+    rec[:, 7] = 1e30
+    return rec
+
+
+def run_batching(args):
+    import torch
+
+    from luxcore_gb300 import lrx
+
+    dev = "cuda:0"
+    torch.cuda.set_device(0)
+    tri_counts, extents, batches = W.uneven_batches(n_batches=args.batches)
+    log(f"[batching] scenes {tri_counts.tolist()}")
+    scenes = []
+    for k, (n, ext) in enumerate(zip(tri_counts.tolist(), extents.tolist())):
+        scenes.append(lrx.Scene(W.SceneDesc([W.random_triangles(int(n), W.BASE_SEED + 40 + k, extent=ext)])))
+    stream = torch.cuda.Stream()
+    st = stream.cuda_stream
+    items = []
+    for k, (si, n, anyhit) in enumerate(batches):
+        rec = device_random_rays(torch, int(n), float(extents[si]), W.BASE_SEED + 1000 + k, dev)
+        hits = torch.empty(int(n) * HIT_BYTES, dtype=torch.uint8, device=dev)
+        items.append((scenes[si], rec, hits, int(n), lrx.LRX_TRACE_ANY if anyhit else lrx.LRX_TRACE_CLOSEST))
+    total_rays = sum(x[3] for x in items)
+    torch.cuda.synchronize()
+    log(f"[batching] {len(items)} batches, {total_rays} rays resident")
+
+    # per-scene autotune on a 262,144-ray sample of each mode
+    tuned = {}
+    if not args.no_autotune:
+        for k, s in enumerate(scenes):
+            sample = device_random_rays(torch, 1 << 18, float(extents[k]), W.BASE_SEED + 7 + k, dev)
+            tuned[k] = {m: s.autotune(sample.data_ptr(), 1 << 18, m, st)
+                        for m in (lrx.LRX_TRACE_CLOSEST, lrx.LRX_TRACE_ANY)}
+        torch.cuda.synchronize()
+
+    def plain():
+        for s, rec, hits, n, mode in items:
+            s.trace(rec.data_ptr(), hits.data_ptr(), n, mode, st)
+
+    arr = lrx.batch_array([(s, rec.data_ptr(), hits.data_ptr(), n, mode) for s, rec, hits, n, mode in items])
+
+    def batched():
+        lrx.trace_batches(items, st, arr=arr)
+
+    def timed(fn, reps):
+        with torch.cuda.stream(stream):
+            fn()
+        stream.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps, (time.perf_counter() - t0) * 1e3 / reps
+
+    def graphed(fn):
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=stream):
+            fn_st = torch.cuda.current_stream().cuda_stream
+            assert fn_st == st
+            fn()
+        return lambda: g.replay()
+
+    res = {}
+    res["plain"] = timed(plain, args.steps)
+    plain_hits = [h.clone() for _, _, h, _, _ in items[:8]]
+    res["batched"] = timed(batched, args.steps)
+    same = all(torch.equal(a, b[2]) for a, b in zip(plain_hits, items[:8]))
+    res["plain_graph"] = timed(graphed(plain), args.steps)
+    res["batched_graph"] = timed(graphed(batched), args.steps)
+    for s in scenes:
+        if s.device_status(st) != 0:
+            raise RuntimeError("device status word set")
+    mrays = {k: round(total_rays / (v[0] / 1e3) / 1e6, 1) for k, v in res.items()}
+    line = {
+        "metric": "Mrays/s on uneven batches (batched queue kernel + CUDA graph vs one launch per RayBuffer)",
+        "value": mrays["batched_graph"], "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": 1,
+        "ms_per_step": round(res["batched_graph"][0], 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": f"{len(items)} batches log-uniform [1024, 2097152] rays over 8 scenes "
+                               f"({int(min(tri_counts))}-{int(max(tri_counts))} triangles), 70/30 closest/any",
+                   "rays_per_step": total_rays, "Mrays_by_form": mrays,
+                   "device_ms_by_form": {k: round(v[0], 3) for k, v in res.items()},
+                   "host_ms_by_form": {k: round(v[1], 3) for k, v in res.items()},
+                   "batched_over_plain": round(mrays["batched_graph"] / mrays["plain"], 3),
+                   "results_equal_plain": bool(same), "autotuned": tuned},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="lrx", choices=["lrx", "reference"])
+    ap.add_argument("--workload", default="heightfield", choices=["heightfield", "batching"],
+                    help="heightfield = the headline line; batching = uneven batches, plain vs queue kernel")
+    ap.add_argument("--batches", type=int, default=512)
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--ref-fraction", type=int, default=4,
                     help="CPU legs trace every Nth ray of each set")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -464,6 +576,8 @@ def main():
     if args.warmup < 3:
         log("warmup raised to 3 (timing rule)")
         args.warmup = 3
+    if args.workload == "batching" and args.impl == "lrx":
+        return run_batching(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_lrx(args)

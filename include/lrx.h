@@ -182,6 +182,15 @@ typedef struct lrx_trace_config {
 lrx_status lrx_scene_set_trace_config(lrx_scene *scene, const lrx_trace_config *config);
 lrx_status lrx_scene_get_trace_config(const lrx_scene *scene, lrx_trace_config *config);
 
+/* Autotuner: traces the sample batch (device rays) under each candidate
+ * launch configuration -- block size {32, 64, 128} x postpone {0, 8, 16} x
+ * variant {none, streaming ray access, ray sort} -- keeps the fastest for
+ * `mode` in the scene and returns it in `chosen` (nullable).  Synchronises
+ * `stream`; do not trace the same scene from other threads meanwhile.
+ * No reference counterpart (the reference fixes its launch shape). */
+lrx_status lrx_scene_autotune(lrx_scene *scene, const void *d_sample_rays, uint32_t count, uint32_t mode,
+		void *stream, lrx_trace_config *chosen);
+
 /* One ray batch of a multi-batch call (device buffers, as for lrx_trace). */
 typedef struct lrx_batch {
 	lrx_scene *scene;

@@ -707,6 +707,57 @@ lrx_status lrx_scene_get_trace_config(const lrx_scene *s, lrx_trace_config *c) {
 	return LRX_OK;
 }
 
+lrx_status lrx_scene_autotune(lrx_scene *s, const void *d_rays, uint32_t count, uint32_t mode, void *stream,
+		lrx_trace_config *chosen) {
+	if (!s || !d_rays || count == 0 || mode > LRX_TRACE_ANY) {
+		set_error("lrx_scene_autotune: null scene/rays, empty sample or unknown mode");
+		return LRX_ERR_INVALID_ARGUMENT;
+	}
+	DeviceGuard g(s->device);
+	cudaStream_t st = (cudaStream_t)stream;
+	cudaMemPool_t pool;
+	lrx_status rc = stream_pool(s->device, &pool);
+	if (rc != LRX_OK) return rc;
+	void *hits = nullptr;
+	LRX_CUDA(cudaMallocFromPoolAsync(&hits, sizeof(lrx_hit) * (size_t)count, pool, st));
+	cudaEvent_t e0 = nullptr, e1 = nullptr;
+	cudaEventCreate(&e0);
+	cudaEventCreate(&e1);
+	const int m = mode == LRX_TRACE_ANY ? 1 : 0;
+	lrx_trace_config best = s->tcfg[m];
+	float best_ms = INFINITY;
+	static const uint32_t kBlocks[] = {32, 64, 128};
+	static const uint32_t kPostpone[] = {0, 8, 16};
+	static const uint32_t kVariants[] = {0, LRX_VARIANT_STREAM_RAYS, LRX_VARIANT_SORT_RAYS};
+	for (uint32_t bs : kBlocks) {
+		for (uint32_t pp : kPostpone) {
+			for (uint32_t var : kVariants) {
+				if ((var & LRX_VARIANT_SORT_RAYS) && count < kSortMinRays) continue;
+				s->tcfg[m] = lrx_trace_config{sizeof(lrx_trace_config), bs, pp, var, 1u << m};
+				if ((rc = trace_common(s, d_rays, hits, count, mode, nullptr, st)) != LRX_OK) break;
+				cudaEventRecord(e0, st);
+				for (int r = 0; r < 3 && rc == LRX_OK; ++r) rc = trace_common(s, d_rays, hits, count, mode, nullptr, st);
+				cudaEventRecord(e1, st);
+				if (rc != LRX_OK || cudaEventSynchronize(e1) != cudaSuccess) break;
+				float ms = 0.f;
+				cudaEventElapsedTime(&ms, e0, e1);
+				if (ms < best_ms) {
+					best_ms = ms;
+					best = s->tcfg[m];
+				}
+			}
+		}
+	}
+	s->tcfg[m] = best;
+	cudaFreeAsync(hits, st);
+	cudaStreamSynchronize(st);
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	if (rc != LRX_OK) return rc;
+	if (chosen) *chosen = best;
+	return LRX_OK;
+}
+
 lrx_status lrx_trace(lrx_scene *s, const void *d_rays, void *d_hits, uint32_t count, uint32_t mode, void *stream) {
 	return trace_common(s, d_rays, d_hits, count, mode, nullptr, (cudaStream_t)stream);
 }

@@ -142,6 +142,10 @@ struct QueueParams {
 };
 static_assert(sizeof(QueueParams) <= 32000, "kernel parameter limit");
 
+// Library-owned stream-ordered memory pool of a device (freed blocks are
+// kept for reuse); for per-call scratch that must not synchronise the device.
+lrx_status stream_pool(int dev, cudaMemPool_t *out);
+
 // One launch of the persistent queue kernel over p.n batches.
 lrx_status launch_trace_queue(const QueueParams &p, cudaStream_t stream);
 

@@ -25,7 +25,13 @@ constexpr int kMaxDevices = 64;
 std::mutex g_pool_mu;
 cudaMemPool_t g_pool[kMaxDevices] = {};
 
-lrx_status pool_for(int dev, cudaMemPool_t *out) {
+}  // namespace
+
+lrx_status stream_pool(int dev, cudaMemPool_t *out) {
+	if (dev < 0 || dev >= kMaxDevices) {
+		set_error("device index out of range");
+		return LRX_ERR_NOT_SUPPORTED;
+	}
 	std::lock_guard<std::mutex> lk(g_pool_mu);
 	if (!g_pool[dev]) {
 		cudaMemPoolProps props = {};
@@ -41,6 +47,8 @@ lrx_status pool_for(int dev, cudaMemPool_t *out) {
 	*out = g_pool[dev];
 	return LRX_OK;
 }
+
+namespace {
 
 __device__ __forceinline__ uint32_t spread10(uint32_t v) {
 	v &= 0x3ffu;
@@ -78,7 +86,7 @@ lrx_status launch_trace_sorted(const TraceArgs &a_in, const float lo[3], const f
 	LRX_CUDA(cudaGetDevice(&dev));
 	if (dev < 0 || dev >= kMaxDevices) return launch_trace(a, st);
 	cudaMemPool_t pool;
-	lrx_status rc = pool_for(dev, &pool);
+	lrx_status rc = stream_pool(dev, &pool);
 	if (rc != LRX_OK) return rc;
 
 	// octant-only keys sort in one pass and keep caller order inside an octant

@@ -31,7 +31,8 @@ STATUS_NAMES = {0: "LRX_OK", 1: "LRX_ERR_INVALID_ARGUMENT", 2: "LRX_ERR_CUDA", 3
 EXPORTED = ["lrx_abi_version", "lrx_last_error", "lrx_scene_create", "lrx_scene_destroy",
             "lrx_scene_update_instances", "lrx_scene_get_info", "lrx_trace", "lrx_trace_host",
             "lrx_trace_counted", "lrx_scene_device_status", "lrx_trace_host_noalloc",
-            "lrx_scene_set_trace_config", "lrx_scene_get_trace_config", "lrx_trace_batches"]
+            "lrx_scene_set_trace_config", "lrx_scene_get_trace_config", "lrx_trace_batches",
+            "lrx_scene_autotune"]
 LRX_NOALLOC_MAX_RAYS = 131072
 
 
@@ -108,6 +109,8 @@ def load(path: str | None = None):
         L.lrx_scene_set_trace_config.argtypes = [vp, ctypes.POINTER(TraceConfig)]
         L.lrx_scene_get_trace_config.restype = st
         L.lrx_scene_get_trace_config.argtypes = [vp, ctypes.POINTER(TraceConfig)]
+        L.lrx_scene_autotune.restype = st
+        L.lrx_scene_autotune.argtypes = [vp, vp, u32, u32, vp, ctypes.POINTER(TraceConfig)]
         L.lrx_trace_batches.restype = st
         L.lrx_trace_batches.argtypes = [vp, u32, vp]
         L.lrx_trace_host_noalloc.restype = st
@@ -211,6 +214,14 @@ class Scene:
         c = TraceConfig()
         c.modes = 2 if mode == LRX_TRACE_ANY else 1
         check(load().lrx_scene_get_trace_config(self.handle, ctypes.byref(c)))
+        return {"block_size": c.block_size, "postpone": c.postpone, "variant": c.variant}
+
+    def autotune(self, d_rays: int, count: int, mode: int = LRX_TRACE_CLOSEST, stream: int = 0) -> dict:
+        """Picks this scene's fastest launch configuration for `mode` on a
+        device-resident sample of rays."""
+        c = TraceConfig()
+        check(load().lrx_scene_autotune(self.handle, ctypes.c_void_p(d_rays), count, mode,
+                                        ctypes.c_void_p(stream), ctypes.byref(c)))
         return {"block_size": c.block_size, "postpone": c.postpone, "variant": c.variant}
 
     def update_instances(self, scene: W.SceneDesc, stream: int = 0):
