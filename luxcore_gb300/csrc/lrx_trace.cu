@@ -245,7 +245,9 @@ __device__ __forceinline__ void trace_ray(const TraceArgs &a, uint32_t tid, bool
 			} else {
 				bool done = false;
 				while (tg.y) {
-					if (ng.y > 0x00ffffffu && __popc(__activemask()) < a.postpone) {
+					// Any-hit never defers: the hit it returns must depend only on the
+					// ray and the tree, not on which rays share its warp.
+					if (!ANY && ng.y > 0x00ffffffu && __popc(__activemask()) < a.postpone) {
 						LRX_PUSH(tg);  // test later, when the warp does triangles together
 						tg.y = 0;
 						break;
