@@ -511,10 +511,11 @@ def run_batching(args):
         stream.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         t0 = time.perf_counter()
-        e0.record(stream)
-        for _ in range(reps):
-            fn()
-        e1.record(stream)
+        with torch.cuda.stream(stream):  # graph replays launch on the current stream
+            e0.record(stream)
+            for _ in range(reps):
+                fn()
+            e1.record(stream)
         e1.synchronize()
         return e0.elapsed_time(e1) / reps, (time.perf_counter() - t0) * 1e3 / reps
 
@@ -532,7 +533,11 @@ def run_batching(args):
     res["batched"] = timed(batched, args.steps)
     same = all(torch.equal(a, b[2]) for a, b in zip(plain_hits, items[:8]))
     res["plain_graph"] = timed(graphed(plain), args.steps)
+    for _, _, h, _, _ in items[:8]:
+        h.zero_()
+    torch.cuda.synchronize()
     res["batched_graph"] = timed(graphed(batched), args.steps)
+    same = same and all(torch.equal(a, b[2]) for a, b in zip(plain_hits, items[:8]))
     for s in scenes:
         if s.device_status(st) != 0:
             raise RuntimeError("device status word set")
