@@ -210,6 +210,56 @@ typedef struct lrx_batch {
  * calls (hardwareintersectiondevice.h:67-68), one per RayBuffer. */
 lrx_status lrx_trace_batches(const lrx_batch *batches, uint32_t batch_count, void *stream);
 
+/* ------------------------------------------------------------------------
+ * Serving: many render sessions submit ray batches against registered scenes;
+ * one server per device keeps scenes resident under an HBM budget (least
+ * recently used scenes with no work in flight are evicted and rebuilt on
+ * demand) and runs a continuous-batching loop: whenever one of its streams
+ * is free, every admitted pending request is launched together through the
+ * queue kernel, so requests arriving while others run overlap them on the
+ * device.  No reference counterpart (the reference traces one RayBuffer per
+ * call on stream 0, pathoclopenclthread.cpp:185).
+ * ------------------------------------------------------------------------ */
+typedef struct lrx_server lrx_server;
+
+#define LRX_SERVE_BATCHED 0u  /* continuous batching over `streams` streams (default) */
+#define LRX_SERVE_PLAIN 1u    /* one lrx_trace per request, FIFO on one stream (comparison) */
+
+typedef struct lrx_server_opts {
+	uint32_t struct_size;      /* sizeof(lrx_server_opts) */
+	uint32_t policy;           /* LRX_SERVE_* */
+	uint64_t budget_bytes;     /* device memory for resident scenes (0 = unlimited) */
+	uint32_t streams;          /* concurrent launches in flight (0 = 4) */
+	uint32_t max_requests_per_launch;  /* (0 = 384) */
+} lrx_server_opts;
+
+typedef struct lrx_server_stats {
+	uint64_t requests_done, rays_done;
+	uint64_t requests_failed;
+	uint64_t scene_builds, scene_evictions;
+	uint64_t resident_bytes, peak_resident_bytes;
+	uint64_t launches;
+	double latency_p50_us, latency_p99_us, latency_mean_us, latency_max_us;
+	double busy_seconds;       /* wall time from the first submit to the last completion */
+} lrx_server_stats;
+
+lrx_status lrx_server_create(const lrx_server_opts *opts, lrx_server **out_server);
+/* Waits for in-flight work, frees every resident scene and stops the worker. */
+lrx_status lrx_server_destroy(lrx_server *server);
+/* Registers a scene (arguments as lrx_scene_create); the server keeps a host
+ * copy so it can rebuild the scene after an eviction.  Not built until used. */
+lrx_status lrx_server_add_scene(lrx_server *server, const lrx_mesh_desc *meshes, uint32_t mesh_count,
+		const lrx_object_desc *objects, uint32_t object_count, uint32_t *out_scene_id);
+/* Queues a ray batch (device buffers that stay valid until the request
+ * completes); returns at once with a ticket. */
+lrx_status lrx_server_submit(lrx_server *server, uint32_t scene_id, const void *d_rays, void *d_hits,
+		uint32_t count, uint32_t mode, uint64_t *out_ticket);
+/* Waits up to timeout_ms for a ticket: LRX_OK when its hits are written,
+ * LRX_ERR_TIMEOUT if still running, or the error that failed it. */
+lrx_status lrx_server_wait(lrx_server *server, uint64_t ticket, uint32_t timeout_ms);
+lrx_status lrx_server_get_stats(lrx_server *server, lrx_server_stats *stats);
+lrx_status lrx_server_reset_stats(lrx_server *server);
+
 /* Largest batch lrx_trace_host_noalloc accepts (its fixed staging area). */
 #define LRX_NOALLOC_MAX_RAYS 131072u
 

@@ -32,7 +32,10 @@ EXPORTED = ["lrx_abi_version", "lrx_last_error", "lrx_scene_create", "lrx_scene_
             "lrx_scene_update_instances", "lrx_scene_get_info", "lrx_trace", "lrx_trace_host",
             "lrx_trace_counted", "lrx_scene_device_status", "lrx_trace_host_noalloc",
             "lrx_scene_set_trace_config", "lrx_scene_get_trace_config", "lrx_trace_batches",
-            "lrx_scene_autotune"]
+            "lrx_scene_autotune", "lrx_server_create", "lrx_server_destroy", "lrx_server_add_scene",
+            "lrx_server_submit", "lrx_server_wait", "lrx_server_get_stats", "lrx_server_reset_stats"]
+LRX_SERVE_BATCHED = 0
+LRX_SERVE_PLAIN = 1
 LRX_NOALLOC_MAX_RAYS = 131072
 
 
@@ -109,6 +112,20 @@ def load(path: str | None = None):
         L.lrx_scene_set_trace_config.argtypes = [vp, ctypes.POINTER(TraceConfig)]
         L.lrx_scene_get_trace_config.restype = st
         L.lrx_scene_get_trace_config.argtypes = [vp, ctypes.POINTER(TraceConfig)]
+        L.lrx_server_create.restype = st
+        L.lrx_server_create.argtypes = [ctypes.POINTER(ServerOpts), ctypes.POINTER(vp)]
+        L.lrx_server_destroy.restype = st
+        L.lrx_server_destroy.argtypes = [vp]
+        L.lrx_server_add_scene.restype = st
+        L.lrx_server_add_scene.argtypes = [vp, vp, u32, vp, u32, ctypes.POINTER(u32)]
+        L.lrx_server_submit.restype = st
+        L.lrx_server_submit.argtypes = [vp, u32, vp, vp, u32, u32, ctypes.POINTER(u64)]
+        L.lrx_server_wait.restype = st
+        L.lrx_server_wait.argtypes = [vp, u64, u32]
+        L.lrx_server_get_stats.restype = st
+        L.lrx_server_get_stats.argtypes = [vp, ctypes.POINTER(ServerStats)]
+        L.lrx_server_reset_stats.restype = st
+        L.lrx_server_reset_stats.argtypes = [vp]
         L.lrx_scene_autotune.restype = st
         L.lrx_scene_autotune.argtypes = [vp, vp, u32, u32, vp, ctypes.POINTER(TraceConfig)]
         L.lrx_trace_batches.restype = st
@@ -151,6 +168,91 @@ def trace_batches(batches, stream: int = 0, arr=None):
     if arr is None:
         arr = batch_array(batches)
     check(load().lrx_trace_batches(arr, len(batches), ctypes.c_void_p(stream)))
+
+
+class ServerOpts(ctypes.Structure):
+    _fields_ = [("struct_size", ctypes.c_uint32), ("policy", ctypes.c_uint32), ("budget_bytes", ctypes.c_uint64),
+                ("streams", ctypes.c_uint32), ("max_requests_per_launch", ctypes.c_uint32)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("requests_done", ctypes.c_uint64), ("rays_done", ctypes.c_uint64),
+                ("requests_failed", ctypes.c_uint64), ("scene_builds", ctypes.c_uint64),
+                ("scene_evictions", ctypes.c_uint64), ("resident_bytes", ctypes.c_uint64),
+                ("peak_resident_bytes", ctypes.c_uint64), ("launches", ctypes.c_uint64),
+                ("latency_p50_us", ctypes.c_double), ("latency_p99_us", ctypes.c_double),
+                ("latency_mean_us", ctypes.c_double), ("latency_max_us", ctypes.c_double),
+                ("busy_seconds", ctypes.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def _mesh_array(scene: W.SceneDesc):
+    keep = []
+    meshes = (MeshDesc * max(1, len(scene.meshes)))()
+    for i, m in enumerate(scene.meshes):
+        v = np.ascontiguousarray(m.vertices, np.float32)
+        t = np.ascontiguousarray(m.triangles, np.uint32)
+        keep += [v, t]
+        meshes[i].vertices = v.ctypes.data
+        meshes[i].triangles = t.ctypes.data
+        meshes[i].vertex_count = v.shape[0]
+        meshes[i].triangle_count = t.shape[0]
+    return meshes, keep
+
+
+class Server:
+    """lrx_server: scenes kept resident under an HBM budget and ray-batch
+    requests served by continuous batching (policy LRX_SERVE_BATCHED) or one
+    launch per request (LRX_SERVE_PLAIN)."""
+
+    def __init__(self, policy: int = LRX_SERVE_BATCHED, budget_bytes: int = 0, streams: int = 0,
+                 max_requests_per_launch: int = 0):
+        o = ServerOpts(ctypes.sizeof(ServerOpts), policy, budget_bytes, streams, max_requests_per_launch)
+        h = ctypes.c_void_p()
+        check(load().lrx_server_create(ctypes.byref(o), ctypes.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if getattr(self, "handle", None):
+            load().lrx_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add_scene(self, scene: W.SceneDesc) -> int:
+        meshes, keep = _mesh_array(scene)
+        objs = _object_array(scene)
+        has_inst = scene.has_instances
+        sid = ctypes.c_uint32()
+        check(load().lrx_server_add_scene(self.handle, meshes, len(scene.meshes), objs if has_inst else None,
+                                          len(scene.objects) if has_inst else 0, ctypes.byref(sid)))
+        del keep  # the server copied the geometry
+        return sid.value
+
+    def submit(self, scene_id: int, d_rays: int, d_hits: int, count: int, mode: int = LRX_TRACE_CLOSEST) -> int:
+        t = ctypes.c_uint64()
+        check(load().lrx_server_submit(self.handle, scene_id, ctypes.c_void_p(d_rays), ctypes.c_void_p(d_hits),
+                                       count, mode, ctypes.byref(t)))
+        return t.value
+
+    def wait(self, ticket: int, timeout_ms: int = 60000) -> int:
+        """LRX_OK (0) when done; raises LrxError on failure or timeout."""
+        check(load().lrx_server_wait(self.handle, ticket, timeout_ms))
+        return 0
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        check(load().lrx_server_get_stats(self.handle, ctypes.byref(s)))
+        return s.as_dict()
+
+    def reset_stats(self):
+        check(load().lrx_server_reset_stats(self.handle))
 
 
 def _object_array(scene: W.SceneDesc):
