@@ -559,13 +559,164 @@ def run_batching(args):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# Serving: 64 sessions over 12 scenes, Poisson arrivals, LRU under a budget
+# ---------------------------------------------------------------------------
+
+SERVE_SIZE_RANGE = (4096, 4_194_304)
+
+
+def serving_scenes(max_tris):
+    """12 scenes with log-uniform triangle counts in [100k, max_tris]; every
+    third is instanced (displaced icospheres under random transforms)."""
+    rng = W.Rng(W.BASE_SEED + 5, 21)
+    counts = W.log_uniform_int(rng, 12, 100_000, max_tris).tolist()
+    descs, extents = [], []
+    for k, n in enumerate(counts):
+        if k % 3 == 2:
+            n_inst = max(1, n // 14_580)  # 8 unique icospheres of 20 * 27^2 = 14,580 triangles
+            ext = max(1.0, (n_inst / 64.0) ** (1.0 / 3.0))
+            descs.append(W.instanced_scene(n_meshes=8, freq=27, n_inst=n_inst, seed=W.BASE_SEED + 60 + k,
+                                           scale=(0.1, 0.4), extent=ext))
+        else:
+            ext = (n / 65536.0) ** (1.0 / 3.0)
+            descs.append(W.SceneDesc([W.random_triangles_fast(n, W.BASE_SEED + 60 + k, extent=ext)]))
+        extents.append(ext)
+    return counts, descs, extents
+
+
+def run_serving(args):
+    import torch
+
+    from luxcore_gb300 import lrx
+
+    dev = "cuda:0"
+    torch.cuda.set_device(0)
+    t0 = time.perf_counter()
+    counts, descs, extents = serving_scenes(args.serve_max_tris)
+    log(f"[serving] scenes {counts} generated in {time.perf_counter() - t0:.1f}s")
+    pool_n = SERVE_SIZE_RANGE[1]
+    pools = []
+    for k, ext in enumerate(extents):
+        closest = device_random_rays(torch, pool_n, ext, W.BASE_SEED + 2000 + k, dev)
+        anyr = device_random_rays(torch, pool_n, ext, W.BASE_SEED + 3000 + k, dev)
+        anyr[:, 7] = torch.rand(pool_n, device=dev) * (0.5 * ext) + 0.05 * ext  # shadow-ray lengths
+        pools.append((closest, anyr))
+    n_sess, k_buf = args.sessions, 4
+    hits = [[torch.empty(pool_n * HIT_BYTES, dtype=torch.uint8, device=dev) for _ in range(k_buf)]
+            for _ in range(n_sess)]
+    torch.cuda.synchronize()
+
+    def schedule(rate, duration, seed):
+        g = np.random.default_rng(seed)
+        n = int(rate * duration * 1.5) + 16
+        t = np.cumsum(g.exponential(1.0 / rate, n))
+        t = t[t < duration]
+        lo, hi = SERVE_SIZE_RANGE
+        sizes = np.floor(np.exp(g.uniform(np.log(lo), np.log(hi), t.size))).astype(np.int64)
+        sess = g.integers(0, n_sess, t.size)
+        return list(zip(t.tolist(), sess.tolist(), sizes.tolist()))
+
+    def one_run(policy, budget, rate):
+        server = lrx.Server(policy=policy, budget_bytes=budget, streams=args.serve_streams)
+        ids = [server.add_scene(d) for d in descs]
+        if not budget or budget >= (150 << 30):
+            for k in range(len(descs)):  # make every scene resident before the clock starts
+                c, _ = pools[k]
+                server.wait(server.submit(ids[k], c.data_ptr(), hits[0][0].data_ptr(), 1024, lrx.LRX_TRACE_CLOSEST))
+        server.reset_stats()
+        sched = schedule(rate, args.serve_seconds, W.BASE_SEED + 77)
+        step = [0] * n_sess
+        inflight = [[None] * k_buf for _ in range(n_sess)]
+        deferred = 0
+        start = time.perf_counter()
+        for t_arr, s, n in sched:
+            while time.perf_counter() - start < t_arr:
+                pass
+            free = [b for b in range(k_buf) if inflight[s][b] is None]
+            if not free:  # the session still has k_buf batches in flight: wait for its oldest
+                deferred += 1
+                b = 0
+                server.wait(inflight[s][0])
+                inflight[s][0] = None
+                free = [0]
+            b = free[0]
+            sid = s % len(descs)
+            mode = lrx.LRX_TRACE_CLOSEST if step[s] % 2 == 0 else lrx.LRX_TRACE_ANY  # bounce, then shadow
+            step[s] += 1
+            rays = pools[sid][0 if mode == lrx.LRX_TRACE_CLOSEST else 1]
+            inflight[s][b] = server.submit(ids[sid], rays.data_ptr(), hits[s][b].data_ptr(), int(n), mode)
+            # collect what has finished so buffers come back
+            for ss in (s,):
+                for bb in range(k_buf):
+                    tk = inflight[ss][bb]
+                    if tk is not None and bb != b:
+                        try:
+                            server.wait(tk, 0)
+                            inflight[ss][bb] = None
+                        except lrx.LrxError as e:
+                            if e.status != 9:  # not a timeout
+                                raise
+        for s in range(n_sess):
+            for b in range(k_buf):
+                if inflight[s][b] is not None:
+                    server.wait(inflight[s][b])
+        wall = time.perf_counter() - start
+        st = server.stats()
+        server.close()
+        return {"offered_batches_per_s": rate, "batches": len(sched), "deferred_by_session": deferred,
+                "p50_us": round(st["latency_p50_us"], 1), "p99_us": round(st["latency_p99_us"], 1),
+                "mean_us": round(st["latency_mean_us"], 1), "max_us": round(st["latency_max_us"], 1),
+                "Mrays_per_s": round(st["rays_done"] / max(wall, 1e-9) / 1e6, 1),
+                "wall_s": round(wall, 3), "launches": st["launches"], "failed": st["requests_failed"],
+                "builds": st["scene_builds"], "evictions": st["scene_evictions"],
+                "peak_resident_GB": round(st["peak_resident_bytes"] / 2 ** 30, 3)}
+
+    full = 150 << 30
+    res = {}
+    for rate in args.serve_rates:
+        res[f"batched@{rate}"] = one_run(lrx.LRX_SERVE_BATCHED, full, rate)
+        res[f"plain@{rate}"] = one_run(lrx.LRX_SERVE_PLAIN, full, rate)
+    # scaled budget: ~40 % of the scene bytes, so scenes are evicted and rebuilt
+    probe_total = 0
+    for d in descs:
+        s = lrx.Scene(d)
+        probe_total += s.info()["device_bytes"]
+        s.close()
+    small = int(probe_total * 0.4)
+    low_rate = min(args.serve_rates)
+    res[f"batched@{low_rate}-budget40pct"] = one_run(lrx.LRX_SERVE_BATCHED, small, low_rate)
+    head = res[f"batched@{args.serve_rates[0]}"]
+    plain = res[f"plain@{args.serve_rates[0]}"]
+    line = {
+        "metric": "served p50/p99 batch latency and Mrays/s (continuous batching vs plain launch)",
+        "value": head["Mrays_per_s"], "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 1,
+        "ms_per_step": round(head["wall_s"] * 1e3, 1), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": f"{n_sess} sessions over 12 scenes ({min(counts)}-{max(counts)} triangles, 4 "
+                               f"instanced), Poisson arrivals, sizes log-uniform {list(SERVE_SIZE_RANGE)}, "
+                               f"bounce (closest) / shadow (any) alternating per session",
+                   "scene_bytes_total_GB": round(probe_total / 2 ** 30, 3), "budgets_GB": [150, round(small / 2 ** 30, 3)],
+                   "runs": res,
+                   "p99_over_p50": round(head["p99_us"] / max(head["p50_us"], 1e-9), 2),
+                   "batched_over_plain_Mrays": round(head["Mrays_per_s"] / max(plain["Mrays_per_s"], 1e-9), 3)},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="lrx", choices=["lrx", "reference"])
-    ap.add_argument("--workload", default="heightfield", choices=["heightfield", "batching"],
+    ap.add_argument("--sessions", type=int, default=64)
+    ap.add_argument("--serve-max-tris", type=int, default=20_000_000)
+    ap.add_argument("--serve-seconds", type=float, default=2.0)
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[2000.0, 800.0])
+    ap.add_argument("--serve-streams", type=int, default=4)
+    ap.add_argument("--workload", default="heightfield", choices=["heightfield", "batching", "serving"],
                     help="heightfield = the headline line; batching = uneven batches, plain vs queue kernel")
     ap.add_argument("--batches", type=int, default=512)
     ap.add_argument("--no-autotune", action="store_true")
@@ -581,6 +732,8 @@ def main():
     if args.warmup < 3:
         log("warmup raised to 3 (timing rule)")
         args.warmup = 3
+    if args.workload == "serving" and args.impl == "lrx":
+        return run_serving(args)
     if args.workload == "batching" and args.impl == "lrx":
         return run_batching(args)
     if args.impl == "reference":

@@ -39,6 +39,7 @@ struct SceneEntry {
 	std::vector<lrx_object_desc> objects;
 	bool has_objects = false;
 	uint64_t est_bytes = 0;                     // estimate until built, then exact
+	bool exact = false;                         // est_bytes is a measured size
 	lrx_scene *scene = nullptr;                 // resident when not null
 	uint64_t bytes = 0;
 	uint64_t last_used = 0;
@@ -152,8 +153,12 @@ lrx_status lrx_server::make_resident(std::unique_lock<std::mutex> &lk, uint32_t 
 		const std::vector<uint32_t> &pinned) {
 	SceneEntry *e = scenes[id].get();
 	if (e->scene) return LRX_OK;
-	if (opts.budget_bytes && e->est_bytes > opts.budget_bytes) return LRX_ERR_BUDGET;
-	if (!make_room(e->est_bytes, pinned)) return LRX_ERR_BUSY;
+	const uint64_t budget = opts.budget_bytes;
+	// before the first build the size is only an estimate: make room for at
+	// most the whole budget and try; afterwards the exact size decides
+	if (budget && e->exact && e->est_bytes > budget) return LRX_ERR_BUDGET;
+	const uint64_t need = budget ? std::min(e->est_bytes, budget) : e->est_bytes;
+	if (!make_room(need, pinned)) return LRX_ERR_BUSY;
 	lk.unlock();
 	lrx_scene *sc = nullptr;
 	lrx_status rc = lrx_scene_create(e->meshes.data(), (uint32_t)e->meshes.size(),
@@ -162,9 +167,14 @@ lrx_status lrx_server::make_resident(std::unique_lock<std::mutex> &lk, uint32_t 
 	if (rc == LRX_OK) lrx_scene_get_info(sc, &info);
 	lk.lock();
 	if (rc != LRX_OK) return rc;
+	e->est_bytes = info.device_bytes;
+	e->exact = true;
+	if (budget && info.device_bytes > budget) {  // larger than the whole budget
+		lrx_scene_destroy(sc);
+		return LRX_ERR_BUDGET;
+	}
 	e->scene = sc;
 	e->bytes = info.device_bytes;
-	e->est_bytes = info.device_bytes;
 	resident += e->bytes;
 	peak_resident = std::max(peak_resident, resident);
 	++builds;
@@ -398,11 +408,11 @@ lrx_status lrx_server_add_scene(lrx_server *s, const lrx_mesh_desc *meshes, uint
 		} else {
 			for (uint32_t i = 0; i < mesh_count; ++i) tris += meshes[i].triangle_count;
 		}
-		// first estimate: ~20 B of wide nodes + 48 B of triangle record per
+		// first estimate: ~13 B of wide nodes + 48 B of triangle record per
 		// unique triangle, 160 B per object; replaced by the exact size once built
 		uint64_t unique = 0;
 		for (uint32_t i = 0; i < mesh_count; ++i) unique += meshes[i].triangle_count;
-		e->est_bytes = 72ull * unique + 160ull * (objects ? object_count : mesh_count) + 4096;
+		e->est_bytes = 64ull * unique + 160ull * (objects ? object_count : mesh_count) + 4096;
 		(void)tris;
 		std::lock_guard<std::mutex> lk(s->mu);
 		*out_id = (uint32_t)s->scenes.size();
