@@ -566,6 +566,18 @@ def run_batching(args):
 SERVE_SIZE_RANGE = (4096, 4_194_304)
 
 
+def collect(server, ticket, timeout_ms=600_000):
+    """Waits for a ticket; True once it is finished (a failed request counts
+    as finished -- the server's statistics record it), False on timeout."""
+    from luxcore_gb300 import lrx
+    try:
+        server.wait(ticket, timeout_ms)
+    except lrx.LrxError as e:
+        if e.status == 9:  # LRX_ERR_TIMEOUT: still running
+            return False
+    return True
+
+
 def serving_scenes(max_tris):
     """12 scenes with log-uniform triangle counts in [100k, max_tris]; every
     third is instanced (displaced icospheres under random transforms)."""
@@ -637,7 +649,7 @@ def run_serving(args):
             if not free:  # the session still has k_buf batches in flight: wait for its oldest
                 deferred += 1
                 b = 0
-                server.wait(inflight[s][0])
+                collect(server, inflight[s][0])
                 inflight[s][0] = None
                 free = [0]
             b = free[0]
@@ -650,17 +662,12 @@ def run_serving(args):
             for ss in (s,):
                 for bb in range(k_buf):
                     tk = inflight[ss][bb]
-                    if tk is not None and bb != b:
-                        try:
-                            server.wait(tk, 0)
-                            inflight[ss][bb] = None
-                        except lrx.LrxError as e:
-                            if e.status != 9:  # not a timeout
-                                raise
+                    if tk is not None and bb != b and collect(server, tk, 0):
+                        inflight[ss][bb] = None
         for s in range(n_sess):
             for b in range(k_buf):
                 if inflight[s][b] is not None:
-                    server.wait(inflight[s][b])
+                    collect(server, inflight[s][b])
         wall = time.perf_counter() - start
         st = server.stats()
         server.close()
@@ -678,12 +685,13 @@ def run_serving(args):
         res[f"batched@{rate}"] = one_run(lrx.LRX_SERVE_BATCHED, full, rate)
         res[f"plain@{rate}"] = one_run(lrx.LRX_SERVE_PLAIN, full, rate)
     # scaled budget: ~40 % of the scene bytes, so scenes are evicted and rebuilt
-    probe_total = 0
+    probe_total, probe_max = 0, 0
     for d in descs:
         s = lrx.Scene(d)
         probe_total += s.info()["device_bytes"]
+        probe_max = max(probe_max, s.info()["device_bytes"])
         s.close()
-    small = int(probe_total * 0.4)
+    small = int(max(probe_total * 0.4, probe_max * 1.25))  # the largest scene must still fit
     low_rate = min(args.serve_rates)
     res[f"batched@{low_rate}-budget40pct"] = one_run(lrx.LRX_SERVE_BATCHED, small, low_rate)
     head = res[f"batched@{args.serve_rates[0]}"]
