@@ -210,6 +210,16 @@ typedef struct lrx_batch {
  * calls (hardwareintersectiondevice.h:67-68), one per RayBuffer. */
 lrx_status lrx_trace_batches(const lrx_batch *batches, uint32_t batch_count, void *stream);
 
+/* lrx_trace_batches with a completion notice per batch: d_done_flags[k] is
+ * set to 1 (after the batch's hits are written and fenced system-wide) as
+ * soon as batch k is finished, while other batches of the launch may still
+ * run -- the flags may live in host-mapped memory and be polled by the host.
+ * The caller zeroes the flags; d_tile_counters (batch_count words of device
+ * memory) is scratch that the call zeroes on `stream`.  Flags of empty batches
+ * are not written.  No reference counterpart. */
+lrx_status lrx_trace_batches_ex(const lrx_batch *batches, uint32_t batch_count, void *stream,
+		uint32_t *d_tile_counters, uint32_t *d_done_flags);
+
 /* ------------------------------------------------------------------------
  * Serving: many render sessions submit ray batches against registered scenes;
  * one server per device keeps scenes resident under an HBM budget (least

@@ -763,8 +763,17 @@ lrx_status lrx_trace(lrx_scene *s, const void *d_rays, void *d_hits, uint32_t co
 }
 
 lrx_status lrx_trace_batches(const lrx_batch *batches, uint32_t n_batches, void *stream) {
+	return lrx_trace_batches_ex(batches, n_batches, stream, nullptr, nullptr);
+}
+
+lrx_status lrx_trace_batches_ex(const lrx_batch *batches, uint32_t n_batches, void *stream,
+		uint32_t *d_tile_counters, uint32_t *d_done_flags) {
 	if (n_batches && !batches) {
 		set_error("lrx_trace_batches: null batch array");
+		return LRX_ERR_INVALID_ARGUMENT;
+	}
+	if ((d_tile_counters == nullptr) != (d_done_flags == nullptr)) {
+		set_error("lrx_trace_batches_ex: give both the tile counters and the done flags, or neither");
 		return LRX_ERR_INVALID_ARGUMENT;
 	}
 	int dev = 0;
@@ -793,6 +802,9 @@ lrx_status lrx_trace_batches(const lrx_batch *batches, uint32_t n_batches, void 
 	cudaStream_t st = (cudaStream_t)stream;
 	p.n = 0;
 	p.total_tiles = 0;
+	p.tiles_done = d_tile_counters;
+	p.done_flags = d_done_flags;
+	if (d_tile_counters) LRX_CUDA(cudaMemsetAsync(d_tile_counters, 0, sizeof(uint32_t) * n_batches, st));
 	auto flush = [&]() -> lrx_status {
 		if (p.n == 0) return LRX_OK;
 		p.slot = next_slot.fetch_add(1u) % kQueueSlots;
@@ -826,7 +838,7 @@ lrx_status lrx_trace_batches(const lrx_batch *batches, uint32_t n_batches, void 
 		q.flags = (b.mode == LRX_TRACE_ANY ? 1u : 0u) | (s->two_level ? 2u : 0u) | ((cfg.postpone & 0xffu) << 8) |
 				(var << 16);
 		q.visit_limit = scene_visit_limit(s);
-		q.pad = 0;
+		q.user_index = k;
 		p.total_tiles += tiles;
 	}
 	return flush();

@@ -131,13 +131,16 @@ struct QueueBatch {
 	uint32_t root, count;
 	uint32_t tile_begin;   // first 64-ray tile of this batch in the launch
 	uint32_t flags;        // bit 0 any-hit, bit 1 two-level, bits 8-15 postpone, bits 16-23 variant
-	uint32_t visit_limit, pad;
+	uint32_t visit_limit;
+	uint32_t user_index;   // the caller's index of this batch (completion flags)
 };
 constexpr uint32_t kTileRays = 64;
 constexpr uint32_t kMaxQueueBatches = 384;  // keeps the parameter block under 32 KB
 constexpr uint32_t kQueueSlots = 4096;      // concurrent queue launches per device
 struct QueueParams {
 	uint32_t n, total_tiles, slot, pad;
+	uint32_t *tiles_done;   // per batch, zeroed before the launch (nullable)
+	uint32_t *done_flags;   // per batch, set to 1 when its last tile is written (nullable, may be host-mapped)
 	QueueBatch b[kMaxQueueBatches];
 };
 static_assert(sizeof(QueueParams) <= 32000, "kernel parameter limit");

@@ -60,6 +60,10 @@ struct Slot {
 	cudaEvent_t done = nullptr;
 	bool busy = false;
 	std::vector<Request> reqs;
+	std::vector<char> fin;           // request already completed through its flag
+	uint32_t *d_counters = nullptr;  // tile counters of the queue launch
+	uint32_t *h_flags = nullptr;     // host-mapped completion flags, one per request
+	uint32_t *d_flags = nullptr;     // their device address
 };
 
 struct TicketState {
@@ -226,6 +230,10 @@ bool lrx_server::launch_one(std::unique_lock<std::mutex> &lk) {
 		scenes[r.scene]->inflight++;
 		scenes[r.scene]->last_used = ++use_clock;
 	}
+	// shortest first: the queue kernel hands out tiles in batch order, so small
+	// requests finish (and raise their flags) before the large ones
+	if (!plain)
+		std::stable_sort(take.begin(), take.end(), [](const Request &a, const Request &b) { return a.count < b.count; });
 	std::vector<lrx_batch> batch;
 	batch.reserve(take.size());
 	for (const Request &r : take)
@@ -236,7 +244,8 @@ bool lrx_server::launch_one(std::unique_lock<std::mutex> &lk) {
 		for (const lrx_batch &b : batch)
 			if ((rc = lrx_trace(b.scene, b.d_rays, b.d_hits, b.count, b.mode, slot->stream)) != LRX_OK) break;
 	} else {
-		rc = lrx_trace_batches(batch.data(), (uint32_t)batch.size(), slot->stream);
+		for (size_t i = 0; i < batch.size(); ++i) reinterpret_cast<volatile uint32_t *>(slot->h_flags)[i] = 0u;
+		rc = lrx_trace_batches_ex(batch.data(), (uint32_t)batch.size(), slot->stream, slot->d_counters, slot->d_flags);
 	}
 	std::string err = rc == LRX_OK ? std::string() : std::string(lrx_last_error());
 	if (rc == LRX_OK && cudaEventRecord(slot->done, slot->stream) != cudaSuccess) {
@@ -254,6 +263,7 @@ bool lrx_server::launch_one(std::unique_lock<std::mutex> &lk) {
 		return true;
 	}
 	slot->reqs.swap(take);
+	slot->fin.assign(slot->reqs.size(), 0);
 	slot->busy = true;
 	++launches;
 	return true;
@@ -264,11 +274,23 @@ void lrx_server::reap(std::unique_lock<std::mutex> &) {
 	bool any = false;
 	for (Slot &s : slots) {
 		if (!s.busy) continue;
+		if (opts.policy != LRX_SERVE_PLAIN) {
+			// requests whose batch already finished inside a running launch
+			for (size_t i = 0; i < s.reqs.size(); ++i) {
+				if (s.fin[i] || !reinterpret_cast<volatile uint32_t *>(s.h_flags)[i]) continue;
+				s.fin[i] = 1;
+				scenes[s.reqs[i].scene]->inflight--;
+				finish(s.reqs[i], LRX_OK, std::string());
+				any = true;
+			}
+		}
 		const cudaError_t q = cudaEventQuery(s.done);
 		if (q == cudaErrorNotReady) continue;
 		const lrx_status st = q == cudaSuccess ? LRX_OK : LRX_ERR_CUDA;
 		const std::string err = q == cudaSuccess ? std::string() : std::string(cudaGetErrorString(q));
-		for (const Request &r : s.reqs) {
+		for (size_t i = 0; i < s.reqs.size(); ++i) {
+			if (s.fin[i]) continue;
+			const Request &r = s.reqs[i];
 			scenes[r.scene]->inflight--;
 			finish(r, st, err);
 		}
@@ -285,9 +307,13 @@ void lrx_server::run() {
 		err = "cannot create the server's streams";
 	for (Slot &s : slots) {
 		if (!err.empty()) break;
+		const size_t words = opts.max_requests_per_launch;
 		if (cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking) != cudaSuccess ||
-				cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming) != cudaSuccess)
-			err = "cannot create the server's streams";
+				cudaEventCreateWithFlags(&s.done, cudaEventDisableTiming) != cudaSuccess ||
+				cudaMalloc(&s.d_counters, sizeof(uint32_t) * words) != cudaSuccess ||
+				cudaHostAlloc(&s.h_flags, sizeof(uint32_t) * words, cudaHostAllocMapped) != cudaSuccess ||
+				cudaHostGetDevicePointer((void **)&s.d_flags, s.h_flags, 0) != cudaSuccess)
+			err = "cannot create the server's streams and completion flags";
 	}
 	std::unique_lock<std::mutex> lk(mu);
 	started = true;
@@ -315,6 +341,8 @@ void lrx_server::run() {
 	for (Slot &s : slots) {
 		if (s.done) cudaEventDestroy(s.done);
 		if (s.stream) cudaStreamDestroy(s.stream);
+		if (s.d_counters) cudaFree(s.d_counters);
+		if (s.h_flags) cudaFreeHost(s.h_flags);
 	}
 	if (build_stream) cudaStreamDestroy(build_stream);
 }

@@ -391,6 +391,19 @@ __global__ void __launch_bounds__(kTileRays) k_trace_queue(const __grid_constant
 			if (a.two_level) trace_ray<false, true, false, CV>(a, tid, active, cnt);
 			else trace_ray<false, false, false, CV>(a, tid, active, cnt);
 		}
+		if (p.done_flags) {
+			// completion notice per batch: every thread's hits are fenced, then
+			// the block that finishes the batch's last tile raises its flag
+			__threadfence_system();
+			__syncthreads();
+			if (threadIdx.x == 0) {
+				const uint32_t ntiles = (qb.count + kTileRays - 1) / kTileRays;
+				if (atomicAdd(&p.tiles_done[qb.user_index], 1u) + 1u == ntiles) {
+					__threadfence_system();
+					*reinterpret_cast<volatile uint32_t *>(&p.done_flags[qb.user_index]) = 1u;
+				}
+			}
+		}
 	}
 	if (threadIdx.x == 0) {
 		__threadfence();

@@ -32,7 +32,8 @@ EXPORTED = ["lrx_abi_version", "lrx_last_error", "lrx_scene_create", "lrx_scene_
             "lrx_scene_update_instances", "lrx_scene_get_info", "lrx_trace", "lrx_trace_host",
             "lrx_trace_counted", "lrx_scene_device_status", "lrx_trace_host_noalloc",
             "lrx_scene_set_trace_config", "lrx_scene_get_trace_config", "lrx_trace_batches",
-            "lrx_scene_autotune", "lrx_server_create", "lrx_server_destroy", "lrx_server_add_scene",
+            "lrx_scene_autotune", "lrx_trace_batches_ex", "lrx_server_create", "lrx_server_destroy",
+            "lrx_server_add_scene",
             "lrx_server_submit", "lrx_server_wait", "lrx_server_get_stats", "lrx_server_reset_stats"]
 LRX_SERVE_BATCHED = 0
 LRX_SERVE_PLAIN = 1
