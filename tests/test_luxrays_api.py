@@ -31,7 +31,7 @@ def compile_demo(out_dir, syntax_only=False):
                 f"-Wl,-rpath,{lib_dir}", "-L", os.path.join(CUDA, "lib64"), "-lcudart",
                 f"-Wl,-rpath,{os.path.join(CUDA, 'lib64')}"]
     subprocess.check_call(cmd)
-    return os.path.join(out_dir, "luxrays_api_demo")
+    return None if syntax_only else os.path.join(out_dir, "luxrays_api_demo")
 
 
 @pytest.mark.skipif(shutil.which("g++") is None, reason="needs g++")
