@@ -171,19 +171,61 @@ def load_peaks():
 
 
 def load_traffic_per_ray():
-    """DRAM bytes per ray of the traversal kernel from the committed ncu
-    summary (profiles/trace_heightfield_ncu.md, line `dram_bytes_per_ray:`)."""
+    """DRAM bytes per ray of each ray set's traversal launch, from the
+    committed ncu summary (profiles/trace_heightfield_ncu.md, lines
+    `dram_bytes_per_ray_<set>: <bytes>`)."""
     p = os.path.join(ROOT, "profiles", "trace_heightfield_ncu.md")
+    out = {}
     if not os.path.exists(p):
-        return None
+        return out
     with open(p) as f:
         for ln in f:
-            if ln.strip().startswith("dram_bytes_per_ray:"):
+            ln = ln.strip().strip("`")
+            if ln.startswith("dram_bytes_per_ray_"):
+                key, _, val = ln.partition(":")
                 try:
-                    return float(ln.split(":", 1)[1].split()[0])
-                except ValueError:
-                    return None
-    return None
+                    out[key[len("dram_bytes_per_ray_"):]] = float(val.split()[0])
+                except (ValueError, IndexError):
+                    pass
+    return out
+
+
+def count_kernel_launches(stream_handle, fn):
+    """Kernels that fn() enqueues on the stream: the calls are captured into a
+    CUDA graph (driver API, relaxed mode; nothing runs) and its kernel nodes
+    counted -- this includes the ray-sort kernels of sorted launches.  None if
+    the capture is not possible."""
+    import ctypes
+    try:
+        cu = ctypes.CDLL("libcuda.so.1")
+        s = ctypes.c_void_p(stream_handle)
+        if cu.cuStreamBeginCapture_v2(s, ctypes.c_int(2)) != 0:  # CU_STREAM_CAPTURE_MODE_RELAXED
+            return None
+        ok = True
+        try:
+            fn()
+        except Exception:  # a call that cannot be captured: no count
+            ok = False
+        g = ctypes.c_void_p()
+        rc = cu.cuStreamEndCapture(s, ctypes.byref(g))
+        if rc != 0 or not g.value:
+            return None
+        if not ok:
+            cu.cuGraphDestroy(g)
+            return None
+        n = ctypes.c_size_t(0)
+        cu.cuGraphGetNodes(g, None, ctypes.byref(n))
+        nodes = (ctypes.c_void_p * n.value)()
+        cu.cuGraphGetNodes(g, nodes, ctypes.byref(n))
+        kernels = 0
+        for k in range(n.value):
+            t = ctypes.c_int(-1)
+            cu.cuGraphNodeGetType(ctypes.c_void_p(nodes[k]), ctypes.byref(t))
+            kernels += t.value == 0  # CU_GRAPH_NODE_TYPE_KERNEL
+        cu.cuGraphDestroy(g)
+        return kernels
+    except (OSError, AttributeError):
+        return None
 
 
 # ---------------------------------------------------------------------------
@@ -265,7 +307,7 @@ def run_lrx(args):
     build_s = time.perf_counter() - t0
     if args.block_size is not None or args.postpone is not None or args.variant is not None:
         scene.set_trace_config(args.block_size or 64, 8 if args.postpone is None else args.postpone,
-                               args.variant or 0)
+                               args.variant or 0, refill=args.refill or 0)
     saved_cfg = {m: scene.trace_config(m) for m in (lrx.LRX_TRACE_CLOSEST, lrx.LRX_TRACE_ANY)}
     info = scene.info()
 
@@ -324,6 +366,7 @@ def run_lrx(args):
     stream.synchronize()
     if scene.device_status(st) != 0:
         raise RuntimeError("device status word set during warm-up")
+    launches_per_step = count_kernel_launches(st, step)
     log(f"[bench] {time.strftime('%H:%M:%S')} warm-up done, timing {args.steps} steps")
 
     ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in dev]
@@ -353,10 +396,11 @@ def run_lrx(args):
     # for comparison; outside the timed region
     alt = {}
     if args.sweep:
-        for bs, pp, var in [(64, 8, 0), (64, 8, 16), (64, 8, 48), (64, 8, 52), (32, 8, 48), (128, 8, 48),
-                            (64, 4, 48), (64, 16, 48), (64, 8, 4)]:
-            scene.set_trace_config(bs, pp, var)
-            key = f"b{bs}-p{pp}-v{var}"
+        for bs, pp, var, rf in [(64, 8, 0, 0), (64, 8, 64, 16), (64, 8, 64, 8), (64, 8, 64, 24), (64, 8, 64, 4),
+                                (128, 8, 64, 16), (32, 8, 64, 16), (64, 0, 64, 16), (64, 16, 64, 16),
+                                (64, 8, 68, 16), (64, 8, 16, 0), (64, 8, 80, 16), (64, 8, 80, 8)]:
+            scene.set_trace_config(bs, pp, var, refill=rf)
+            key = f"b{bs}-p{pp}-v{var}-r{rf}"
             alt[key] = {}
             for name, dr, dh, n, mode in dev:
                 e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -368,7 +412,8 @@ def run_lrx(args):
                 e1.synchronize()
                 alt[key][name] = round(n * 5 / (e0.elapsed_time(e1) / 1e3) / 1e6, 1)
         for m, c in saved_cfg.items():
-            scene.set_trace_config(c["block_size"], c["postpone"], c["variant"], modes=2 if m == lrx.LRX_TRACE_ANY else 1)
+            scene.set_trace_config(c["block_size"], c["postpone"], c["variant"], modes=2 if m == lrx.LRX_TRACE_ANY else 1,
+                                   refill=c["refill"])
 
     # roofline of the traversal kernel: algorithmic bytes / kernel time
     peak, peak_kind = load_peaks()
@@ -376,7 +421,9 @@ def run_lrx(args):
     tot_ms = sum(kern_ms.values())
     achieved = tot_alg / (tot_ms / 1e3) / 1e9
     tpr = load_traffic_per_ray()
-    traffic = None if tpr is None else tpr * rays_per_step / len(dev)
+    traffic = None
+    if all(name in tpr for name, *_r in dev):  # DRAM bytes per trace launch, averaged over the sets
+        traffic = round(sum(tpr[name] * n for name, _dr, _dh, n, _m in dev) / len(dev))
 
     # end to end: host rays in pinned memory -> lrx_trace_host -> host hits
     e2e_value = None
@@ -437,7 +484,8 @@ def run_lrx(args):
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "api": "lrx_trace_host (pinned host buffers)"},
-            "gpu_launches": len(dev) * args.steps,
+            "gpu_launches": (launches_per_step if launches_per_step is not None else len(dev)) * args.steps,
+            "gpu_launches_per_step": launches_per_step,
             "clocks": clk,
         }
         print(json.dumps(line), flush=True)
@@ -736,6 +784,7 @@ def main():
     ap.add_argument("--block-size", type=int, default=None, help="override the per-mode defaults")
     ap.add_argument("--postpone", type=int, default=None)
     ap.add_argument("--variant", type=int, default=None, help="LRX_VARIANT_* bits")
+    ap.add_argument("--refill", type=int, default=None, help="with LRX_VARIANT_PERSISTENT: idle lanes per claim")
     args = ap.parse_args()
     if args.warmup < 3:
         log("warmup raised to 3 (timing rule)")

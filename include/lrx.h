@@ -24,7 +24,7 @@
 extern "C" {
 #endif
 
-#define LRX_ABI_VERSION 1u
+#define LRX_ABI_VERSION 2u
 #define LRX_NULL_INDEX 0xffffffffu      /* luxrays_types.cl:21 */
 #define LRX_RAY_FLAGS_MASKED 0x1u       /* ray_types.cl:22 */
 
@@ -166,6 +166,9 @@ typedef struct lrx_trace_config {
 	uint32_t variant;         /* LRX_VARIANT_* bits */
 	uint32_t modes;           /* set: which trace modes take this config (bit 0 closest,
 	                             bit 1 any-hit; 0 = both).  get: bit 1 set reads the any-hit one */
+	uint32_t refill;          /* with LRX_VARIANT_PERSISTENT: idle lanes of a warp that trigger
+	                             its next ray claim, 1-32 (0 = 16).  Added in ABI 2: a caller
+	                             passing the 20-byte ABI 1 struct gets 0 */
 } lrx_trace_config;
 #define LRX_VARIANT_MINMAX3 0x1u       /* 3-input min/max in the slab tests */
 #define LRX_VARIANT_SCENE_L2_KEEP 0x2u /* node/triangle loads marked evict-last in L2 */
@@ -175,6 +178,8 @@ typedef struct lrx_trace_config {
                                           origin before tracing (hits stay in caller order) */
 #define LRX_VARIANT_SORT_OCTANT 0x20u  /* with SORT_RAYS: key on the direction octant only
                                           (one radix pass, caller order kept within an octant) */
+#define LRX_VARIANT_PERSISTENT 0x40u   /* persistent warps claim rays from a device counter
+                                          (ballot + shuffle) and refill idle lanes; blocks <= 128 */
 
 /* Sets / reads the launch configuration lrx_trace uses for this scene.
  * No reference counterpart (the reference fixes 32-thread blocks,
@@ -184,7 +189,8 @@ lrx_status lrx_scene_get_trace_config(const lrx_scene *scene, lrx_trace_config *
 
 /* Autotuner: traces the sample batch (device rays) under each candidate
  * launch configuration -- block size {32, 64, 128} x postpone {0, 8, 16} x
- * variant {none, streaming ray access, ray sort} -- keeps the fastest for
+ * variant {none, streaming ray access, ray sort, persistent (refill 8),
+ * persistent + streaming} -- keeps the fastest for
  * `mode` in the scene and returns it in `chosen` (nullable).  Synchronises
  * `stream`; do not trace the same scene from other threads meanwhile.
  * No reference counterpart (the reference fixes its launch shape). */

@@ -112,13 +112,20 @@ struct TraceArgs {
 	uint32_t variant = 0;          // lrx_trace_config.variant bits
 	uint32_t visit_limit = 1u << 24;  // node visits after which a ray is abandoned (status bit 1)
 	const uint32_t *order = nullptr;  // thread i traces ray order[i] (sorted launches)
+	uint32_t refill = 0;           // persistent fetch: idle lanes that trigger a warp's claim (0 = 16)
 };
 constexpr uint32_t kTraceBlock = 128;
 constexpr uint32_t kVarSortRays = 0x10u;   // reorder rays by octant + origin before tracing
 constexpr uint32_t kVarSortOctantOnly = 0x20u;  // ... by direction octant only (one radix pass)
+constexpr uint32_t kVarPersistent = 0x40u;  // persistent warps with warp-level ray fetch
+constexpr uint32_t kVarAll = 0x7fu;        // every defined variant bit
 constexpr uint32_t kSortMinRays = 32768;   // smaller batches are traced in caller order
 
 lrx_status launch_trace(const TraceArgs &a, cudaStream_t stream);
+
+// Counter slot for the next persistent launch (round robin over kQueueSlots;
+// a slot is reused only kQueueSlots launches later).
+uint32_t next_queue_slot();
 
 // One batch of a multi-batch queue launch (kernel parameter space).
 struct QueueBatch {

@@ -22,6 +22,7 @@
 // that moment (__activemask, no waiting) while node work remains -- then the
 // group is pushed and tested later, which keeps lanes in step.
 #include <algorithm>
+#include <atomic>
 
 #include "lrx_common.cuh"
 #include "lrx_internal.h"
@@ -151,6 +152,180 @@ struct Counts {
 	uint32_t nodes, tris, insts, rays;
 };
 
+// Traversal state of one ray between loop trips.
+struct TravState {
+	ActiveRay ray;             // in the current BVH's space (world, or an instance's local space)
+	float3 wo, wd;             // world-space origin / direction
+	float mint, best_t, best_b1, best_b2;
+	uint32_t best_mesh, best_tri;
+	uint32_t inst_obj;         // object of the instance being traversed (kNull at top level)
+	uint32_t visits;
+	int sp, inst_sp;           // stack depth; depth at which the current BLAS was entered (-1: none)
+	uint2 ng, tg;              // node group, triangle (or instance) group
+};
+// The traversal stack lives apart from TravState so that the state's scalars
+// stay in registers (a dynamically indexed member would put the whole
+// struct in local memory).
+typedef uint2 TravStack[kStackSize];
+
+enum : int { kRayMasked = 0, kRayAnswered = 1, kRayTraverse = 2 };
+
+// Reads ray i and sets up its traversal.  kRayMasked: skip it and write
+// nothing (bvh.cl:243-244); kRayAnswered: the initial miss (t = maxt) is the
+// answer -- empty scene, NaN/infinite origin or direction, NaN maxt;
+// kRayTraverse: traverse.
+__device__ __forceinline__ int ray_begin(const TraceArgs &a, uint32_t i, bool stream, TravState &s) {
+	const float4 *rp = reinterpret_cast<const float4 *>(a.rays) + 3 * (size_t)i;
+	float4 r0, r1, r2;
+	if (stream) {
+		r0 = __ldcs(rp);
+		r1 = __ldcs(rp + 1);
+		r2 = __ldcs(rp + 2);
+	} else {
+		r0 = __ldg(rp);
+		r1 = __ldg(rp + 1);
+		r2 = __ldg(rp + 2);
+	}
+	if (__float_as_uint(r2.y) & LRX_RAY_FLAGS_MASKED) return kRayMasked;
+	s.wo = make_float3(r0.x, r0.y, r0.z);
+	s.wd = make_float3(r0.w, r1.x, r1.y);
+	s.mint = r1.z;
+	s.best_t = r1.w;
+	s.best_b1 = 0.f;
+	s.best_b2 = 0.f;
+	s.best_mesh = kNull;
+	s.best_tri = kNull;
+	if (a.root == kNull || !finite3(s.wo) || !finite3(s.wd) || isnan(s.best_t)) return kRayAnswered;
+	make_active(s.ray, s.wo, s.wd);
+	s.sp = 0;
+	s.inst_sp = -1;
+	s.inst_obj = kNull;
+	s.visits = 0;
+	s.ng = make_uint2(a.root, (1u << (24 + s.ray.oct)) | 1u);
+	s.tg = make_uint2(0u, 0u);
+	return kRayTraverse;
+}
+
+// One trip of the traversal loop: expand one node (or take a popped group),
+// test the triangles it yields (or enter one instance), pop when the node
+// group is spent.  Returns true when the ray is finished: stack empty, any
+// hit found, or abandoned (stack overflow / visit limit, recorded in the
+// status word).  Every trip either expands a node -- at most visit_limit of
+// them -- or consumes a stack entry or an instance bit, so a ray finishes in
+// a bounded number of trips.
+template <bool ANY, bool TWO_LEVEL, bool COUNT, bool MM3>
+__device__ __forceinline__ bool ray_step(const TraceArgs &a, TravState &s, TravStack &stack, bool keep, uint64_t pol,
+		Counts &c) {
+#define LRX_PUSH(V)                                          \
+	{                                                        \
+		if (s.sp >= kStackSize) {                            \
+			atomicOr(a.status, kStatusStackOverflow);        \
+			return true;                                     \
+		}                                                    \
+		stack[s.sp++] = (V);                                 \
+	}
+	if (s.ng.y > 0x00ffffffu) {
+		const uint32_t j = __ffs(s.ng.y >> 24) - 1;
+		s.ng.y &= ~(1u << (24 + j));
+		const uint32_t sl = j ^ s.ray.oct;
+		const uint32_t node = s.ng.x + __popc(s.ng.y & ((1u << sl) - 1u) & 0xffu);
+		if (s.ng.y > 0x00ffffffu) LRX_PUSH(s.ng);
+		if (++s.visits > a.visit_limit) {
+			atomicOr(a.status, kStatusVisitLimit);
+			return true;
+		}
+		if (COUNT) ++c.nodes;
+		const NodeHits h = intersect_node<MM3>(a.nodes, node, s.ray, s.mint, s.best_t, keep, pol);
+		s.ng = make_uint2(h.child_base, (h.ihits << 24) | h.imask);
+		s.tg = make_uint2(h.tri_base, h.tmask);
+	} else {
+		s.tg = s.ng;  // a popped triangle (or, at top level, instance) group
+		s.ng = make_uint2(0u, 0u);
+	}
+	if (TWO_LEVEL && s.inst_sp < 0) {
+		if (s.tg.y) {
+			// top-level leaf: enter one instance, keep the rest for later
+			const uint32_t k = __ffs(s.tg.y) - 1;
+			s.tg.y &= s.tg.y - 1;
+			if (s.ng.y > 0x00ffffffu) LRX_PUSH(s.ng);
+			if (s.tg.y) LRX_PUSH(s.tg);
+			const InstRecord *ir = a.insts + s.tg.x + k;
+			const uint4 info = __ldg(reinterpret_cast<const uint4 *>(&ir->info));
+			if (COUNT) ++c.insts;
+			s.inst_obj = info.y;
+			if (info.z & kInstIdentity) {
+				make_active(s.ray, s.wo, s.wd);
+			} else {
+				const float4 m0 = __ldg(&ir->r0), m1 = __ldg(&ir->r1), m2 = __ldg(&ir->r2), m3 = __ldg(&ir->r3);
+				make_active(s.ray, xform_point(m0, m1, m2, m3, s.wo), xform_vector(m0, m1, m2, s.wd));
+			}
+			s.inst_sp = s.sp;
+			s.ng = info.x == kNull ? make_uint2(0u, 0u) : make_uint2(info.x, (1u << (24 + s.ray.oct)) | 1u);
+			s.tg = make_uint2(0u, 0u);
+			return false;
+		}
+	} else {
+		while (s.tg.y) {
+			// Any-hit never defers: the hit it returns must depend only on the
+			// ray and the tree, not on which rays share its warp.
+			if (!ANY && s.ng.y > 0x00ffffffu && __popc(__activemask()) < a.postpone) {
+				LRX_PUSH(s.tg);  // test later, when the warp does triangles together
+				s.tg.y = 0;
+				break;
+			}
+			const uint32_t k = __ffs(s.tg.y) - 1;
+			s.tg.y &= s.tg.y - 1;
+			const float4 *tp = reinterpret_cast<const float4 *>(a.tris + s.tg.x + k);
+			const float4 ta = ld_scene_f4(tp, keep, pol), tb = ld_scene_f4(tp + 1, keep, pol),
+					tc = ld_scene_f4(tp + 2, keep, pol);
+			if (COUNT) ++c.tris;
+			float t, b1, b2;
+			if (tri_intersect(s.ray.o, s.ray.d, s.mint, s.best_t, make_float3(ta.x, ta.y, ta.z),
+					make_float3(tb.x, tb.y, tb.z), make_float3(tc.x, tc.y, tc.z), t, b1, b2)) {
+				const uint32_t tri = __float_as_uint(ta.w);
+				uint32_t mesh = __float_as_uint(tb.w);
+				if (TWO_LEVEL && mesh == kNull) mesh = s.inst_obj;
+				if (ANY || t < s.best_t || mesh < s.best_mesh || (mesh == s.best_mesh && tri < s.best_tri)) {
+					s.best_t = t;
+					s.best_b1 = b1;
+					s.best_b2 = b2;
+					s.best_mesh = mesh;
+					s.best_tri = tri;
+					if (ANY) return true;
+				}
+			}
+		}
+	}
+	if (s.ng.y <= 0x00ffffffu) {
+		if (TWO_LEVEL && s.inst_sp == s.sp) {  // this instance's BLAS is exhausted
+			s.inst_sp = -1;
+			s.inst_obj = kNull;
+			make_active(s.ray, s.wo, s.wd);
+		}
+		if (s.sp == 0) return true;
+		s.ng = stack[--s.sp];
+	}
+	return false;
+#undef LRX_PUSH
+}
+
+__device__ __forceinline__ void ray_write(const TraceArgs &a, uint32_t i, const TravState &s, bool stream) {
+	uint32_t *hp = reinterpret_cast<uint32_t *>(a.hits) + 5 * (size_t)i;
+	if (stream) {
+		__stcs(hp, __float_as_uint(s.best_t));
+		__stcs(hp + 1, __float_as_uint(s.best_b1));
+		__stcs(hp + 2, __float_as_uint(s.best_b2));
+		__stcs(hp + 3, s.best_mesh);
+		__stcs(hp + 4, s.best_tri);
+	} else {
+		hp[0] = __float_as_uint(s.best_t);
+		hp[1] = __float_as_uint(s.best_b1);
+		hp[2] = __float_as_uint(s.best_b2);
+		hp[3] = s.best_mesh;
+		hp[4] = s.best_tri;
+	}
+}
+
 // Traces ray `tid` of the batch `a` (through a.order when set) and writes its
 // hit.  Shared by the one-batch kernel and the multi-batch queue kernel.
 template <bool ANY, bool TWO_LEVEL, bool COUNT, uint32_t CV>
@@ -161,158 +336,15 @@ __device__ __forceinline__ void trace_ray(const TraceArgs &a, uint32_t tid, bool
 	const bool keep = (a.variant & kVarSceneEvictLast) != 0;
 	const bool stream = (a.variant & kVarStreamRays) != 0;
 	const uint64_t pol = keep ? evict_last_policy() : 0ull;
-	float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f), r1 = r0, r2 = r0;
-	if (active) {
-		const float4 *rp = reinterpret_cast<const float4 *>(a.rays) + 3 * (size_t)i;
-		if (stream) {
-			r0 = __ldcs(rp);
-			r1 = __ldcs(rp + 1);
-			r2 = __ldcs(rp + 2);
-		} else {
-			r0 = __ldg(rp);
-			r1 = __ldg(rp + 1);
-			r2 = __ldg(rp + 2);
+	TravState s;
+	TravStack stack;
+	const int k = ray_begin(a, i, stream, s);
+	if (k == kRayMasked) return;
+	if (k == kRayTraverse)
+		while (!ray_step<ANY, TWO_LEVEL, COUNT, MM3>(a, s, stack, keep, pol, cnt)) {
 		}
-		if (__float_as_uint(r2.y) & LRX_RAY_FLAGS_MASKED) return;  // bvh.cl:243-244
-	}
-
-	const float3 wo = make_float3(r0.x, r0.y, r0.z);
-	const float3 wd = make_float3(r0.w, r1.x, r1.y);
-	const float mint = r1.z;
-	float best_t = r1.w, best_b1 = 0.f, best_b2 = 0.f;
-	uint32_t best_mesh = kNull, best_tri = kNull;
-	uint32_t n_nodes = 0, n_tris = 0, n_insts = 0;
-
-	if (active && a.root != kNull && finite3(wo) && finite3(wd) && !isnan(best_t)) {
-		ActiveRay ray;
-		make_active(ray, wo, wd);
-		uint2 stack[kStackSize];
-		int sp = 0;
-		int inst_sp = -1;          // stack depth at which the current BLAS was entered
-		uint32_t inst_obj = kNull;
-		uint32_t visits = 0;
-		uint2 ng = make_uint2(a.root, (1u << (24 + ray.oct)) | 1u);
-		uint2 tg = make_uint2(0u, 0u);
-#define LRX_PUSH(V)                                          \
-	{                                                        \
-		if (sp >= kStackSize) {                              \
-			atomicOr(a.status, kStatusStackOverflow);        \
-			break;                                           \
-		}                                                    \
-		stack[sp++] = (V);                                   \
-	}
-		for (;;) {
-			if (ng.y > 0x00ffffffu) {
-				const uint32_t j = __ffs(ng.y >> 24) - 1;
-				ng.y &= ~(1u << (24 + j));
-				const uint32_t s = j ^ ray.oct;
-				const uint32_t node = ng.x + __popc(ng.y & ((1u << s) - 1u) & 0xffu);
-				if (ng.y > 0x00ffffffu) LRX_PUSH(ng);
-				if (++visits > a.visit_limit) {
-					atomicOr(a.status, kStatusVisitLimit);
-					break;
-				}
-				if (COUNT) ++n_nodes;
-				const NodeHits h = intersect_node<MM3>(a.nodes, node, ray, mint, best_t, keep, pol);
-				ng = make_uint2(h.child_base, (h.ihits << 24) | h.imask);
-				tg = make_uint2(h.tri_base, h.tmask);
-			} else {
-				tg = ng;  // a popped triangle (or, at top level, instance) group
-				ng = make_uint2(0u, 0u);
-			}
-			if (TWO_LEVEL && inst_sp < 0) {
-				if (tg.y) {
-					// top-level leaf: enter one instance, keep the rest for later
-					const uint32_t k = __ffs(tg.y) - 1;
-					tg.y &= tg.y - 1;
-					if (ng.y > 0x00ffffffu) LRX_PUSH(ng);
-					if (tg.y) LRX_PUSH(tg);
-					const InstRecord *ir = a.insts + tg.x + k;
-					const uint4 info = __ldg(reinterpret_cast<const uint4 *>(&ir->info));
-					if (COUNT) ++n_insts;
-					inst_obj = info.y;
-					if (info.z & kInstIdentity) {
-						make_active(ray, wo, wd);
-					} else {
-						const float4 m0 = __ldg(&ir->r0), m1 = __ldg(&ir->r1), m2 = __ldg(&ir->r2), m3 = __ldg(&ir->r3);
-						make_active(ray, xform_point(m0, m1, m2, m3, wo), xform_vector(m0, m1, m2, wd));
-					}
-					inst_sp = sp;
-					ng = info.x == kNull ? make_uint2(0u, 0u) : make_uint2(info.x, (1u << (24 + ray.oct)) | 1u);
-					tg = make_uint2(0u, 0u);
-					continue;
-				}
-			} else {
-				bool done = false;
-				while (tg.y) {
-					// Any-hit never defers: the hit it returns must depend only on the
-					// ray and the tree, not on which rays share its warp.
-					if (!ANY && ng.y > 0x00ffffffu && __popc(__activemask()) < a.postpone) {
-						LRX_PUSH(tg);  // test later, when the warp does triangles together
-						tg.y = 0;
-						break;
-					}
-					const uint32_t k = __ffs(tg.y) - 1;
-					tg.y &= tg.y - 1;
-					const float4 *tp = reinterpret_cast<const float4 *>(a.tris + tg.x + k);
-					const float4 ta = ld_scene_f4(tp, keep, pol), tb = ld_scene_f4(tp + 1, keep, pol),
-							tc = ld_scene_f4(tp + 2, keep, pol);
-					if (COUNT) ++n_tris;
-					float t, b1, b2;
-					if (tri_intersect(ray.o, ray.d, mint, best_t, make_float3(ta.x, ta.y, ta.z),
-							make_float3(tb.x, tb.y, tb.z), make_float3(tc.x, tc.y, tc.z), t, b1, b2)) {
-						const uint32_t tri = __float_as_uint(ta.w);
-						uint32_t mesh = __float_as_uint(tb.w);
-						if (TWO_LEVEL && mesh == kNull) mesh = inst_obj;
-						if (ANY || t < best_t || mesh < best_mesh || (mesh == best_mesh && tri < best_tri)) {
-							best_t = t;
-							best_b1 = b1;
-							best_b2 = b2;
-							best_mesh = mesh;
-							best_tri = tri;
-							if (ANY) {
-								done = true;
-								break;
-							}
-						}
-					}
-				}
-				if (done || tg.y) break;  // any hit found, or a push failed
-			}
-			if (ng.y <= 0x00ffffffu) {
-				if (TWO_LEVEL && inst_sp == sp) {  // this instance's BLAS is exhausted
-					inst_sp = -1;
-					inst_obj = kNull;
-					make_active(ray, wo, wd);
-				}
-				if (sp == 0) break;
-				ng = stack[--sp];
-			}
-		}
-#undef LRX_PUSH
-	}
-	if (active) {
-		uint32_t *hp = reinterpret_cast<uint32_t *>(a.hits) + 5 * (size_t)i;
-		if (stream) {
-			__stcs(hp, __float_as_uint(best_t));
-			__stcs(hp + 1, __float_as_uint(best_b1));
-			__stcs(hp + 2, __float_as_uint(best_b2));
-			__stcs(hp + 3, best_mesh);
-			__stcs(hp + 4, best_tri);
-		} else {
-			hp[0] = __float_as_uint(best_t);
-			hp[1] = __float_as_uint(best_b1);
-			hp[2] = __float_as_uint(best_b2);
-			hp[3] = best_mesh;
-			hp[4] = best_tri;
-		}
-	}
-	if (COUNT) {
-		cnt.nodes += n_nodes;
-		cnt.tris += n_tris;
-		cnt.insts += n_insts;
-		cnt.rays += 1;
-	}
+	ray_write(a, i, s, stream);
+	if (COUNT) cnt.rays += 1;
 }
 
 template <bool ANY, bool TWO_LEVEL, bool COUNT, uint32_t CV>
@@ -339,6 +371,90 @@ k_trace(TraceArgs a) {
 	}
 }
 
+__device__ uint32_t g_queue[kQueueSlots][2];  // (next tile / ray, blocks finished) per slot
+
+// Slot protocol shared by the persistent kernels: a launch owns slot
+// (counter, finished blocks), both zero at entry; every block adds itself to
+// the finished count once it has stopped claiming work, and the last one
+// zeroes the slot for its next user.
+__device__ __forceinline__ void release_slot(uint32_t *slot) {
+	if (threadIdx.x == 0) {
+		__threadfence();
+		if (atomicAdd(&slot[1], 1u) == gridDim.x - 1) {  // every block has stopped claiming work
+			slot[0] = 0u;
+			slot[1] = 0u;
+			__threadfence();
+		}
+	}
+}
+
+uint32_t next_queue_slot() {
+	static std::atomic<uint32_t> next{0};
+	return next.fetch_add(1u) % kQueueSlots;
+}
+
+// ---------------------------------------------------------------------------
+// Persistent single-batch kernel with warp-level ray fetch (after Aila and
+// Laine 2009, "dynamic fetch"): resident warps loop until the batch's ray
+// counter runs out.  Each trip a warp ballots its idle lanes; once at least
+// `refill` are idle (or all are), the lowest idle lane claims that many rays
+// with one atomicAdd and __shfl_sync hands each idle lane its index, so a
+// warp keeps its lanes busy instead of idling behind its longest ray.  Then
+// every busy lane runs one ray_step.
+//
+// Termination: a trip either advances some lane's ray (each ray finishes in
+// a bounded number of trips, see ray_step) or, with every lane idle, claims
+// 32 rays from the counter or leaves -- the counter only grows, so the
+// claims run out.  Every ballot/shuffle is executed by all 32 lanes: the
+// block is a whole number of warps, no lane leaves the loop alone (the exit
+// test is warp-uniform), and `refill` is in [1, 32].
+// ---------------------------------------------------------------------------
+
+template <bool ANY, bool TWO_LEVEL, uint32_t CV>
+__global__ void __launch_bounds__(kTraceBlock, 8) k_trace_fetch(TraceArgs a, uint32_t slot_index, uint32_t refill) {
+	constexpr bool MM3 = (CV & kVarMinMax3) != 0;
+	uint32_t *slot = g_queue[slot_index];
+	const bool keep = (a.variant & kVarSceneEvictLast) != 0;
+	const bool stream = (a.variant & kVarStreamRays) != 0;
+	const uint64_t pol = keep ? evict_last_policy() : 0ull;
+	const uint32_t lane = threadIdx.x & 31u;
+	TravState s;
+	TravStack stack;
+	Counts cnt{0, 0, 0, 0};
+	uint32_t rid = kNull;  // ray this lane traces (kNull: idle)
+	bool drained = false;  // warp-uniform: the counter has passed the batch
+	for (;;) {
+		const uint32_t idle = __ballot_sync(0xffffffffu, rid == kNull);
+		const uint32_t nidle = __popc(idle);
+		if (!drained && nidle >= refill) {
+			const uint32_t leader = __ffs(idle) - 1;
+			uint32_t base = 0;
+			if (lane == leader) base = atomicAdd(&slot[0], nidle);
+			base = __shfl_sync(0xffffffffu, base, leader);
+			drained = base + nidle >= a.count;
+			if (rid == kNull) {
+				const uint32_t idx = base + __popc(idle & ((1u << lane) - 1u));
+				if (idx < a.count) {
+					const uint32_t i = a.order ? a.order[idx] : idx;
+					const int k = ray_begin(a, i, stream, s);
+					if (k == kRayTraverse) rid = i;
+					else if (k == kRayAnswered) ray_write(a, i, s, stream);
+				}
+			}
+		}
+		if (__ballot_sync(0xffffffffu, rid != kNull) == 0u) {
+			if (drained) break;
+			continue;  // every lane idle: the next trip claims 32 rays
+		}
+		if (rid != kNull && ray_step<ANY, TWO_LEVEL, false, MM3>(a, s, stack, keep, pol, cnt)) {
+			ray_write(a, rid, s, stream);
+			rid = kNull;
+		}
+	}
+	__syncthreads();
+	release_slot(slot);
+}
+
 // ---------------------------------------------------------------------------
 // Multi-batch queue kernel: one launch drains many ray batches (any mix of
 // scenes and modes).  Persistent 64-thread blocks claim 64-ray tiles from a
@@ -347,8 +463,6 @@ k_trace(TraceArgs a) {
 // barrier is block-uniform (the tile index is broadcast through shared
 // memory), and the loop ends when the tiles run out.
 // ---------------------------------------------------------------------------
-
-__device__ uint32_t g_queue[kQueueSlots][2];  // (next tile, blocks finished) per slot
 
 template <uint32_t CV>
 __global__ void __launch_bounds__(kTileRays) k_trace_queue(const __grid_constant__ QueueParams p) {
@@ -405,14 +519,7 @@ __global__ void __launch_bounds__(kTileRays) k_trace_queue(const __grid_constant
 			}
 		}
 	}
-	if (threadIdx.x == 0) {
-		__threadfence();
-		if (atomicAdd(&slot[1], 1u) == gridDim.x - 1) {  // every block has stopped claiming tiles
-			slot[0] = 0u;
-			slot[1] = 0u;
-			__threadfence();
-		}
-	}
+	release_slot(slot);
 }
 
 lrx_status launch_trace_queue(const QueueParams &p, cudaStream_t st) {
@@ -431,6 +538,28 @@ lrx_status launch_trace_queue(const QueueParams &p, cudaStream_t st) {
 	return LRX_OK;
 }
 
+// Persistent fetch launch: as many blocks as fit on the device at once (at
+// most one ray per thread), all sharing one counter slot.
+template <bool ANY, bool TWO_LEVEL, uint32_t CV>
+static lrx_status launch_fetch(const TraceArgs &a, uint32_t bs, cudaStream_t st) {
+	static int resident[kTraceBlock / 32] = {0};  // blocks per SM for bs = 32, 64, 96, 128
+	static int sms = 0;
+	int &per_sm = resident[bs / 32 - 1];
+	if (per_sm == 0 || sms == 0) {
+		int dev = 0, n = 0, r = 0;
+		LRX_CUDA(cudaGetDevice(&dev));
+		LRX_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
+		LRX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_trace_fetch<ANY, TWO_LEVEL, CV>, (int)bs, 0));
+		sms = n;
+		per_sm = std::max(1, r);
+	}
+	const uint32_t grid = (uint32_t)std::min<uint64_t>(((uint64_t)a.count + bs - 1) / bs, (uint64_t)sms * per_sm);
+	const uint32_t refill = a.refill == 0 ? 16u : std::min(32u, a.refill);
+	k_trace_fetch<ANY, TWO_LEVEL, CV><<<grid, bs, 0, st>>>(a, next_queue_slot(), refill);
+	LRX_CUDA(cudaGetLastError());
+	return LRX_OK;
+}
+
 lrx_status launch_trace(const TraceArgs &a, cudaStream_t st) {
 	if (a.count == 0) return LRX_OK;
 	uint32_t bs = a.block_size ? a.block_size : kTraceBlock;
@@ -440,6 +569,15 @@ lrx_status launch_trace(const TraceArgs &a, cudaStream_t st) {
 	}
 	const uint32_t grid = (a.count + bs - 1) / bs;
 	const bool cnt = a.counters != nullptr;
+	if ((a.variant & kVarPersistent) && !cnt && a.count < 0x80000000u) {
+		// persistent warps with ray fetch; block size capped at kTraceBlock
+		const uint32_t fbs = std::min(bs, kTraceBlock);
+		const bool mm3 = (a.variant & kVarMinMax3) != 0;
+#define LRX_FETCH(A, T) (mm3 ? launch_fetch<A, T, kVarMinMax3>(a, fbs, st) : launch_fetch<A, T, 0u>(a, fbs, st))
+		if (a.any_hit) return a.two_level ? LRX_FETCH(true, true) : LRX_FETCH(true, false);
+		return a.two_level ? LRX_FETCH(false, true) : LRX_FETCH(false, false);
+#undef LRX_FETCH
+	}
 	// compile-time variants; the occupancy-bounded build only takes <= 64-thread blocks
 	uint32_t cv = a.variant & (kVarMinMax3 | kVarOccupancy);
 	if (bs > 64) cv &= ~kVarOccupancy;

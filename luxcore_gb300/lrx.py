@@ -22,6 +22,16 @@ LRX_TRACE_CLOSEST = 0
 LRX_TRACE_ANY = 1
 LRX_OBJECT_INSTANCE = 0x1
 LRX_OBJECT_HAS_INVERSE = 0x2
+LRX_ERR_INVALID_ARGUMENT = 1
+
+# lrx_trace_config.variant bits (include/lrx.h)
+LRX_VARIANT_MINMAX3 = 0x1
+LRX_VARIANT_SCENE_L2_KEEP = 0x2
+LRX_VARIANT_STREAM_RAYS = 0x4
+LRX_VARIANT_OCCUPANCY = 0x8
+LRX_VARIANT_SORT_RAYS = 0x10
+LRX_VARIANT_SORT_OCTANT = 0x20
+LRX_VARIANT_PERSISTENT = 0x40
 
 STATUS_NAMES = {0: "LRX_OK", 1: "LRX_ERR_INVALID_ARGUMENT", 2: "LRX_ERR_CUDA", 3: "LRX_ERR_OUT_OF_MEMORY",
                 4: "LRX_ERR_BUILD", 5: "LRX_ERR_DEVICE", 6: "LRX_ERR_NOT_SUPPORTED", 7: "LRX_ERR_BUDGET",
@@ -63,7 +73,8 @@ class BuildOpts(ctypes.Structure):
 
 class TraceConfig(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_uint32), ("block_size", ctypes.c_uint32),
-                ("postpone", ctypes.c_uint32), ("variant", ctypes.c_uint32), ("modes", ctypes.c_uint32)]
+                ("postpone", ctypes.c_uint32), ("variant", ctypes.c_uint32), ("modes", ctypes.c_uint32),
+                ("refill", ctypes.c_uint32)]
 
 
 class SceneInfo(ctypes.Structure):
@@ -308,24 +319,29 @@ class Scene:
         check(load().lrx_scene_get_info(self.handle, ctypes.byref(inf)))
         return inf.as_dict()
 
-    def set_trace_config(self, block_size: int = 64, postpone: int = 8, variant: int = 0, modes: int = 0):
-        """modes: 1 = closest-hit launches, 2 = any-hit launches, 0 = both."""
-        c = TraceConfig(ctypes.sizeof(TraceConfig), block_size, postpone, variant, modes)
+    def set_trace_config(self, block_size: int = 64, postpone: int = 8, variant: int = 0, modes: int = 0,
+                         refill: int = 0):
+        """modes: 1 = closest-hit launches, 2 = any-hit launches, 0 = both.
+        refill: with LRX_VARIANT_PERSISTENT, idle lanes that trigger a warp's
+        next ray claim (0 = the library default)."""
+        c = TraceConfig(ctypes.sizeof(TraceConfig), block_size, postpone, variant, modes, refill)
         check(load().lrx_scene_set_trace_config(self.handle, ctypes.byref(c)))
 
     def trace_config(self, mode: int = LRX_TRACE_CLOSEST) -> dict:
         c = TraceConfig()
+        c.struct_size = ctypes.sizeof(TraceConfig)
         c.modes = 2 if mode == LRX_TRACE_ANY else 1
         check(load().lrx_scene_get_trace_config(self.handle, ctypes.byref(c)))
-        return {"block_size": c.block_size, "postpone": c.postpone, "variant": c.variant}
+        return {"block_size": c.block_size, "postpone": c.postpone, "variant": c.variant, "refill": c.refill}
 
     def autotune(self, d_rays: int, count: int, mode: int = LRX_TRACE_CLOSEST, stream: int = 0) -> dict:
         """Picks this scene's fastest launch configuration for `mode` on a
         device-resident sample of rays."""
         c = TraceConfig()
+        c.struct_size = ctypes.sizeof(TraceConfig)
         check(load().lrx_scene_autotune(self.handle, ctypes.c_void_p(d_rays), count, mode,
                                         ctypes.c_void_p(stream), ctypes.byref(c)))
-        return {"block_size": c.block_size, "postpone": c.postpone, "variant": c.variant}
+        return {"block_size": c.block_size, "postpone": c.postpone, "variant": c.variant, "refill": c.refill}
 
     def update_instances(self, scene: W.SceneDesc, stream: int = 0):
         objs = _object_array(scene)

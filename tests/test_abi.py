@@ -34,7 +34,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_abi_version_and_error_string(lib):
-    assert lib.lrx_abi_version() == 1
+    assert lib.lrx_abi_version() == 2
     assert isinstance(lib.lrx_last_error(), bytes)
 
 
@@ -44,6 +44,15 @@ def test_struct_layouts():
     assert ctypes.sizeof(lrx.MeshDesc) == 24
     assert ctypes.sizeof(lrx.ObjectDesc) == 136
     assert ctypes.sizeof(lrx.BuildOpts) == 16
+    assert ctypes.sizeof(lrx.TraceConfig) == 24
+
+
+def test_variant_constants_match_the_header():
+    src = open(os.path.join(ROOT, "include", "lrx.h")).read()
+    defs = dict(re.findall(r"#define (LRX_VARIANT_[A-Z0-9_]+) (0x[0-9a-fA-F]+)u", src))
+    assert defs, "no variant defines parsed"
+    for name, val in defs.items():
+        assert getattr(lrx, name) == int(val, 16), name
 
 
 def test_null_arguments_are_rejected_without_a_device(lib):

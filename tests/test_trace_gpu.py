@@ -21,17 +21,24 @@ from parity import check_anyhit, compare  # noqa: E402
 pytestmark = pytest.mark.gpu
 
 SENT = 0xDEADBEEF
-# launch configurations every parity test runs under: (block size, postpone, variant bits)
+# launch configurations every parity test runs under:
+# (block size, postpone, variant bits[, refill])
 KERNELS = pytest.mark.parametrize("kernel", [(128, 0, 0), (64, 8, 0), (256, 24, 0), (64, 8, 0xF), (128, 8, 0x7),
-                                             (64, 8, 0x10), (32, 8, 0x1F), (64, 8, 0x30)],
+                                             (64, 8, 0x10), (32, 8, 0x1F), (64, 8, 0x30),
+                                             (64, 8, 0x40), (128, 0, 0x41, 1), (32, 8, 0x46, 32),
+                                             (64, 8, 0x50, 8)],
                                   ids=["b128", "b64-p8", "b256-p24", "b64-p8-allvariants", "b128-p8-mm3-hints",
-                                       "b64-p8-sorted", "b32-p8-sorted-all", "b64-p8-octsort"])
+                                       "b64-p8-sorted", "b32-p8-sorted-all", "b64-p8-octsort",
+                                       "b64-p8-persistent", "b128-persistent-refill1",
+                                       "b32-p8-persistent-refill32-hints", "b64-p8-sorted-persistent-refill8"])
 
 
 def make_scene(desc, kernel=(64, 8, 0), **kw):
     s = lrx.Scene(desc, **kw)
-    s.set_trace_config(*kernel)
-    assert s.trace_config() == {"block_size": kernel[0], "postpone": kernel[1], "variant": kernel[2]}
+    refill = kernel[3] if len(kernel) > 3 else 0
+    s.set_trace_config(*kernel[:3], refill=refill)
+    assert s.trace_config() == {"block_size": kernel[0], "postpone": kernel[1], "variant": kernel[2],
+                                "refill": refill}
     return s
 
 
@@ -296,6 +303,24 @@ def test_rejects_bad_arguments(torch_cuda):
         lrx.Scene(sing)                                        # singular instance transform
 
 
+def test_trace_config_struct_versions(torch_cuda):
+    """The ABI-1 struct (no refill field) is still accepted on set and get;
+    out-of-range values and unknown variant bits are rejected."""
+    import ctypes
+    scene, _ = W.config1(n_tris=100, n_rays=64, seed=92)
+    s = lrx.Scene(scene)
+    L = lrx.load()
+    old = lrx.TraceConfig(20, 64, 4, lrx.LRX_VARIANT_PERSISTENT, 0, 99)  # refill beyond the 20 bytes: ignored
+    assert L.lrx_scene_set_trace_config(s.handle, ctypes.byref(old)) == 0
+    assert s.trace_config() == {"block_size": 64, "postpone": 4, "variant": lrx.LRX_VARIANT_PERSISTENT, "refill": 0}
+    got = lrx.TraceConfig(20, 0, 0, 0, 0, 77)
+    assert L.lrx_scene_get_trace_config(s.handle, ctypes.byref(got)) == 0
+    assert (got.struct_size, got.block_size, got.refill) == (20, 64, 77)  # nothing past 20 bytes written
+    for bad in [lrx.TraceConfig(16, 64, 8, 0, 0, 0), lrx.TraceConfig(24, 64, 8, 0x80, 0, 0),
+                lrx.TraceConfig(24, 64, 8, 0x40, 0, 33), lrx.TraceConfig(24, 48, 8, 0, 0, 0)]:
+        assert L.lrx_scene_set_trace_config(s.handle, ctypes.byref(bad)) == lrx.LRX_ERR_INVALID_ARGUMENT
+
+
 def test_trace_batches_equals_per_batch_traces(torch_cuda):
     """lrx_trace_batches over a ragged mix of scenes, modes and sizes
     (including empty, single-ray and tile-boundary batches, and more batches
@@ -329,3 +354,24 @@ def test_trace_batches_equals_per_batch_traces(torch_cuda):
         got = h.cpu().numpy().view(W.HIT_DTYPE)[:n]
         bad = np.nonzero(got.view(np.uint32).reshape(-1, 5) != ref.view(np.uint32).reshape(-1, 5))[0]
         assert bad.size == 0, (n, m, bad[:5], got[bad[:3]], ref[bad[:3]])
+
+
+def test_autotune_picks_a_valid_config_and_keeps_results(torch_cuda):
+    """lrx_scene_autotune returns one of its candidates, installs it for that
+    mode only, and traces under it match the oracle."""
+    torch = torch_cuda
+    scene, rays = W.config1(n_tris=30000, n_rays=50000, seed=501)
+    s = lrx.Scene(scene)
+    d_r = torch.from_numpy(rays.view(np.uint8).reshape(-1).copy()).cuda()
+    before_any = s.trace_config(lrx.LRX_TRACE_ANY)
+    st = torch.cuda.current_stream().cuda_stream
+    chosen = s.autotune(d_r.data_ptr(), rays.shape[0], lrx.LRX_TRACE_CLOSEST, st)
+    assert chosen["block_size"] in (32, 64, 128) and chosen["postpone"] in (0, 8, 16)
+    assert chosen["variant"] in (0, lrx.LRX_VARIANT_STREAM_RAYS, lrx.LRX_VARIANT_SORT_RAYS,
+                                 lrx.LRX_VARIANT_PERSISTENT, lrx.LRX_VARIANT_PERSISTENT | lrx.LRX_VARIANT_STREAM_RAYS)
+    assert chosen["refill"] == (8 if chosen["variant"] & lrx.LRX_VARIANT_PERSISTENT else 0)
+    assert s.trace_config(lrx.LRX_TRACE_CLOSEST) == chosen
+    assert s.trace_config(lrx.LRX_TRACE_ANY) == before_any
+    o = po.OracleScene(scene)
+    ref, _ = o.intersect(rays)
+    assert_parity(gpu_trace(torch, s, rays), ref, o, rays, min_hit_rate=0.05)
