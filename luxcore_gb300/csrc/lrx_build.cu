@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(128) k_collapse(const uint2 *__restrict__ item
 			qhz[wsel] |= qhi(cb[k].hi.z, nlo.z, iz) << sh;
 			if (ccount[k] > leaf_max) {
 				imask |= 1u << s;
-				meta[wsel] |= kInternalMeta << sh;
+				meta[wsel] |= (kInternalMetaBase + s) << sh;
 				const uint32_t slot = atomicAdd(n_out, 1u);
 				if (slot < cap) out_items[slot] = make_uint2(cref[k], child_base + int_rank);
 				else atomicOr(&counters[C_ERR], 2u);

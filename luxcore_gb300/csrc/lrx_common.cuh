@@ -20,7 +20,7 @@ constexpr uint32_t kNull = 0xffffffffu;
 constexpr int kStackSize = 64;       // traversal stack entries per ray
 constexpr int kMaxTreeDepth = 30;    // per tree; TLAS + BLAS + 1 <= kStackSize
 constexpr uint32_t kInstGroup = 0x00800000u;  // stack entry holds instance bits
-constexpr uint32_t kInternalMeta = 0x1Fu;     // meta byte of an internal child
+constexpr uint32_t kInternalMetaBase = 0x38u;  // meta byte of internal slot s: 0x38 + s = (1 << 5) | (24 + s)
 
 // Status word bits (lrx_scene_device_status)
 constexpr uint32_t kStatusStackOverflow = 1u;
@@ -34,9 +34,11 @@ constexpr uint32_t kMaxVisits = 1u << 24;
 //   w[3] = (qlo_z[0..3], qlo_z[4..7], qhi_x[0..3], qhi_x[4..7])
 //   w[4] = (qhi_y[0..3], qhi_y[4..7], qhi_z[0..3], qhi_z[4..7])
 // Child slot s is internal iff imask bit s; its node index is
-// child_base + popc(imask & ((1 << s) - 1)).  A leaf slot's meta is
-// (unary triangle count << 5) | offset from tri_base; an internal slot's meta
-// is kInternalMeta; an empty slot's meta is 0.
+// child_base + popc(imask & ((1 << s) - 1)).  Every meta byte is
+// (bit run << 5) | bit position of a 32-bit hit mask: a leaf slot's is
+// (unary triangle count << 5) | offset from tri_base (offsets < 24), an
+// internal slot's is (1 << 5) | (24 + s) -- bit 24 + s, which traversal
+// XORs with the ray's octant -- and an empty slot's is 0 (no bits).
 struct alignas(16) WideNode {
 	uint4 w[5];
 };

@@ -41,12 +41,6 @@ __device__ __forceinline__ void make_active(ActiveRay &r, float3 o, float3 d) {
 	r.oct = (r.idir.x < 0.f ? 1u : 0u) | (r.idir.y < 0.f ? 2u : 0u) | (r.idir.z < 0.f ? 4u : 0u);
 }
 
-// Byte k of w as a float, exactly: PRMT builds 0x4B0000bb (= 2^23 + b).
-template <int K>
-__device__ __forceinline__ float byte_as_float(uint32_t w) {
-	return __uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + K)) - 8388608.f;
-}
-
 struct NodeHits {
 	uint32_t child_base, tri_base, imask;
 	uint32_t ihits;  // internal children, bit j = slot (j ^ oct)
@@ -92,9 +86,42 @@ __device__ __forceinline__ float4 ld_scene_f4(const float4 *p, bool keep, uint64
 	return make_float4(__uint_as_float(v.x), __uint_as_float(v.y), __uint_as_float(v.z), __uint_as_float(v.w));
 }
 
+// Packed FP32 pair arithmetic (fma.rn.f32x2 / add.rn.f32x2, sm_100+): each
+// half is rounded exactly like the scalar fmaf / __fadd_rn.
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+	float2 d;
+	asm("{\n\t.reg .b64 pa, pb, pc, pd;\n\t"
+	    "mov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\tmov.b64 pc, {%6, %7};\n\t"
+	    "fma.rn.f32x2 pd, pa, pb, pc;\n\tmov.b64 {%0, %1}, pd;\n\t}"
+			: "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+	return d;
+}
+__device__ __forceinline__ float2 add2(float2 a, float2 b) {
+	float2 d;
+	asm("{\n\t.reg .b64 pa, pb, pd;\n\t"
+	    "mov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+	    "add.rn.f32x2 pd, pa, pb;\n\tmov.b64 {%0, %1}, pd;\n\t}"
+			: "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+	return d;
+}
+
+// Plane distances of slots (4H + K, 4H + K + 1) on one axis: quantised bytes
+// K, K+1 of w -> exact floats (PRMT builds 2^23 + b, the packed add takes
+// 2^23 off exactly), then t = q * a + b per half, one rounding each.
+template <int K>
+__device__ __forceinline__ float2 plane_pair(uint32_t w, float a, float b) {
+	const float2 q = make_float2(__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + K)),
+			__uint_as_float(__byte_perm(w, 0x4B000000u, 0x7540u + K + 1)));
+	return fma2(add2(q, make_float2(-8388608.f, -8388608.f)), make_float2(a, a), make_float2(b, b));
+}
+
 // Slab test of the 8 quantised child boxes.  t = q * (scale * idir) +
 // (origin - o) * idir; NaN plane distances (zero direction components) are
-// dropped by fminf/fmaxf, which only ever keeps a child.
+// dropped by fminf/fmaxf, which only ever keeps a child.  A hit child adds
+// its meta bits to one 32-bit mask -- bits 0-23 its triangles, bit
+// 24 + (slot ^ octant) an internal child -- with the octant XOR and the bit
+// fields taken for four slots at a time from a meta word; empty slots
+// (meta 0) add nothing whatever their planes.
 template <bool MM3>
 __device__ __forceinline__ NodeHits intersect_node(const WideNode *__restrict__ nodes, uint32_t idx,
 		const ActiveRay &r, float tmin, float tmax, bool keep, uint64_t pol) {
@@ -120,27 +147,38 @@ __device__ __forceinline__ NodeHits intersect_node(const WideNode *__restrict__ 
 	const uint32_t fy[2] = {py ? w4.x : w2.z, py ? w4.y : w2.w};
 	const uint32_t nz[2] = {pz ? w3.x : w4.z, pz ? w3.y : w4.w};
 	const uint32_t fz[2] = {pz ? w4.z : w3.x, pz ? w4.w : w3.y};
-	const uint32_t mw[2] = {w1.z, w1.w};
-	uint32_t ih = 0, tm = 0;
-#define LRX_CHILD(S)                                                                                      \
-	{                                                                                                     \
-		constexpr int H = (S) >> 2, K = (S) & 3;                                                          \
-		const float tnx = fmaf(byte_as_float<K>(nx[H]), ax, bx), tny = fmaf(byte_as_float<K>(ny[H]), ay, by); \
-		const float tnz = fmaf(byte_as_float<K>(nz[H]), az, bz);                                          \
-		const float tfx = fmaf(byte_as_float<K>(fx[H]), ax, bx), tfy = fmaf(byte_as_float<K>(fy[H]), ay, by); \
-		const float tfz = fmaf(byte_as_float<K>(fz[H]), az, bz);                                          \
-		const float tn = MM3 ? fmaxf(max3f(tnx, tny, tnz), tmin) : fmaxf(fmaxf(tnx, tny), fmaxf(tnz, tmin)); \
-		const float tf = MM3 ? fminf(min3f(tfx, tfy, tfz), tmax) : fminf(fminf(tfx, tfy), fminf(tfz, tmax)); \
-		const uint32_t m = (mw[H] >> (8 * K)) & 0xffu;                                                    \
-		if (tn <= tf && m != 0u) {                                                                        \
-			if (h.imask & (1u << (S))) ih |= 1u << ((S) ^ r.oct);                                         \
-			else tm |= ((m >> 5) & 7u) << (m & 31u);                                                      \
-		}                                                                                                 \
+	// per meta word: bit position (internal slots XORed with the octant) and bit run, bytewise
+	uint32_t bpos[2], brun[2];
+#pragma unroll
+	for (int H = 0; H < 2; ++H) {
+		const uint32_t m4 = H ? w1.w : w1.z;
+		const uint32_t inner4 = (m4 & (m4 << 1)) & 0x10101010u;  // bits 4 and 3 set: position >= 24
+		bpos[H] = (m4 ^ ((inner4 >> 4) * r.oct)) & 0x1f1f1f1fu;
+		brun[H] = (m4 >> 5) & 0x07070707u;
 	}
-	LRX_CHILD(0) LRX_CHILD(1) LRX_CHILD(2) LRX_CHILD(3) LRX_CHILD(4) LRX_CHILD(5) LRX_CHILD(6) LRX_CHILD(7)
-#undef LRX_CHILD
-	h.ihits = ih;
-	h.tmask = tm;
+	uint32_t hm = 0;
+#define LRX_PAIR(S)                                                                                   \
+	{                                                                                                 \
+		constexpr int H = (S) >> 2, K = (S) & 3;                                                      \
+		const float2 tnx = plane_pair<K>(nx[H], ax, bx), tny = plane_pair<K>(ny[H], ay, by);          \
+		const float2 tnz = plane_pair<K>(nz[H], az, bz);                                              \
+		const float2 tfx = plane_pair<K>(fx[H], ax, bx), tfy = plane_pair<K>(fy[H], ay, by);          \
+		const float2 tfz = plane_pair<K>(fz[H], az, bz);                                              \
+		const float tn0 = MM3 ? fmaxf(max3f(tnx.x, tny.x, tnz.x), tmin)                              \
+				: fmaxf(fmaxf(tnx.x, tny.x), fmaxf(tnz.x, tmin));                                     \
+		const float tf0 = MM3 ? fminf(min3f(tfx.x, tfy.x, tfz.x), tmax)                              \
+				: fminf(fminf(tfx.x, tfy.x), fminf(tfz.x, tmax));                                     \
+		const float tn1 = MM3 ? fmaxf(max3f(tnx.y, tny.y, tnz.y), tmin)                              \
+				: fmaxf(fmaxf(tnx.y, tny.y), fmaxf(tnz.y, tmin));                                     \
+		const float tf1 = MM3 ? fminf(min3f(tfx.y, tfy.y, tfz.y), tmax)                              \
+				: fminf(fminf(tfx.y, tfy.y), fminf(tfz.y, tmax));                                     \
+		if (tn0 <= tf0) hm |= ((brun[H] >> (8 * K)) & 0xffu) << ((bpos[H] >> (8 * K)) & 0xffu);      \
+		if (tn1 <= tf1) hm |= ((brun[H] >> (8 * K + 8)) & 0xffu) << ((bpos[H] >> (8 * K + 8)) & 0xffu); \
+	}
+	LRX_PAIR(0) LRX_PAIR(2) LRX_PAIR(4) LRX_PAIR(6)
+#undef LRX_PAIR
+	h.ihits = hm >> 24;
+	h.tmask = hm & 0x00ffffffu;
 	return h;
 }
 
@@ -465,7 +503,7 @@ __global__ void __launch_bounds__(kTraceBlock, 8) k_trace_fetch(TraceArgs a, uin
 // ---------------------------------------------------------------------------
 
 template <uint32_t CV>
-__global__ void __launch_bounds__(kTileRays) k_trace_queue(const __grid_constant__ QueueParams p) {
+__global__ void __launch_bounds__(kTileRays, 12) k_trace_queue(const __grid_constant__ QueueParams p) {
 	__shared__ uint32_t s_tile;
 	uint32_t *slot = g_queue[p.slot];
 	Counts cnt{0, 0, 0, 0};
