@@ -535,6 +535,26 @@ def run_batching(args):
     torch.cuda.synchronize()
     log(f"[batching] {len(items)} batches, {total_rays} rays resident")
 
+    def plain():
+        for s, rec, hits, n, mode in items:
+            s.trace(rec.data_ptr(), hits.data_ptr(), n, mode, st)
+
+    # the plain form under the library's default launch configuration,
+    # before any autotuning
+    def timed_plain_default():
+        with torch.cuda.stream(stream):
+            plain()
+            stream.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(args.steps):
+                plain()
+            e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    default_ms = timed_plain_default()
+
     # per-scene autotune on a 262,144-ray sample of each mode
     tuned = {}
     if not args.no_autotune:
@@ -543,10 +563,6 @@ def run_batching(args):
             tuned[k] = {m: s.autotune(sample.data_ptr(), 1 << 18, m, st)
                         for m in (lrx.LRX_TRACE_CLOSEST, lrx.LRX_TRACE_ANY)}
         torch.cuda.synchronize()
-
-    def plain():
-        for s, rec, hits, n, mode in items:
-            s.trace(rec.data_ptr(), hits.data_ptr(), n, mode, st)
 
     arr = lrx.batch_array([(s, rec.data_ptr(), hits.data_ptr(), n, mode) for s, rec, hits, n, mode in items])
 
@@ -590,6 +606,7 @@ def run_batching(args):
         if s.device_status(st) != 0:
             raise RuntimeError("device status word set")
     mrays = {k: round(total_rays / (v[0] / 1e3) / 1e6, 1) for k, v in res.items()}
+    mrays["plain_default_config"] = round(total_rays / (default_ms / 1e3) / 1e6, 1)
     line = {
         "metric": "Mrays/s on uneven batches (batched queue kernel + CUDA graph vs one launch per RayBuffer)",
         "value": mrays["batched_graph"], "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": 1,
@@ -601,6 +618,9 @@ def run_batching(args):
                    "device_ms_by_form": {k: round(v[0], 3) for k, v in res.items()},
                    "host_ms_by_form": {k: round(v[1], 3) for k, v in res.items()},
                    "batched_over_plain": round(mrays["batched_graph"] / mrays["plain"], 3),
+                   "batched_over_plain_default_config": round(mrays["batched_graph"] / mrays["plain_default_config"], 3),
+                   "plain": "one lrx_trace per RayBuffer with the autotuned per-scene configs (the same configs "
+                            "the batched form uses); plain_default_config: the library defaults, no autotune",
                    "results_equal_plain": bool(same), "autotuned": tuned},
     }
     print(json.dumps(line), flush=True)

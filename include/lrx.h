@@ -207,11 +207,15 @@ typedef struct lrx_batch {
 } lrx_batch;
 
 /* Traces many ray batches -- any mix of scenes (on one device) and modes --
- * with one launch of a persistent queue kernel per 384 batches: 64-thread
- * blocks claim 64-ray tiles from a device work queue until every batch is
- * done, so small and uneven batches share the GPU instead of each paying a
- * launch and a tail.  Results equal lrx_trace on each batch.  Asynchronous
- * on `stream`; graph-capturable (no allocation, no host synchronisation).
+ * with one launch of a persistent queue kernel per 384 batches, so small and
+ * uneven batches share the GPU instead of each paying a launch and a tail.
+ * When any batch's scene config for its mode has LRX_VARIANT_PERSISTENT (the
+ * closest-hit default), the batches form one ray index space and persistent
+ * warps claim rays from it with ballot/shuffle, refilling idle lanes (a
+ * warp's lanes may then hold rays of different batches); otherwise 64-thread
+ * blocks claim 64-ray tiles.  Ray sorting is not applied.  Results equal
+ * lrx_trace on each batch.  Asynchronous on `stream`; graph-capturable (no
+ * allocation, no host synchronisation).
  * Replaces: a sequence of HardwareIntersectionKernel::EnqueueTraceRayBuffer
  * calls (hardwareintersectiondevice.h:67-68), one per RayBuffer. */
 lrx_status lrx_trace_batches(const lrx_batch *batches, uint32_t batch_count, void *stream);
@@ -221,7 +225,7 @@ lrx_status lrx_trace_batches(const lrx_batch *batches, uint32_t batch_count, voi
  * soon as batch k is finished, while other batches of the launch may still
  * run -- the flags may live in host-mapped memory and be polled by the host.
  * The caller zeroes the flags; d_tile_counters (batch_count words of device
- * memory) is scratch that the call zeroes on `stream`.  Flags of empty batches
+ * memory) is scratch -- per-batch progress -- that the call zeroes on `stream`.  Flags of empty batches
  * are not written.  No reference counterpart. */
 lrx_status lrx_trace_batches_ex(const lrx_batch *batches, uint32_t batch_count, void *stream,
 		uint32_t *d_tile_counters, uint32_t *d_done_flags);

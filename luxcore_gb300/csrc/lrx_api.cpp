@@ -815,8 +815,26 @@ lrx_status lrx_trace_batches_ex(const lrx_batch *batches, uint32_t n_batches, vo
 	if (!params) params.reset(new QueueParams());
 	QueueParams &p = *params;
 	cudaStream_t st = (cudaStream_t)stream;
+	// Warp-level ray fetch when any batch's scene asks for persistent warps in
+	// its mode (refill from the first such config) and every batch fits one
+	// fetch launch; otherwise 64-ray tiles per block.
+	uint32_t fetch = 0, refill = 16;
+	for (uint32_t k = 0; k < n_batches; ++k) {
+		const lrx_trace_config &cfg = batches[k].scene->tcfg[batches[k].mode == LRX_TRACE_ANY ? 1 : 0];
+		if (!fetch && (cfg.variant & kVarPersistent)) {
+			fetch = 1;
+			if (cfg.refill) refill = std::min(32u, cfg.refill);
+		}
+		if (batches[k].count > kMaxFetchRays) {
+			fetch = 0;
+			break;
+		}
+	}
 	p.n = 0;
 	p.total_tiles = 0;
+	p.total_rays = 0;
+	p.fetch = fetch;
+	p.refill = refill;
 	p.tiles_done = d_tile_counters;
 	p.done_flags = d_done_flags;
 	if (d_tile_counters) LRX_CUDA(cudaMemsetAsync(d_tile_counters, 0, sizeof(uint32_t) * n_batches, st));
@@ -826,6 +844,7 @@ lrx_status lrx_trace_batches_ex(const lrx_batch *batches, uint32_t n_batches, vo
 		lrx_status rc = launch_trace_queue(p, st);
 		p.n = 0;
 		p.total_tiles = 0;
+		p.total_rays = 0;
 		return rc;
 	};
 	for (uint32_t k = 0; k < n_batches; ++k) {
@@ -833,7 +852,8 @@ lrx_status lrx_trace_batches_ex(const lrx_batch *batches, uint32_t n_batches, vo
 		if (b.count == 0) continue;
 		lrx_scene *s = b.scene;
 		const uint32_t tiles = (b.count + kTileRays - 1) / kTileRays;
-		if (p.n == kMaxQueueBatches || (uint64_t)p.total_tiles + tiles > 0xffffffffull) {
+		if (p.n == kMaxQueueBatches || (uint64_t)p.total_tiles + tiles > 0xffffffffull ||
+				(fetch && (uint64_t)p.total_rays + b.count > kMaxFetchRays)) {
 			lrx_status rc = flush();
 			if (rc != LRX_OK) return rc;
 		}
@@ -848,6 +868,7 @@ lrx_status lrx_trace_batches_ex(const lrx_batch *batches, uint32_t n_batches, vo
 		q.root = s->root;
 		q.count = b.count;
 		q.tile_begin = p.total_tiles;
+		q.ray_begin = p.total_rays;
 		// runtime-selectable variants only (cache hints); the queue kernel does not sort
 		const uint32_t var = cfg.variant & (LRX_VARIANT_SCENE_L2_KEEP | LRX_VARIANT_STREAM_RAYS);
 		q.flags = (b.mode == LRX_TRACE_ANY ? 1u : 0u) | (s->two_level ? 2u : 0u) | ((cfg.postpone & 0xffu) << 8) |
@@ -855,6 +876,7 @@ lrx_status lrx_trace_batches_ex(const lrx_batch *batches, uint32_t n_batches, vo
 		q.visit_limit = scene_visit_limit(s);
 		q.user_index = k;
 		p.total_tiles += tiles;
+		p.total_rays += fetch ? b.count : 0u;
 	}
 	return flush();
 }

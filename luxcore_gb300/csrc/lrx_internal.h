@@ -136,7 +136,8 @@ struct QueueBatch {
 	void *hits;
 	uint32_t *status;
 	uint32_t root, count;
-	uint32_t tile_begin;   // first 64-ray tile of this batch in the launch
+	uint32_t tile_begin;   // first 64-ray tile of this batch in the launch (tile kernel)
+	uint32_t ray_begin;    // first ray of this batch in the launch's ray index space (fetch kernel)
 	uint32_t flags;        // bit 0 any-hit, bit 1 two-level, bits 8-15 postpone, bits 16-23 variant
 	uint32_t visit_limit;
 	uint32_t user_index;   // the caller's index of this batch (completion flags)
@@ -144,10 +145,14 @@ struct QueueBatch {
 constexpr uint32_t kTileRays = 64;
 constexpr uint32_t kMaxQueueBatches = 384;  // keeps the parameter block under 32 KB
 constexpr uint32_t kQueueSlots = 4096;      // concurrent queue launches per device
+constexpr uint32_t kMaxFetchRays = 0x7fffffffu;  // rays per fetch-kernel launch (claims stay below 2^32)
 struct QueueParams {
-	uint32_t n, total_tiles, slot, pad;
-	uint32_t *tiles_done;   // per batch, zeroed before the launch (nullable)
-	uint32_t *done_flags;   // per batch, set to 1 when its last tile is written (nullable, may be host-mapped)
+	uint32_t n, total_tiles, slot;
+	uint32_t fetch;         // 1: warp-level ray fetch (k_trace_queue_fetch), 0: 64-ray tiles per block
+	uint32_t total_rays;    // fetch kernel: rays in the launch (<= kMaxFetchRays)
+	uint32_t refill;        // fetch kernel: idle lanes that trigger a warp's claim, 1-32
+	uint32_t *tiles_done;   // per batch progress (tiles, or rays with `fetch`), zeroed before the launch (nullable)
+	uint32_t *done_flags;   // per batch, set to 1 when its last ray is written (nullable, may be host-mapped)
 	QueueBatch b[kMaxQueueBatches];
 };
 static_assert(sizeof(QueueParams) <= 32000, "kernel parameter limit");

@@ -502,6 +502,24 @@ __global__ void __launch_bounds__(kTraceBlock, 8) k_trace_fetch(TraceArgs a, uin
 // memory), and the loop ends when the tiles run out.
 // ---------------------------------------------------------------------------
 
+__device__ __forceinline__ TraceArgs batch_args(const QueueBatch &qb) {
+	TraceArgs a{};
+	a.nodes = qb.nodes;
+	a.tris = qb.tris;
+	a.insts = qb.insts;
+	a.root = qb.root;
+	a.two_level = (qb.flags >> 1) & 1u;
+	a.rays = qb.rays;
+	a.hits = qb.hits;
+	a.count = qb.count;
+	a.any_hit = qb.flags & 1u;
+	a.status = qb.status;
+	a.postpone = (qb.flags >> 8) & 0xffu;
+	a.variant = (qb.flags >> 16) & 0xffu;
+	a.visit_limit = qb.visit_limit;
+	return a;
+}
+
 template <uint32_t CV>
 __global__ void __launch_bounds__(kTileRays, 12) k_trace_queue(const __grid_constant__ QueueParams p) {
 	__shared__ uint32_t s_tile;
@@ -520,20 +538,7 @@ __global__ void __launch_bounds__(kTileRays, 12) k_trace_queue(const __grid_cons
 			else hi = mid;
 		}
 		const QueueBatch &qb = p.b[lo];
-		TraceArgs a{};
-		a.nodes = qb.nodes;
-		a.tris = qb.tris;
-		a.insts = qb.insts;
-		a.root = qb.root;
-		a.two_level = (qb.flags >> 1) & 1u;
-		a.rays = qb.rays;
-		a.hits = qb.hits;
-		a.count = qb.count;
-		a.any_hit = qb.flags & 1u;
-		a.status = qb.status;
-		a.postpone = (qb.flags >> 8) & 0xffu;
-		a.variant = (qb.flags >> 16) & 0xffu;
-		a.visit_limit = qb.visit_limit;
+		const TraceArgs a = batch_args(qb);
 		const uint32_t tid = (tile - qb.tile_begin) * kTileRays + threadIdx.x;
 		const bool active = tid < a.count;
 		if (a.any_hit) {
@@ -560,6 +565,107 @@ __global__ void __launch_bounds__(kTileRays, 12) k_trace_queue(const __grid_cons
 	release_slot(slot);
 }
 
+// Index of the batch holding global ray g (last batch with ray_begin <= g).
+__device__ __forceinline__ uint32_t batch_of_ray(const QueueParams &p, uint32_t g) {
+	uint32_t lo = 0, hi = p.n;
+	while (hi - lo > 1) {
+		const uint32_t mid = (lo + hi) >> 1;
+		if (p.b[mid].ray_begin <= g) lo = mid;
+		else hi = mid;
+	}
+	return lo;
+}
+
+// ---------------------------------------------------------------------------
+// Multi-batch queue kernel with warp-level ray fetch: the launch's batches
+// form one index space of p.total_rays rays (batch k at p.b[k].ray_begin),
+// and persistent warps claim rays from it exactly as k_trace_fetch does from
+// one batch -- lanes of a warp may hold rays of different batches (scenes,
+// modes), each running its own batch's ray_step.  Completion flags count
+// finished rays per batch: the lanes finishing in one trip fence their hits,
+// group by batch (__match_any_sync) and one lane per group adds the group's
+// size; the lane that brings a batch to its count raises the batch's flag.
+// Termination as k_trace_fetch: each trip steps a busy lane or claims rays.
+// ---------------------------------------------------------------------------
+
+template <uint32_t CV>
+__global__ void __launch_bounds__(kTraceBlock, 6) k_trace_queue_fetch(const __grid_constant__ QueueParams p) {
+	constexpr bool MM3 = (CV & kVarMinMax3) != 0;
+	uint32_t *slot = g_queue[p.slot];
+	const uint32_t lane = threadIdx.x & 31u;
+	TravState s;
+	TravStack stack;
+	Counts cnt{0, 0, 0, 0};
+	uint32_t rid = kNull;  // ray (index within its batch) this lane traces; kNull: idle
+	uint32_t bi = 0;       // its batch
+	bool drained = false;  // warp-uniform
+	for (;;) {
+		bool fin = false;  // this lane completed a ray in this trip
+		const uint32_t idle = __ballot_sync(0xffffffffu, rid == kNull);
+		const uint32_t nidle = __popc(idle);
+		if (!drained && nidle >= p.refill) {
+			const uint32_t leader = __ffs(idle) - 1;
+			uint32_t base = 0;
+			if (lane == leader) base = atomicAdd(&slot[0], nidle);
+			base = __shfl_sync(0xffffffffu, base, leader);
+			drained = base + nidle >= p.total_rays;
+			if (rid == kNull) {
+				const uint32_t g = base + __popc(idle & ((1u << lane) - 1u));
+				if (g < p.total_rays) {
+					bi = batch_of_ray(p, g);
+					const TraceArgs a = batch_args(p.b[bi]);
+					const uint32_t i = g - p.b[bi].ray_begin;
+					const bool stream = (a.variant & kVarStreamRays) != 0;
+					const int k = ray_begin(a, i, stream, s);
+					if (k == kRayTraverse) {
+						rid = i;
+					} else {
+						if (k == kRayAnswered) ray_write(a, i, s, stream);
+						fin = true;
+					}
+				}
+			}
+		}
+		if (rid != kNull) {
+			const TraceArgs a = batch_args(p.b[bi]);
+			const bool keep = (a.variant & kVarSceneEvictLast) != 0;
+			const uint64_t pol = keep ? evict_last_policy() : 0ull;
+			bool done;
+			if (a.any_hit) {
+				done = a.two_level ? ray_step<true, true, false, MM3>(a, s, stack, keep, pol, cnt)
+						: ray_step<true, false, false, MM3>(a, s, stack, keep, pol, cnt);
+			} else {
+				done = a.two_level ? ray_step<false, true, false, MM3>(a, s, stack, keep, pol, cnt)
+						: ray_step<false, false, false, MM3>(a, s, stack, keep, pol, cnt);
+			}
+			if (done) {
+				ray_write(a, rid, s, (a.variant & kVarStreamRays) != 0);
+				rid = kNull;
+				fin = true;
+			}
+		}
+		if (p.done_flags) {
+			const uint32_t fm = __ballot_sync(0xffffffffu, fin);
+			if (fin) {
+				__threadfence_system();  // this lane's hit before the count that covers it
+				const uint32_t peers = __match_any_sync(fm, bi);
+				__syncwarp(fm);
+				if (lane == __ffs(peers) - 1u) {
+					const QueueBatch &qb = p.b[bi];
+					const uint32_t add = __popc(peers);
+					if (atomicAdd(&p.tiles_done[qb.user_index], add) + add == qb.count) {
+						__threadfence_system();
+						*reinterpret_cast<volatile uint32_t *>(&p.done_flags[qb.user_index]) = 1u;
+					}
+				}
+			}
+		}
+		if (drained && __ballot_sync(0xffffffffu, rid != kNull) == 0u) break;
+	}
+	__syncthreads();
+	release_slot(slot);
+}
+
 lrx_status launch_trace_queue(const QueueParams &p, cudaStream_t st) {
 	if (p.total_tiles == 0) return LRX_OK;
 	static int resident = 0;  // 64-thread blocks resident per GB300 at this kernel's occupancy
@@ -569,6 +675,25 @@ lrx_status launch_trace_queue(const QueueParams &p, cudaStream_t st) {
 		LRX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
 		LRX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_queue<0u>, kTileRays, 0));
 		resident = std::max(1, sms * std::max(1, per_sm));
+	}
+	if (p.fetch) {
+		static int fetch_resident = 0;  // 128-thread blocks resident per device
+		if (fetch_resident == 0) {
+			int dev = 0, sms = 0, per_sm = 0;
+			LRX_CUDA(cudaGetDevice(&dev));
+			LRX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+			LRX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_queue_fetch<0u>, kTraceBlock, 0));
+			fetch_resident = std::max(1, sms * std::max(1, per_sm));
+		}
+		if (p.total_rays == 0 || p.refill < 1 || p.refill > 32) {
+			set_error("queue fetch launch: empty or bad refill");
+			return LRX_ERR_INVALID_ARGUMENT;
+		}
+		const uint32_t grid = (uint32_t)std::min<uint64_t>(((uint64_t)p.total_rays + kTraceBlock - 1) / kTraceBlock,
+				(uint64_t)fetch_resident);
+		k_trace_queue_fetch<0u><<<grid, kTraceBlock, 0, st>>>(p);
+		LRX_CUDA(cudaGetLastError());
+		return LRX_OK;
 	}
 	const uint32_t grid = std::min<uint32_t>(p.total_tiles, (uint32_t)resident);
 	k_trace_queue<0u><<<grid, kTileRays, 0, st>>>(p);

@@ -321,14 +321,22 @@ def test_trace_config_struct_versions(torch_cuda):
         assert L.lrx_scene_set_trace_config(s.handle, ctypes.byref(bad)) == lrx.LRX_ERR_INVALID_ARGUMENT
 
 
-def test_trace_batches_equals_per_batch_traces(torch_cuda):
+@pytest.mark.parametrize("queue", ["fetch", "fetch-refill1", "tiles"])
+def test_trace_batches_equals_per_batch_traces(torch_cuda, queue):
     """lrx_trace_batches over a ragged mix of scenes, modes and sizes
     (including empty, single-ray and tile-boundary batches, and more batches
-    than one queue launch holds) returns exactly what lrx_trace returns."""
+    than one queue launch holds) returns exactly what lrx_trace returns --
+    with warp-level ray fetch (a scene config with the persistent variant,
+    the closest-hit default) and with 64-ray tiles (no such config)."""
     torch = torch_cuda
     flat_desc, _ = W.config1(n_tris=20000, n_rays=1, seed=301)
     inst_desc, _, _ = W.config3(n_rays=1, n_meshes=2, freq=8, n_inst=50, extent=1.0, scale=(0.05, 0.2))
     scenes = [lrx.Scene(flat_desc), lrx.Scene(inst_desc)]
+    for s in scenes:
+        if queue == "tiles":
+            s.set_trace_config(64, 8, 0)
+        elif queue == "fetch-refill1":
+            s.set_trace_config(64, 8, lrx.LRX_VARIANT_PERSISTENT, refill=1)
     rng = np.random.default_rng(302)
     sizes = [0, 1, 63, 64, 65, 1000, 100_000] + rng.integers(1, 3000, 400).tolist()
     st = torch.cuda.current_stream().cuda_stream
