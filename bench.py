@@ -414,6 +414,19 @@ def run_lrx(args):
         for m, c in saved_cfg.items():
             scene.set_trace_config(c["block_size"], c["postpone"], c["variant"], modes=2 if m == lrx.LRX_TRACE_ANY else 1,
                                    refill=c["refill"])
+        # each set as a one-batch lrx_trace_batches call (the queue kernel)
+        alt["queue-1batch"] = {}
+        for name, dr, dh, n, mode in dev:
+            one = [(scene, dr.data_ptr(), dh.data_ptr(), n, mode)]
+            arr1 = lrx.batch_array(one)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            lrx.trace_batches(one, st, arr=arr1)
+            e0.record(stream)
+            for _ in range(5):
+                lrx.trace_batches(one, st, arr=arr1)
+            e1.record(stream)
+            e1.synchronize()
+            alt["queue-1batch"][name] = round(n * 5 / (e0.elapsed_time(e1) / 1e3) / 1e6, 1)
 
     # roofline of the traversal kernel: algorithmic bytes / kernel time
     peak, peak_kind = load_peaks()

@@ -213,9 +213,11 @@ typedef struct lrx_batch {
  * closest-hit default), the batches form one ray index space and persistent
  * warps claim rays from it with ballot/shuffle, refilling idle lanes (a
  * warp's lanes may then hold rays of different batches); otherwise 64-thread
- * blocks claim 64-ray tiles.  Ray sorting is not applied.  Results equal
- * lrx_trace on each batch.  Asynchronous on `stream`; graph-capturable (no
- * allocation, no host synchronisation).
+ * blocks claim 64-ray tiles.  Batches whose scene config has
+ * LRX_VARIANT_SORT_RAYS and at least 32,768 rays are reordered first (one
+ * radix sort per launch).  Results equal lrx_trace on each batch.
+ * Asynchronous on `stream`; graph-capturable (no host synchronisation; the
+ * sort scratch is stream-ordered pool memory).
  * Replaces: a sequence of HardwareIntersectionKernel::EnqueueTraceRayBuffer
  * calls (hardwareintersectiondevice.h:67-68), one per RayBuffer. */
 lrx_status lrx_trace_batches(const lrx_batch *batches, uint32_t batch_count, void *stream);

@@ -830,21 +830,79 @@ lrx_status lrx_trace_batches_ex(const lrx_batch *batches, uint32_t n_batches, vo
 			break;
 		}
 	}
-	p.n = 0;
-	p.total_tiles = 0;
-	p.total_rays = 0;
 	p.fetch = fetch;
 	p.refill = refill;
 	p.tiles_done = d_tile_counters;
 	p.done_flags = d_done_flags;
 	if (d_tile_counters) LRX_CUDA(cudaMemsetAsync(d_tile_counters, 0, sizeof(uint32_t) * n_batches, st));
+	// The batches of one launch are gathered first, then laid out by ray class
+	// (closest/any x flat/two-level) so each class is one contiguous range.
+	struct Entry {
+		uint32_t k, cls;
+		bool sort;  // scene config sorts rays and the batch has >= kSortMinRays
+	};
+	std::vector<Entry> pending;
+	uint64_t pend_tiles = 0, pend_rays = 0, pend_sorted = 0;
+	std::vector<SortBatch> sorted;
 	auto flush = [&]() -> lrx_status {
-		if (p.n == 0) return LRX_OK;
-		p.slot = next_queue_slot();
-		lrx_status rc = launch_trace_queue(p, st);
+		if (pending.empty()) return LRX_OK;
+		std::stable_sort(pending.begin(), pending.end(), [](const Entry &a, const Entry &b) { return a.cls < b.cls; });
 		p.n = 0;
 		p.total_tiles = 0;
 		p.total_rays = 0;
+		p.order = nullptr;
+		sorted.clear();
+		uint32_t sorted_rays = 0;
+		for (uint32_t c = 0; c <= 4; ++c) p.class_batch[c] = (uint32_t)pending.size();
+		for (const Entry &e : pending) {
+			const lrx_batch &b = batches[e.k];
+			lrx_scene *s = b.scene;
+			const lrx_trace_config &cfg = s->tcfg[b.mode == LRX_TRACE_ANY ? 1 : 0];
+			if (p.class_batch[e.cls] == pending.size()) p.class_batch[e.cls] = p.n;
+			QueueBatch &q = p.b[p.n++];
+			q.nodes = s->nodes.as<WideNode>();
+			q.tris = s->tris.as<TriRecord>();
+			q.insts = s->insts.as<InstRecord>();
+			q.rays = b.d_rays;
+			q.hits = b.d_hits;
+			q.status = s->status.as<uint32_t>();
+			q.root = s->root;
+			q.count = b.count;
+			q.tile_begin = p.total_tiles;
+			q.ray_begin = p.total_rays;
+			// runtime-selectable variants only (cache hints); sorting is done before the launch
+			const uint32_t var = cfg.variant & (LRX_VARIANT_SCENE_L2_KEEP | LRX_VARIANT_STREAM_RAYS);
+			q.flags = (b.mode == LRX_TRACE_ANY ? 1u : 0u) | (s->two_level ? 2u : 0u) |
+					((cfg.postpone & 0xffu) << 8) | (var << 16);
+			q.visit_limit = scene_visit_limit(s);
+			q.user_index = e.k;
+			q.order_begin = kNull;
+			if (e.sort) {
+				SortBatch sb;
+				sb.rays = b.d_rays;
+				sb.count = b.count;
+				sb.offset = sorted_rays;
+				for (int c = 0; c < 3; ++c) {
+					sb.lo[c] = s->bounds_lo[c];
+					sb.hi[c] = s->bounds_hi[c];
+				}
+				sb.octant_only = (cfg.variant & kVarSortOctantOnly) != 0;
+				sorted.push_back(sb);
+				q.order_begin = sorted_rays;
+				sorted_rays += b.count;
+			}
+			p.total_tiles += (b.count + kTileRays - 1) / kTileRays;
+			p.total_rays += fetch ? b.count : 0u;
+		}
+		// a class with no batches starts where the next non-empty one does
+		for (int c = 3; c >= 0; --c) p.class_batch[c] = std::min(p.class_batch[c], p.class_batch[c + 1]);
+		p.slot = next_queue_slot();
+		void *scratch = nullptr;
+		lrx_status rc = sort_queue_batches(sorted, sorted_rays, st, &p.order, &scratch);
+		if (rc == LRX_OK) rc = launch_trace_queue(p, st);
+		if (scratch) cudaFreeAsync(scratch, st);  // ordered after the launch that reads it
+		pending.clear();
+		pend_tiles = pend_rays = pend_sorted = 0;
 		return rc;
 	};
 	for (uint32_t k = 0; k < n_batches; ++k) {
@@ -852,31 +910,17 @@ lrx_status lrx_trace_batches_ex(const lrx_batch *batches, uint32_t n_batches, vo
 		if (b.count == 0) continue;
 		lrx_scene *s = b.scene;
 		const uint32_t tiles = (b.count + kTileRays - 1) / kTileRays;
-		if (p.n == kMaxQueueBatches || (uint64_t)p.total_tiles + tiles > 0xffffffffull ||
-				(fetch && (uint64_t)p.total_rays + b.count > kMaxFetchRays)) {
+		const lrx_trace_config &cfg = s->tcfg[b.mode == LRX_TRACE_ANY ? 1 : 0];
+		const bool sort = (cfg.variant & kVarSortRays) && b.count >= kSortMinRays && s->root != kNull;
+		if (pending.size() == kMaxQueueBatches || pend_tiles + tiles > 0xffffffffull ||
+				(fetch && pend_rays + b.count > kMaxFetchRays) || (sort && pend_sorted + b.count > kMaxFetchRays)) {
 			lrx_status rc = flush();
 			if (rc != LRX_OK) return rc;
 		}
-		const lrx_trace_config &cfg = s->tcfg[b.mode == LRX_TRACE_ANY ? 1 : 0];
-		QueueBatch &q = p.b[p.n++];
-		q.nodes = s->nodes.as<WideNode>();
-		q.tris = s->tris.as<TriRecord>();
-		q.insts = s->insts.as<InstRecord>();
-		q.rays = b.d_rays;
-		q.hits = b.d_hits;
-		q.status = s->status.as<uint32_t>();
-		q.root = s->root;
-		q.count = b.count;
-		q.tile_begin = p.total_tiles;
-		q.ray_begin = p.total_rays;
-		// runtime-selectable variants only (cache hints); the queue kernel does not sort
-		const uint32_t var = cfg.variant & (LRX_VARIANT_SCENE_L2_KEEP | LRX_VARIANT_STREAM_RAYS);
-		q.flags = (b.mode == LRX_TRACE_ANY ? 1u : 0u) | (s->two_level ? 2u : 0u) | ((cfg.postpone & 0xffu) << 8) |
-				(var << 16);
-		q.visit_limit = scene_visit_limit(s);
-		q.user_index = k;
-		p.total_tiles += tiles;
-		p.total_rays += fetch ? b.count : 0u;
+		pending.push_back({k, (b.mode == LRX_TRACE_ANY ? 2u : 0u) | (s->two_level ? 1u : 0u), sort});
+		pend_tiles += tiles;
+		pend_rays += b.count;
+		pend_sorted += sort ? b.count : 0u;
 	}
 	return flush();
 }

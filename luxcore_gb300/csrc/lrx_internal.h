@@ -141,6 +141,7 @@ struct QueueBatch {
 	uint32_t flags;        // bit 0 any-hit, bit 1 two-level, bits 8-15 postpone, bits 16-23 variant
 	uint32_t visit_limit;
 	uint32_t user_index;   // the caller's index of this batch (completion flags)
+	uint32_t order_begin;  // sorted batch: its permutation at QueueParams::order + order_begin; else kNull
 };
 constexpr uint32_t kTileRays = 64;
 constexpr uint32_t kMaxQueueBatches = 384;  // keeps the parameter block under 32 KB
@@ -153,6 +154,11 @@ struct QueueParams {
 	uint32_t refill;        // fetch kernel: idle lanes that trigger a warp's claim, 1-32
 	uint32_t *tiles_done;   // per batch progress (tiles, or rays with `fetch`), zeroed before the launch (nullable)
 	uint32_t *done_flags;   // per batch, set to 1 when its last ray is written (nullable, may be host-mapped)
+	const uint32_t *order;  // permutations of the sorted batches, concatenated (nullable)
+	// batches are ordered by ray class (0 closest flat, 1 closest two-level, 2 any flat,
+	// 3 any two-level); class c is batches [class_batch[c], class_batch[c + 1])
+	uint32_t class_batch[5];
+	uint32_t pad2;
 	QueueBatch b[kMaxQueueBatches];
 };
 static_assert(sizeof(QueueParams) <= 32000, "kernel parameter limit");
@@ -167,6 +173,21 @@ lrx_status launch_trace_queue(const QueueParams &p, cudaStream_t stream);
 // Sorts the rays (octant, origin Morton code in [lo, hi]) and traces them in
 // that order; scratch from a stream-ordered pool.  Hits land in caller order.
 lrx_status launch_trace_sorted(const TraceArgs &a, const float lo[3], const float hi[3], cudaStream_t stream);
+
+// One batch of a queue launch to reorder: its rays, count, the scene box and
+// the offset of its permutation in the launch's concatenated order array.
+struct SortBatch {
+	const void *rays;
+	uint32_t count, offset;
+	float lo[3], hi[3];
+	bool octant_only;
+};
+// Computes every listed batch's permutation with one radix sort (batch index
+// above the ray key) into pool scratch; *order gets the concatenated
+// permutations, *scratch what to release (cudaFreeAsync on `stream`) after
+// the launch that reads them.
+lrx_status sort_queue_batches(const std::vector<SortBatch> &batches, uint32_t total, cudaStream_t stream,
+		const uint32_t **order, void **scratch);
 
 // CUDA device a scene was built on.
 int scene_device(const lrx_scene *scene);

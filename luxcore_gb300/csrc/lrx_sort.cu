@@ -11,6 +11,7 @@
 // the device.
 #include <cstdint>
 #include <mutex>
+#include <vector>
 
 #include <cub/device/device_radix_sort.cuh>
 
@@ -77,7 +78,80 @@ __global__ void k_ray_keys(const float4 *__restrict__ rays, uint32_t n, float3 l
 	idx[i] = i;
 }
 
+// Queue-launch keys: batch index j above the 30-bit ray key, so one stable
+// sort leaves each batch's permutation at its own offset.
+__global__ void k_ray_keys_batch(const float4 *__restrict__ rays, uint32_t n, float3 lo, float3 inv_ext,
+		uint64_t j, uint32_t key_mask, uint64_t *__restrict__ keys, uint32_t *__restrict__ idx) {
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	const float4 r0 = __ldcs(rays + 3 * (size_t)i), r1 = __ldcs(rays + 3 * (size_t)i + 1);
+	const uint32_t oct = (__float_as_uint(r0.w) >> 31) | ((__float_as_uint(r1.x) >> 31) << 1) |
+			((__float_as_uint(r1.y) >> 31) << 2);
+	auto q = [](float v, float l, float s) {
+		const float u = (v - l) * s;
+		return u > 0.f ? (u < 511.f ? (uint32_t)u : 511u) : 0u;  // NaN -> 0
+	};
+	const uint32_t m = (spread10(q(r0.x, lo.x, inv_ext.x)) << 2) | (spread10(q(r0.y, lo.y, inv_ext.y)) << 1) |
+			spread10(q(r0.z, lo.z, inv_ext.z));
+	keys[i] = (j << 30) | (((oct << 27) | (m & 0x07ffffffu)) & key_mask);
+	idx[i] = i;
+}
+
+float3 key_scale(const float lo[3], const float hi[3]) {
+	return make_float3(hi[0] > lo[0] ? 512.f / (hi[0] - lo[0]) : 0.f, hi[1] > lo[1] ? 512.f / (hi[1] - lo[1]) : 0.f,
+			hi[2] > lo[2] ? 512.f / (hi[2] - lo[2]) : 0.f);
+}
+
 }  // namespace
+
+lrx_status sort_queue_batches(const std::vector<SortBatch> &batches, uint32_t total, cudaStream_t st,
+		const uint32_t **order, void **scratch) {
+	*order = nullptr;
+	*scratch = nullptr;
+	if (batches.empty() || total == 0) return LRX_OK;
+	int dev = 0;
+	LRX_CUDA(cudaGetDevice(&dev));
+	cudaMemPool_t pool;
+	lrx_status rc = stream_pool(dev, &pool);
+	if (rc != LRX_OK) return rc;
+	int end_bit = 30;
+	while ((1ull << (end_bit - 30)) < batches.size()) ++end_bit;
+	size_t temp_bytes = 0;
+	{
+		cub::DoubleBuffer<uint64_t> dk(nullptr, nullptr);
+		cub::DoubleBuffer<uint32_t> dv(nullptr, nullptr);
+		LRX_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, temp_bytes, dk, dv, (int)total, 0, end_bit, st));
+	}
+	auto round = [](size_t b) { return ((b + 255) / 256) * 256; };
+	const size_t k_arr = round(sizeof(uint64_t) * (size_t)total), v_arr = round(sizeof(uint32_t) * (size_t)total);
+	void *base = nullptr;
+	LRX_CUDA(cudaMallocFromPoolAsync(&base, 2 * k_arr + 2 * v_arr + temp_bytes, pool, st));
+	unsigned char *p = static_cast<unsigned char *>(base);
+	uint64_t *k0 = reinterpret_cast<uint64_t *>(p), *k1 = reinterpret_cast<uint64_t *>(p + k_arr);
+	uint32_t *v0 = reinterpret_cast<uint32_t *>(p + 2 * k_arr), *v1 = reinterpret_cast<uint32_t *>(p + 2 * k_arr + v_arr);
+	void *temp = p + 2 * k_arr + 2 * v_arr;
+	cudaError_t e = cudaSuccess;
+	for (size_t j = 0; j < batches.size() && e == cudaSuccess; ++j) {
+		const SortBatch &b = batches[j];
+		const float3 l = make_float3(b.lo[0], b.lo[1], b.lo[2]);
+		k_ray_keys_batch<<<(b.count + 255) / 256, 256, 0, st>>>(reinterpret_cast<const float4 *>(b.rays), b.count, l,
+				key_scale(b.lo, b.hi), (uint64_t)j, b.octant_only ? 0x38000000u : 0x3fffffffu, k0 + b.offset,
+				v0 + b.offset);
+		e = cudaGetLastError();
+	}
+	if (e == cudaSuccess) {
+		cub::DoubleBuffer<uint64_t> dk(k0, k1);
+		cub::DoubleBuffer<uint32_t> dv(v0, v1);
+		e = cub::DeviceRadixSort::SortPairs(temp, temp_bytes, dk, dv, (int)total, 0, end_bit, st);
+		if (e == cudaSuccess) *order = dv.Current();
+	}
+	if (e != cudaSuccess) {
+		cudaFreeAsync(base, st);
+		return cuda_fail(e, "queue ray sort");
+	}
+	*scratch = base;
+	return LRX_OK;
+}
 
 lrx_status launch_trace_sorted(const TraceArgs &a_in, const float lo[3], const float hi[3], cudaStream_t st) {
 	TraceArgs a = a_in;
@@ -106,8 +180,7 @@ lrx_status launch_trace_sorted(const TraceArgs &a_in, const float lo[3], const f
 	void *temp = p + 4 * arr;
 
 	float3 l = make_float3(lo[0], lo[1], lo[2]);
-	float3 s = make_float3(hi[0] > lo[0] ? 512.f / (hi[0] - lo[0]) : 0.f, hi[1] > lo[1] ? 512.f / (hi[1] - lo[1]) : 0.f,
-			hi[2] > lo[2] ? 512.f / (hi[2] - lo[2]) : 0.f);
+	float3 s = key_scale(lo, hi);
 	k_ray_keys<<<(n + 255) / 256, 256, 0, st>>>(reinterpret_cast<const float4 *>(a.rays), n, l, s, k0, v0);
 	cudaError_t e = cudaGetLastError();
 	if (e == cudaSuccess) {

@@ -409,18 +409,21 @@ k_trace(TraceArgs a) {
 	}
 }
 
-__device__ uint32_t g_queue[kQueueSlots][2];  // (next tile / ray, blocks finished) per slot
+// Per-launch counter slots: words 0-3 claim counters (one per ray class of
+// a queue launch; single-batch kernels use word 0), word 4 the count of
+// blocks that have stopped claiming.
+constexpr int kSlotWords = 8, kSlotFinished = 4;
+__device__ uint32_t g_queue[kQueueSlots][kSlotWords];
 
-// Slot protocol shared by the persistent kernels: a launch owns slot
-// (counter, finished blocks), both zero at entry; every block adds itself to
-// the finished count once it has stopped claiming work, and the last one
-// zeroes the slot for its next user.
+// Slot protocol shared by the persistent kernels: a launch owns a slot, all
+// zero at entry; every block adds itself to the finished count once it has
+// stopped claiming work, and the last one zeroes the slot for its next user.
 __device__ __forceinline__ void release_slot(uint32_t *slot) {
 	if (threadIdx.x == 0) {
 		__threadfence();
-		if (atomicAdd(&slot[1], 1u) == gridDim.x - 1) {  // every block has stopped claiming work
-			slot[0] = 0u;
-			slot[1] = 0u;
+		if (atomicAdd(&slot[kSlotFinished], 1u) == gridDim.x - 1) {  // every block has stopped claiming work
+#pragma unroll
+			for (int w = 0; w < kSlotWords; ++w) slot[w] = 0u;
 			__threadfence();
 		}
 	}
@@ -502,8 +505,9 @@ __global__ void __launch_bounds__(kTraceBlock, 8) k_trace_fetch(TraceArgs a, uin
 // memory), and the loop ends when the tiles run out.
 // ---------------------------------------------------------------------------
 
-__device__ __forceinline__ TraceArgs batch_args(const QueueBatch &qb) {
+__device__ __forceinline__ TraceArgs batch_args(const QueueParams &p, const QueueBatch &qb) {
 	TraceArgs a{};
+	a.order = qb.order_begin != kNull ? p.order + qb.order_begin : nullptr;
 	a.nodes = qb.nodes;
 	a.tris = qb.tris;
 	a.insts = qb.insts;
@@ -538,7 +542,7 @@ __global__ void __launch_bounds__(kTileRays, 12) k_trace_queue(const __grid_cons
 			else hi = mid;
 		}
 		const QueueBatch &qb = p.b[lo];
-		const TraceArgs a = batch_args(qb);
+		const TraceArgs a = batch_args(p, qb);
 		const uint32_t tid = (tile - qb.tile_begin) * kTileRays + threadIdx.x;
 		const bool active = tid < a.count;
 		if (a.any_hit) {
@@ -565,9 +569,28 @@ __global__ void __launch_bounds__(kTileRays, 12) k_trace_queue(const __grid_cons
 	release_slot(slot);
 }
 
-// Index of the batch holding global ray g (last batch with ray_begin <= g).
-__device__ __forceinline__ uint32_t batch_of_ray(const QueueParams &p, uint32_t g) {
-	uint32_t lo = 0, hi = p.n;
+// Adds n finished rays to batch bi's progress counter; the add that brings
+// the batch to its count raises the batch's completion flag.  The hits the
+// count covers were ordered before this thread's fence by a warp sync.
+__device__ __forceinline__ void add_done(const QueueParams &p, uint32_t bi, uint32_t n) {
+	const QueueBatch &qb = p.b[bi];
+	__threadfence();
+	if (atomicAdd(&p.tiles_done[qb.user_index], n) + n == qb.count) {
+		__threadfence_system();
+		*reinterpret_cast<volatile uint32_t *>(&p.done_flags[qb.user_index]) = 1u;
+	}
+}
+
+// Warp-wide (every lane): orders all lanes' hit writes before lane 0 adds
+// the warp's pending count of finished rays.
+__device__ __forceinline__ void flush_done(const QueueParams &p, uint32_t bi, uint32_t n, uint32_t lane) {
+	__syncwarp();
+	if (n && lane == 0) add_done(p, bi, n);
+}
+
+// Index of the batch holding global ray g among batches [lo, hi) (the last
+// one with ray_begin <= g).
+__device__ __forceinline__ uint32_t batch_of_ray(const QueueParams &p, uint32_t g, uint32_t lo, uint32_t hi) {
 	while (hi - lo > 1) {
 		const uint32_t mid = (lo + hi) >> 1;
 		if (p.b[mid].ray_begin <= g) lo = mid;
@@ -576,29 +599,30 @@ __device__ __forceinline__ uint32_t batch_of_ray(const QueueParams &p, uint32_t 
 	return lo;
 }
 
-// ---------------------------------------------------------------------------
-// Multi-batch queue kernel with warp-level ray fetch: the launch's batches
-// form one index space of p.total_rays rays (batch k at p.b[k].ray_begin),
-// and persistent warps claim rays from it exactly as k_trace_fetch does from
-// one batch -- lanes of a warp may hold rays of different batches (scenes,
-// modes), each running its own batch's ray_step.  Completion flags count
-// finished rays per batch: the lanes finishing in one trip fence their hits,
-// group by batch (__match_any_sync) and one lane per group adds the group's
-// size; the lane that brings a batch to its count raises the batch's flag.
-// Termination as k_trace_fetch: each trip steps a busy lane or claims rays.
-// ---------------------------------------------------------------------------
-
-template <uint32_t CV>
-__global__ void __launch_bounds__(kTraceBlock, 6) k_trace_queue_fetch(const __grid_constant__ QueueParams p) {
-	constexpr bool MM3 = (CV & kVarMinMax3) != 0;
-	uint32_t *slot = g_queue[p.slot];
-	const uint32_t lane = threadIdx.x & 31u;
-	TravState s;
-	TravStack stack;
+// One ray class of a queue launch -- batches [class_batch[c], class_batch[c+1]),
+// all of one mode and one scene kind -- drained by persistent warps with
+// warp-level ray fetch from the class's own counter, exactly as k_trace_fetch
+// drains one batch; lanes of a warp may hold rays of different batches
+// (scenes) of the class.  Completion flags count finished rays per batch: a
+// warp keeps a pending count while its finishing lanes stay in one batch and
+// adds it to the batch's counter (after a warp sync and a fence that order
+// the hits before it) every 16 trips, when the batch changes and at the end;
+// a trip whose finishing lanes span batches adds per batch group
+// (__match_any_sync).  The add that brings a batch to its count raises the
+// batch's flag.  Termination as k_trace_fetch: each trip steps a busy lane or
+// claims rays, and the counter only grows.
+template <bool ANY, bool TWO_LEVEL, bool MM3, bool FLAGS>
+__device__ __forceinline__ void drain_class(const QueueParams &p, uint32_t c, uint32_t *counter, uint32_t lane,
+		TravState &s, TravStack &stack) {
+	const uint32_t cb = p.class_batch[c], ce = p.class_batch[c + 1];
+	if (cb == ce) return;
+	const uint32_t r0 = p.b[cb].ray_begin;
+	const uint32_t nrays = (ce == p.n ? p.total_rays : p.b[ce].ray_begin) - r0;
 	Counts cnt{0, 0, 0, 0};
 	uint32_t rid = kNull;  // ray (index within its batch) this lane traces; kNull: idle
-	uint32_t bi = 0;       // its batch
+	uint32_t bi = cb;      // its batch
 	bool drained = false;  // warp-uniform
+	uint32_t pend_bi = 0, pend_n = 0, trip = 0;  // warp-uniform: finished rays not yet counted
 	for (;;) {
 		bool fin = false;  // this lane completed a ray in this trip
 		const uint32_t idle = __ballot_sync(0xffffffffu, rid == kNull);
@@ -606,15 +630,16 @@ __global__ void __launch_bounds__(kTraceBlock, 6) k_trace_queue_fetch(const __gr
 		if (!drained && nidle >= p.refill) {
 			const uint32_t leader = __ffs(idle) - 1;
 			uint32_t base = 0;
-			if (lane == leader) base = atomicAdd(&slot[0], nidle);
+			if (lane == leader) base = atomicAdd(counter, nidle);
 			base = __shfl_sync(0xffffffffu, base, leader);
-			drained = base + nidle >= p.total_rays;
+			drained = base + nidle >= nrays;
 			if (rid == kNull) {
 				const uint32_t g = base + __popc(idle & ((1u << lane) - 1u));
-				if (g < p.total_rays) {
-					bi = batch_of_ray(p, g);
-					const TraceArgs a = batch_args(p.b[bi]);
-					const uint32_t i = g - p.b[bi].ray_begin;
+				if (g < nrays) {
+					bi = batch_of_ray(p, r0 + g, cb, ce);
+					const TraceArgs a = batch_args(p, p.b[bi]);
+					const uint32_t local = r0 + g - p.b[bi].ray_begin;
+					const uint32_t i = a.order ? a.order[local] : local;  // the ray (sorted batches: permuted)
 					const bool stream = (a.variant & kVarStreamRays) != 0;
 					const int k = ray_begin(a, i, stream, s);
 					if (k == kRayTraverse) {
@@ -627,41 +652,66 @@ __global__ void __launch_bounds__(kTraceBlock, 6) k_trace_queue_fetch(const __gr
 			}
 		}
 		if (rid != kNull) {
-			const TraceArgs a = batch_args(p.b[bi]);
+			const TraceArgs a = batch_args(p, p.b[bi]);
 			const bool keep = (a.variant & kVarSceneEvictLast) != 0;
 			const uint64_t pol = keep ? evict_last_policy() : 0ull;
-			bool done;
-			if (a.any_hit) {
-				done = a.two_level ? ray_step<true, true, false, MM3>(a, s, stack, keep, pol, cnt)
-						: ray_step<true, false, false, MM3>(a, s, stack, keep, pol, cnt);
-			} else {
-				done = a.two_level ? ray_step<false, true, false, MM3>(a, s, stack, keep, pol, cnt)
-						: ray_step<false, false, false, MM3>(a, s, stack, keep, pol, cnt);
-			}
-			if (done) {
+			if (ray_step<ANY, TWO_LEVEL, false, MM3>(a, s, stack, keep, pol, cnt)) {
 				ray_write(a, rid, s, (a.variant & kVarStreamRays) != 0);
 				rid = kNull;
 				fin = true;
 			}
 		}
-		if (p.done_flags) {
+		if (FLAGS) {
 			const uint32_t fm = __ballot_sync(0xffffffffu, fin);
-			if (fin) {
-				__threadfence_system();  // this lane's hit before the count that covers it
-				const uint32_t peers = __match_any_sync(fm, bi);
-				__syncwarp(fm);
-				if (lane == __ffs(peers) - 1u) {
-					const QueueBatch &qb = p.b[bi];
-					const uint32_t add = __popc(peers);
-					if (atomicAdd(&p.tiles_done[qb.user_index], add) + add == qb.count) {
-						__threadfence_system();
-						*reinterpret_cast<volatile uint32_t *>(&p.done_flags[qb.user_index]) = 1u;
+			bool flush = pend_n != 0 && ((++trip & 15u) == 0u);
+			if (fm) {
+				const uint32_t b0 = __shfl_sync(0xffffffffu, bi, __ffs(fm) - 1);
+				const bool one = __all_sync(0xffffffffu, !fin || bi == b0);
+				if (one && (pend_n == 0 || pend_bi == b0)) {
+					pend_bi = b0;
+					pend_n += __popc(fm);
+				} else {
+					flush_done(p, pend_bi, pend_n, lane);  // what was pending, then this trip's groups
+					pend_n = 0;
+					flush = false;
+					if (one) {
+						pend_bi = b0;
+						pend_n = __popc(fm);
+					} else if (fin) {
+						const uint32_t peers = __match_any_sync(fm, bi);
+						if (lane == __ffs(peers) - 1u) add_done(p, bi, __popc(peers));
 					}
 				}
 			}
+			const bool leaving = drained && __ballot_sync(0xffffffffu, rid != kNull) == 0u;
+			if (flush || (leaving && pend_n)) {
+				flush_done(p, pend_bi, pend_n, lane);
+				pend_n = 0;
+			}
+			if (leaving) break;
+			continue;
 		}
 		if (drained && __ballot_sync(0xffffffffu, rid != kNull) == 0u) break;
 	}
+}
+
+// Multi-batch queue kernel with warp-level ray fetch: every warp drains the
+// launch's four ray classes in turn (closest flat, closest two-level, any
+// flat, any two-level), each with a loop specialised for its class; warps
+// that find a class drained move on while others finish its last rays.
+// FLAGS: the launch keeps completion flags (a separate build, so launches
+// without them carry none of that state).
+template <uint32_t CV, bool FLAGS>
+__global__ void __launch_bounds__(kTraceBlock, 7) k_trace_queue_fetch(const __grid_constant__ QueueParams p) {
+	constexpr bool MM3 = (CV & kVarMinMax3) != 0;
+	uint32_t *slot = g_queue[p.slot];
+	const uint32_t lane = threadIdx.x & 31u;
+	TravState s;
+	TravStack stack;
+	drain_class<false, false, MM3, FLAGS>(p, 0, &slot[0], lane, s, stack);
+	drain_class<false, true, MM3, FLAGS>(p, 1, &slot[1], lane, s, stack);
+	drain_class<true, false, MM3, FLAGS>(p, 2, &slot[2], lane, s, stack);
+	drain_class<true, true, MM3, FLAGS>(p, 3, &slot[3], lane, s, stack);
 	__syncthreads();
 	release_slot(slot);
 }
@@ -677,21 +727,26 @@ lrx_status launch_trace_queue(const QueueParams &p, cudaStream_t st) {
 		resident = std::max(1, sms * std::max(1, per_sm));
 	}
 	if (p.fetch) {
-		static int fetch_resident = 0;  // 128-thread blocks resident per device
-		if (fetch_resident == 0) {
+		static int fetch_resident[2] = {0, 0};  // 128-thread blocks resident per device, without / with flags
+		const int fl = p.done_flags ? 1 : 0;
+		if (fetch_resident[fl] == 0) {
 			int dev = 0, sms = 0, per_sm = 0;
 			LRX_CUDA(cudaGetDevice(&dev));
 			LRX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-			LRX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_queue_fetch<0u>, kTraceBlock, 0));
-			fetch_resident = std::max(1, sms * std::max(1, per_sm));
+			if (fl)
+				LRX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_queue_fetch<0u, true>, kTraceBlock, 0));
+			else
+				LRX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_queue_fetch<0u, false>, kTraceBlock, 0));
+			fetch_resident[fl] = std::max(1, sms * std::max(1, per_sm));
 		}
 		if (p.total_rays == 0 || p.refill < 1 || p.refill > 32) {
 			set_error("queue fetch launch: empty or bad refill");
 			return LRX_ERR_INVALID_ARGUMENT;
 		}
 		const uint32_t grid = (uint32_t)std::min<uint64_t>(((uint64_t)p.total_rays + kTraceBlock - 1) / kTraceBlock,
-				(uint64_t)fetch_resident);
-		k_trace_queue_fetch<0u><<<grid, kTraceBlock, 0, st>>>(p);
+				(uint64_t)fetch_resident[fl]);
+		if (fl) k_trace_queue_fetch<0u, true><<<grid, kTraceBlock, 0, st>>>(p);
+		else k_trace_queue_fetch<0u, false><<<grid, kTraceBlock, 0, st>>>(p);
 		LRX_CUDA(cudaGetLastError());
 		return LRX_OK;
 	}

@@ -321,7 +321,7 @@ def test_trace_config_struct_versions(torch_cuda):
         assert L.lrx_scene_set_trace_config(s.handle, ctypes.byref(bad)) == lrx.LRX_ERR_INVALID_ARGUMENT
 
 
-@pytest.mark.parametrize("queue", ["fetch", "fetch-refill1", "tiles"])
+@pytest.mark.parametrize("queue", ["fetch", "fetch-refill1", "tiles", "fetch-sorted", "tiles-sorted"])
 def test_trace_batches_equals_per_batch_traces(torch_cuda, queue):
     """lrx_trace_batches over a ragged mix of scenes, modes and sizes
     (including empty, single-ray and tile-boundary batches, and more batches
@@ -337,8 +337,12 @@ def test_trace_batches_equals_per_batch_traces(torch_cuda, queue):
             s.set_trace_config(64, 8, 0)
         elif queue == "fetch-refill1":
             s.set_trace_config(64, 8, lrx.LRX_VARIANT_PERSISTENT, refill=1)
+        elif queue == "fetch-sorted":  # batches >= 32,768 rays are reordered inside the queue launch
+            s.set_trace_config(64, 8, lrx.LRX_VARIANT_PERSISTENT | lrx.LRX_VARIANT_SORT_RAYS, refill=8)
+        elif queue == "tiles-sorted":
+            s.set_trace_config(64, 8, lrx.LRX_VARIANT_SORT_RAYS)
     rng = np.random.default_rng(302)
-    sizes = [0, 1, 63, 64, 65, 1000, 100_000] + rng.integers(1, 3000, 400).tolist()
+    sizes = [0, 1, 63, 64, 65, 1000, 100_000, 40_000, 32_768] + rng.integers(1, 3000, 400).tolist()
     st = torch.cuda.current_stream().cuda_stream
     items, refs = [], []
     for k, n in enumerate(sizes):
