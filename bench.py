@@ -302,8 +302,9 @@ def run_lrx(args):
 
     scene_desc = make_scene()
     t0 = time.perf_counter()
+    build_kw = {} if args.treelet_passes is None else {"treelet_passes": args.treelet_passes}
     with torch.cuda.stream(stream):
-        scene = lrx.Scene(scene_desc, stream=st)
+        scene = lrx.Scene(scene_desc, stream=st, **build_kw)
     build_s = time.perf_counter() - t0
     if args.block_size is not None or args.postpone is not None or args.variant is not None:
         scene.set_trace_config(args.block_size or 64, 8 if args.postpone is None else args.postpone,
@@ -414,6 +415,34 @@ def run_lrx(args):
         for m, c in saved_cfg.items():
             scene.set_trace_config(c["block_size"], c["postpone"], c["variant"], modes=2 if m == lrx.LRX_TRACE_ANY else 1,
                                    refill=c["refill"])
+    builds = {}
+    if args.build_sweep:
+        # the same sets on trees built with 0-3 treelet passes (default launch configs)
+        for passes in (0, 1, 2, 3):
+            with torch.cuda.stream(stream):
+                sc = lrx.Scene(scene_desc, stream=st, treelet_passes=passes)
+            inf = sc.info()
+            row = {"build_ms": round(inf["build_ms"], 2), "wide_nodes": inf["node_count"], "depth": inf["max_depth"]}
+            for name, dr, dh, n, mode in dev:
+                cb = torch.zeros(4, dtype=torch.int64, device=f"cuda:{local}")
+                torch.cuda.synchronize()
+                sc.trace_counted(dr.data_ptr(), dh.data_ptr(), n, mode, cb.data_ptr(), st)
+                stream.synchronize()
+                nn, nt, _ni, _nr = cb.cpu().tolist()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                sc.trace(dr.data_ptr(), dh.data_ptr(), n, mode, st)
+                e0.record(stream)
+                for _ in range(5):
+                    sc.trace(dr.data_ptr(), dh.data_ptr(), n, mode, st)
+                e1.record(stream)
+                e1.synchronize()
+                row[name] = {"Mrays": round(n * 5 / (e0.elapsed_time(e1) / 1e3) / 1e6, 1),
+                             "nodes_per_ray": round(nn / n, 2), "tris_per_ray": round(nt / n, 2)}
+            sc.close()
+            builds[f"treelet{passes}"] = row
+        log(f"[bench] {time.strftime('%H:%M:%S')} build sweep done")
+
+    if args.sweep:
         # each set as a one-batch lrx_trace_batches call (the queue kernel)
         alt["queue-1batch"] = {}
         for name, dr, dh, n, mode in dev:
@@ -489,6 +518,8 @@ def run_lrx(args):
                 "trace_config": {"closest": scene.trace_config(lrx.LRX_TRACE_CLOSEST),
                                  "any": scene.trace_config(lrx.LRX_TRACE_ANY)},
                 "config_sweep_Mrays": alt,
+                "build_sweep": builds,
+                "treelet_passes": args.treelet_passes,
             },
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": traffic,
@@ -814,6 +845,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (lrx_trace_host) leg")
     ap.add_argument("--sweep", action="store_true", help="also time other launch configurations")
+    ap.add_argument("--treelet-passes", type=int, default=None, help="BVH treelet passes (default: the library's)")
+    ap.add_argument("--build-sweep", action="store_true",
+                    help="also build with 0-3 treelet passes and time each tree (outside the timed region)")
     ap.add_argument("--block-size", type=int, default=None, help="override the per-mode defaults")
     ap.add_argument("--postpone", type=int, default=None)
     ap.add_argument("--variant", type=int, default=None, help="LRX_VARIANT_* bits")

@@ -418,7 +418,7 @@ lrx_status lrx_scene_create(const lrx_mesh_desc *meshes, uint32_t mesh_count, co
 		s->mesh_count = mesh_count;
 		s->opts.struct_size = sizeof(lrx_build_opts);
 		s->opts.leaf_max = 3;
-		s->opts.treelet_passes = 0;
+		s->opts.treelet_passes = 2;
 		if (opts && opts->struct_size >= sizeof(lrx_build_opts)) {
 			if (opts->leaf_max) s->opts.leaf_max = std::min(3u, opts->leaf_max);
 			s->opts.treelet_passes = opts->treelet_passes;

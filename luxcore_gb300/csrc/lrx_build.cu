@@ -110,9 +110,14 @@ __device__ __forceinline__ bool delta_less(const uint64_t *__restrict__ keys, ui
 	return (a ^ (a + 1)) < (b ^ (b + 1));
 }
 
+// Per internal node k of the binary tree: children bchild[2k], bchild[2k+1]
+// (kLeafFlag | leaf position in sorted order, or an internal node), box
+// bn_lo/bn_hi[k], bmeta[k] = (leaf count, parent; kNull for the root); per
+// leaf position i: lparent[i].  The treelet pass rewrites topology, boxes
+// and counts in place, so subtrees need not stay contiguous in sorted order.
 __global__ void k_hierarchy(uint32_t n, const uint64_t *__restrict__ keys, const uint32_t *__restrict__ sorted,
 		const float4 *__restrict__ plo, const float4 *__restrict__ phi, uint32_t *bchild, float4 *bn_lo,
-		float4 *bn_hi, uint2 *brange, uint32_t *other, uint32_t *counters) {
+		float4 *bn_hi, uint2 *bmeta, uint32_t *lparent, uint32_t *other, uint32_t *counters) {
 	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
 	if (i >= n) return;
 	const uint32_t p = sorted[i];
@@ -134,6 +139,8 @@ __global__ void k_hierarchy(uint32_t n, const uint64_t *__restrict__ keys, const
 		const bool left_child = (l == 0) || (r != n - 1 && delta_less(keys, r, l - 1));
 		const uint32_t parent = left_child ? r : l - 1;
 		bchild[2 * parent + (left_child ? 0 : 1)] = cur;
+		if (cur & kLeafFlag) lparent[cur & ~kLeafFlag] = parent;
+		else reinterpret_cast<uint32_t *>(bmeta)[2 * cur + 1] = parent;
 		__threadfence();
 		const uint32_t prev = atomicExch(&other[parent], left_child ? l : r);
 		if (prev == kNull) return;  // the sibling finishes this node
@@ -154,7 +161,7 @@ __global__ void k_hierarchy(uint32_t n, const uint64_t *__restrict__ keys, const
 		hi = make_float4(fmaxf(hi.x, shi.x), fmaxf(hi.y, shi.y), fmaxf(hi.z, shi.z), 0.f);
 		__stcg(&bn_lo[parent], lo);
 		__stcg(&bn_hi[parent], hi);
-		__stcg(&brange[parent], make_uint2(l, r));
+		__stcg(reinterpret_cast<uint32_t *>(bmeta) + 2 * parent, r - l + 1);
 		cur = parent;
 		if (l == 0 && r == n - 1) {
 			counters[C_ROOT] = parent;
@@ -163,6 +170,182 @@ __global__ void k_hierarchy(uint32_t n, const uint64_t *__restrict__ keys, const
 			box[3] = hi.x; box[4] = hi.y; box[5] = hi.z;
 			return;
 		}
+	}
+}
+
+// ---------------------------------------------------------------------------
+// Treelet restructuring (after Karras and Aila 2013): a bottom-up sweep in
+// which the second thread to reach a node owns its whole (finished) subtree.
+// At a node with at least `min_prims` primitives it grows a treelet of up to
+// 7 leaves -- repeatedly splitting the treelet leaf of largest area -- finds
+// the topology of least SAH cost over those leaves by dynamic programming
+// over the 127 leaf subsets, and rewrites the treelet's internal nodes in
+// place (same node indices, the treelet root keeps its position).  Costs:
+// internal node 1.2 x area, leaf-sized subtree (<= leaf_max primitives,
+// which the collapse turns into one leaf slot) 1.0 x area x primitives.
+// ---------------------------------------------------------------------------
+
+constexpr float kSahNode = 1.2f, kSahTri = 1.0f;
+constexpr int kTreeletLeaves = 7;
+
+__device__ __forceinline__ float box_area(float3 lo, float3 hi) {
+	const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
+	return dx * dy + dx * dz + dy * dz;
+}
+
+struct TreeletLeaf {
+	uint32_t ref, count;
+	float3 lo, hi;
+	float cost;
+};
+
+__device__ __forceinline__ void treelet_leaf(uint32_t ref, const uint32_t *__restrict__ sorted,
+		const float4 *__restrict__ plo, const float4 *__restrict__ phi, const float4 *bn_lo, const float4 *bn_hi,
+		const uint2 *bmeta, const float *cost, TreeletLeaf &t) {
+	t.ref = ref;
+	float4 a, c;
+	if (ref & kLeafFlag) {
+		const uint32_t p = sorted[ref & ~kLeafFlag];
+		a = plo[p];
+		c = phi[p];
+		t.count = 1;
+	} else {
+		a = __ldcg(&bn_lo[ref]);
+		c = __ldcg(&bn_hi[ref]);
+		t.count = __ldcg(reinterpret_cast<const uint32_t *>(bmeta) + 2 * ref);
+	}
+	t.lo = make_float3(a.x, a.y, a.z);
+	t.hi = make_float3(c.x, c.y, c.z);
+	t.cost = (ref & kLeafFlag) ? kSahTri * box_area(t.lo, t.hi) : __ldcg(&cost[ref]);
+}
+
+__device__ __forceinline__ float subtree_cost(float area, float child_costs, uint32_t count, uint32_t leaf_max) {
+	const float c = kSahNode * area + child_costs;
+	return count <= leaf_max ? fminf(c, kSahTri * area * (float)count) : c;
+}
+
+__global__ void __launch_bounds__(128) k_treelet(uint32_t n, const uint32_t *__restrict__ sorted,
+		const float4 *__restrict__ plo, const float4 *__restrict__ phi, uint32_t *bchild, float4 *bn_lo,
+		float4 *bn_hi, uint2 *bmeta, uint32_t *lparent, float *cost, uint32_t *visits, uint32_t leaf_max,
+		uint32_t min_prims) {
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	uint32_t *meta = reinterpret_cast<uint32_t *>(bmeta);  // [2k] leaf count, [2k + 1] parent
+	uint32_t node = __ldcg(&lparent[i]);
+	// each step moves to the parent, so the climb ends within n steps
+	for (uint32_t step = 0; step < n && node != kNull; ++step) {
+		__threadfence();
+		if (atomicAdd(&visits[node], 1u) == 0u) return;  // the sibling subtree's thread continues
+		__threadfence();
+		const uint32_t count = __ldcg(&meta[2 * node]);
+		TreeletLeaf L[kTreeletLeaves];
+		treelet_leaf(__ldcg(&bchild[2 * node]), sorted, plo, phi, bn_lo, bn_hi, bmeta, cost, L[0]);
+		treelet_leaf(__ldcg(&bchild[2 * node + 1]), sorted, plo, phi, bn_lo, bn_hi, bmeta, cost, L[1]);
+		const float4 nlo4 = __ldcg(&bn_lo[node]), nhi4 = __ldcg(&bn_hi[node]);
+		const float area = box_area(make_float3(nlo4.x, nlo4.y, nlo4.z), make_float3(nhi4.x, nhi4.y, nhi4.z));
+		const float current = subtree_cost(area, L[0].cost + L[1].cost, count, leaf_max);
+		float best_cost = current;
+		if (count >= min_prims) {
+			uint32_t inner[kTreeletLeaves - 1];
+			int nl = 2, ni = 1;
+			inner[0] = node;
+			while (nl < kTreeletLeaves) {  // split the largest-area internal leaf
+				int best = -1;
+				float ba = -1.f;
+				for (int k = 0; k < nl; ++k) {
+					if (L[k].ref & kLeafFlag) continue;
+					const float a = box_area(L[k].lo, L[k].hi);
+					if (a > ba) {
+						ba = a;
+						best = k;
+					}
+				}
+				if (best < 0) break;
+				const uint32_t r = L[best].ref;
+				inner[ni++] = r;
+				treelet_leaf(__ldcg(&bchild[2 * r]), sorted, plo, phi, bn_lo, bn_hi, bmeta, cost, L[best]);
+				treelet_leaf(__ldcg(&bchild[2 * r + 1]), sorted, plo, phi, bn_lo, bn_hi, bmeta, cost, L[nl++]);
+			}
+			if (nl >= 3) {
+				float copt[1 << kTreeletLeaves];
+				uint8_t part[1 << kTreeletLeaves];
+				const uint32_t full = (1u << nl) - 1u;
+				for (uint32_t S = 1; S <= full; ++S) {
+					if ((S & (S - 1u)) == 0u) {
+						copt[S] = L[__ffs(S) - 1].cost;
+						part[S] = 0;
+						continue;
+					}
+					float3 lo = make_float3(INFINITY, INFINITY, INFINITY), hi = make_float3(-INFINITY, -INFINITY, -INFINITY);
+					uint32_t c = 0;
+					for (int k = 0; k < nl; ++k) {
+						if (!((S >> k) & 1u)) continue;
+						lo = make_float3(fminf(lo.x, L[k].lo.x), fminf(lo.y, L[k].lo.y), fminf(lo.z, L[k].lo.z));
+						hi = make_float3(fmaxf(hi.x, L[k].hi.x), fmaxf(hi.y, L[k].hi.y), fmaxf(hi.z, L[k].hi.z));
+						c += L[k].count;
+					}
+					// two-way splits of S; the part holding S's lowest leaf enumerates each once
+					const uint32_t low = S & (0u - S), rest = S ^ low;
+					float bc = INFINITY;
+					uint32_t bp = low;
+					for (uint32_t sub = rest;; sub = (sub - 1u) & rest) {
+						const uint32_t P = sub | low;
+						if (P != S) {
+							const float cc = copt[P] + copt[S ^ P];
+							if (cc < bc) {
+								bc = cc;
+								bp = P;
+							}
+						}
+						if (sub == 0u) break;
+					}
+					copt[S] = subtree_cost(box_area(lo, hi), bc, c, leaf_max);
+					part[S] = (uint8_t)bp;
+				}
+				if (copt[full] < current * 0.9999f) {
+					best_cost = copt[full];
+					// rewrite: subsets of the optimal split tree onto the treelet's internal nodes
+					uint32_t st_set[kTreeletLeaves], st_node[kTreeletLeaves];
+					int sp = 0, next = 1;
+					st_set[sp] = full;
+					st_node[sp++] = node;
+					while (sp > 0) {
+						--sp;
+						const uint32_t S = st_set[sp], idx = st_node[sp];
+						const uint32_t halves[2] = {part[S], S ^ part[S]};
+						for (int side = 0; side < 2; ++side) {
+							const uint32_t sub = halves[side];
+							uint32_t ref;
+							if ((sub & (sub - 1u)) == 0u) {
+								ref = L[__ffs(sub) - 1].ref;
+								if (ref & kLeafFlag) __stcg(&lparent[ref & ~kLeafFlag], idx);
+								else __stcg(&meta[2 * ref + 1], idx);
+							} else {
+								ref = inner[next++];
+								__stcg(&meta[2 * ref + 1], idx);
+								st_set[sp] = sub;
+								st_node[sp++] = ref;
+							}
+							__stcg(&bchild[2 * idx + side], ref);
+						}
+						float3 lo = make_float3(INFINITY, INFINITY, INFINITY), hi = make_float3(-INFINITY, -INFINITY, -INFINITY);
+						uint32_t c = 0;
+						for (int k = 0; k < nl; ++k) {
+							if (!((S >> k) & 1u)) continue;
+							lo = make_float3(fminf(lo.x, L[k].lo.x), fminf(lo.y, L[k].lo.y), fminf(lo.z, L[k].lo.z));
+							hi = make_float3(fmaxf(hi.x, L[k].hi.x), fmaxf(hi.y, L[k].hi.y), fmaxf(hi.z, L[k].hi.z));
+							c += L[k].count;
+						}
+						__stcg(&bn_lo[idx], make_float4(lo.x, lo.y, lo.z, 0.f));
+						__stcg(&bn_hi[idx], make_float4(hi.x, hi.y, hi.z, 0.f));
+						__stcg(&meta[2 * idx], c);
+						__stcg(&cost[idx], copt[S]);
+					}
+				}
+			}
+		}
+		__stcg(&cost[node], best_cost);
+		node = __ldcg(&meta[2 * node + 1]);
 	}
 }
 
@@ -178,11 +361,6 @@ __device__ __forceinline__ uint32_t quant_exponent(float ext) {
 	if (e < 1) e = 1;
 	while (e < 253 && __fmul_ru(ext, __uint_as_float((uint32_t)(254 - e) << 23)) > 255.f) ++e;
 	return (uint32_t)e;
-}
-
-__device__ __forceinline__ float box_area(float3 lo, float3 hi) {
-	const float dx = hi.x - lo.x, dy = hi.y - lo.y, dz = hi.z - lo.z;
-	return dx * dy + dx * dz + dy * dz;
 }
 
 struct ChildBox {
@@ -207,7 +385,7 @@ __device__ __forceinline__ void load_ref_box(uint32_t ref, const uint32_t *__res
 
 __global__ void __launch_bounds__(128) k_collapse(const uint2 *__restrict__ items, const uint32_t *n_items_ptr,
 		uint2 *__restrict__ out_items, uint32_t *n_out, const uint32_t *__restrict__ bchild,
-		const float4 *__restrict__ bn_lo, const float4 *__restrict__ bn_hi, const uint2 *__restrict__ brange,
+		const float4 *__restrict__ bn_lo, const float4 *__restrict__ bn_hi, const uint2 *__restrict__ bmeta,
 		const uint32_t *__restrict__ sorted, const float4 *__restrict__ plo, const float4 *__restrict__ phi,
 		uint32_t leaf_max, WideNode *__restrict__ wnodes, uint32_t *__restrict__ prim_order, uint32_t *counters,
 		uint32_t cap) {
@@ -249,19 +427,12 @@ __global__ void __launch_bounds__(128) k_collapse(const uint2 *__restrict__ item
 			load_ref_box(cref[cnt], sorted, plo, phi, bn_lo, bn_hi, cb[cnt]);
 			++cnt;
 		}
-		// Child ranges and node bounds
-		uint32_t cfirst[8], ccount[8];
+		// Child primitive counts and node bounds
+		uint32_t ccount[8];
 		float3 nlo = cb[0].lo, nhi = cb[0].hi;
 		uint32_t n_int = 0, n_tri = 0;
 		for (int k = 0; k < cnt; ++k) {
-			if (cref[k] & kLeafFlag) {
-				cfirst[k] = cref[k] & ~kLeafFlag;
-				ccount[k] = 1;
-			} else {
-				const uint2 rg = brange[cref[k]];
-				cfirst[k] = rg.x;
-				ccount[k] = rg.y - rg.x + 1;
-			}
+			ccount[k] = (cref[k] & kLeafFlag) ? 1u : bmeta[cref[k]].x;
 			if (ccount[k] > leaf_max) ++n_int;
 			else n_tri += ccount[k];
 			nlo = make_float3(fminf(nlo.x, cb[k].lo.x), fminf(nlo.y, cb[k].lo.y), fminf(nlo.z, cb[k].lo.z));
@@ -348,8 +519,19 @@ __global__ void __launch_bounds__(128) k_collapse(const uint2 *__restrict__ item
 			} else {
 				const uint32_t m = (((1u << ccount[k]) - 1u) << 5) | tri_off;
 				meta[wsel] |= m << sh;
-				for (uint32_t j = 0; j < ccount[k]; ++j)
-					prim_order[tri_base + tri_off + j] = sorted[cfirst[k] + j];
+				// the subtree's (<= leaf_max <= 3) primitives, by a walk of its binary nodes
+				uint32_t walk[4], wsp = 0, j = 0;
+				walk[wsp++] = cref[k];
+				for (int it = 0; it < 16 && wsp && j < ccount[k]; ++it) {  // <= 5 nodes; the cap guards bad input
+					const uint32_t r = walk[--wsp];
+					if (r & kLeafFlag) {
+						prim_order[tri_base + tri_off + j++] = sorted[r & ~kLeafFlag];
+					} else if (wsp + 2 <= 4) {
+						walk[wsp++] = bchild[2 * r + 1];
+						walk[wsp++] = bchild[2 * r];
+					}
+				}
+				if (j != ccount[k]) atomicOr(&counters[C_ERR], 32u);
 				tri_off += ccount[k];
 			}
 		}
@@ -438,6 +620,7 @@ lrx_status build_wide_bvh(uint32_t n, const float4 *d_lo, const float4 *d_hi, ui
 	if ((rc = S.vals_alt.alloc(sizeof(uint32_t) * n)) != LRX_OK) return rc;
 	if ((rc = S.bnodes.alloc((sizeof(float4) * 2 + sizeof(uint32_t) * 2) * ni)) != LRX_OK) return rc;
 	if ((rc = S.branges.alloc(sizeof(uint2) * ni)) != LRX_OK) return rc;
+	if ((rc = S.treelet_scratch.alloc(sizeof(uint32_t) * ((size_t)n + ni))) != LRX_OK) return rc;
 	if ((rc = S.other_bound.alloc(sizeof(uint32_t) * ni)) != LRX_OK) return rc;
 	if ((rc = S.wide_nodes.alloc(sizeof(WideNode) * (size_t)n)) != LRX_OK) return rc;
 	if ((rc = S.prim_order.alloc(sizeof(uint32_t) * n)) != LRX_OK) return rc;
@@ -449,7 +632,9 @@ lrx_status build_wide_bvh(uint32_t n, const float4 *d_lo, const float4 *d_hi, ui
 	float4 *bn_lo = S.bnodes.as<float4>();
 	float4 *bn_hi = bn_lo + ni;
 	uint32_t *bchild = reinterpret_cast<uint32_t *>(bn_hi + ni);
-	uint2 *brange = S.branges.as<uint2>();
+	uint2 *bmeta = S.branges.as<uint2>();
+	uint32_t *lparent = S.treelet_scratch.as<uint32_t>();
+	float *sah = reinterpret_cast<float *>(lparent + n);
 
 	k_init_counters<<<1, 32, 0, st>>>(counters);
 	k_centroid_bounds<<<std::min(blocks_for(n, 256), 1024u), 256, 0, st>>>(n, d_lo, d_hi, counters);
@@ -466,11 +651,18 @@ lrx_status build_wide_bvh(uint32_t n, const float4 *d_lo, const float4 *d_hi, ui
 	const uint32_t *sorted = dv.Current();
 
 	LRX_CUDA(cudaMemsetAsync(S.other_bound.ptr, 0xff, sizeof(uint32_t) * ni, st));
-	k_hierarchy<<<blocks_for(n, 128), 128, 0, st>>>(n, keys, sorted, d_lo, d_hi, bchild, bn_lo, bn_hi, brange,
-			S.other_bound.as<uint32_t>(), counters);
+	LRX_CUDA(cudaMemsetAsync(bmeta, 0xff, sizeof(uint2) * ni, st));  // root's parent stays kNull
+	k_hierarchy<<<blocks_for(n, 128), 128, 0, st>>>(n, keys, sorted, d_lo, d_hi, bchild, bn_lo, bn_hi, bmeta,
+			lparent, S.other_bound.as<uint32_t>(), counters);
 	LRX_CUDA(cudaGetLastError());
 
-	(void)treelet_passes;
+	// Treelet passes: pass k restructures subtrees of >= 7 * 2^k primitives.
+	for (uint32_t pass = 0; n > 2 && pass < treelet_passes; ++pass) {
+		LRX_CUDA(cudaMemsetAsync(S.other_bound.ptr, 0, sizeof(uint32_t) * ni, st));  // visit counters
+		k_treelet<<<blocks_for(n, 128), 128, 0, st>>>(n, sorted, d_lo, d_hi, bchild, bn_lo, bn_hi, bmeta, lparent,
+				sah, S.other_bound.as<uint32_t>(), leaf_max, 7u << std::min(pass, 20u));
+		LRX_CUDA(cudaGetLastError());
+	}
 
 	// Level-synchronous collapse
 	k_init_collapse<<<1, 1, 0, st>>>(S.queue_a.as<uint2>(), counters);
@@ -489,12 +681,14 @@ lrx_status build_wide_bvh(uint32_t n, const float4 *d_lo, const float4 *d_hi, ui
 		}
 		++depth;
 		if (depth > (uint32_t)kMaxTreeDepth) {
+			// a restructured tree may be deeper than the stack allows: build the plain LBVH instead
+			if (treelet_passes > 0) return build_wide_bvh(n, d_lo, d_hi, leaf_max, 0, st, S, out);
 			set_error("BVH deeper than the traversal stack allows");
 			return LRX_ERR_BUILD;
 		}
 		LRX_CUDA(cudaMemsetAsync(counters + cout, 0, sizeof(uint32_t), st));
 		k_collapse<<<std::min(blocks_for(n_in, 128), 152u * 16u), 128, 0, st>>>(qin, counters + cin, qout,
-				counters + cout, bchild, bn_lo, bn_hi, brange, sorted, d_lo, d_hi, leaf_max,
+				counters + cout, bchild, bn_lo, bn_hi, bmeta, sorted, d_lo, d_hi, leaf_max,
 				S.wide_nodes.as<WideNode>(), S.prim_order.as<uint32_t>(), counters, n);
 		LRX_CUDA(cudaGetLastError());
 		std::swap(qin, qout);

@@ -165,8 +165,15 @@ lrx_status lrx_server::make_resident(std::unique_lock<std::mutex> &lk, uint32_t 
 	if (!make_room(need, pinned)) return LRX_ERR_BUSY;
 	lk.unlock();
 	lrx_scene *sc = nullptr;
+	// Admission builds the plain LBVH (no treelet passes): a scene evicted
+	// under the budget is rebuilt on its next request, and that build is on
+	// the request's latency.
+	lrx_build_opts bo{};
+	bo.struct_size = sizeof(bo);
+	bo.leaf_max = 3;
+	bo.treelet_passes = 0;
 	lrx_status rc = lrx_scene_create(e->meshes.data(), (uint32_t)e->meshes.size(),
-			e->has_objects ? e->objects.data() : nullptr, (uint32_t)e->objects.size(), nullptr, build_stream, &sc);
+			e->has_objects ? e->objects.data() : nullptr, (uint32_t)e->objects.size(), &bo, build_stream, &sc);
 	lrx_scene_info info{};
 	if (rc == LRX_OK) lrx_scene_get_info(sc, &info);
 	lk.lock();

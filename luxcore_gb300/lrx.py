@@ -282,7 +282,7 @@ def _object_array(scene: W.SceneDesc):
 class Scene:
     """A device-resident scene (lrx_scene): meshes + objects of a SceneDesc."""
 
-    def __init__(self, scene: W.SceneDesc, stream: int = 0, leaf_max: int = 3, treelet_passes: int = 0):
+    def __init__(self, scene: W.SceneDesc, stream: int = 0, leaf_max: int = 3, treelet_passes: int = 2):
         L = load()
         self._keep = []
         meshes = (MeshDesc * max(1, len(scene.meshes)))()

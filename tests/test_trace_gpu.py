@@ -387,3 +387,35 @@ def test_autotune_picks_a_valid_config_and_keeps_results(torch_cuda):
     o = po.OracleScene(scene)
     ref, _ = o.intersect(rays)
     assert_parity(gpu_trace(torch, s, rays), ref, o, rays, min_hit_rate=0.05)
+
+
+@pytest.mark.parametrize("passes", [1, 2, 3])
+def test_treelet_restructured_builds_keep_parity(torch_cuda, passes):
+    """Treelet SAH passes rewrite the binary tree before the collapse: the
+    builder's structural validation must pass and traces must still match the
+    oracle -- flat, heightfield, instanced and tiny scenes."""
+    torch = torch_cuda
+    scene, rays = W.config1(n_tris=30000, n_rays=40000, seed=700 + passes)
+    s = lrx.Scene(scene, treelet_passes=passes)
+    o = po.OracleScene(scene)
+    ref, _ = o.intersect(rays)
+    assert_parity(gpu_trace(torch, s, rays), ref, o, rays, min_hit_rate=0.2)
+    a = check_anyhit(gpu_trace(torch, s, rays, lrx.LRX_TRACE_ANY), ref, o, rays)
+    assert a["ok"], a
+    hf = W.SceneDesc([W.heightfield_mesh(128, 710 + passes)])
+    s = lrx.Scene(hf, treelet_passes=passes)
+    prim = W.pinhole_rays(128, 128)
+    o = po.OracleScene(hf)
+    ref, _ = o.intersect(prim)
+    assert_parity(gpu_trace(torch, s, prim), ref, o, prim, min_hit_rate=0.2)
+    inst, closest, _ = W.config3(n_rays=1 << 13, n_meshes=3, freq=10, n_inst=100, extent=3.0, scale=(0.1, 0.4))
+    s = lrx.Scene(inst, treelet_passes=passes)
+    o = po.OracleScene(inst)
+    ref, _ = o.intersect(closest)
+    assert_parity(gpu_trace(torch, s, closest), ref, o, closest, min_hit_rate=0.05)
+    for n in (1, 2, 3, 4, 7, 8, 9, 30):
+        tiny, r = W.config1(n_tris=n, n_rays=2000, seed=720 + n)
+        s = lrx.Scene(tiny, treelet_passes=passes)
+        o = po.OracleScene(tiny)
+        ref, _ = o.intersect(r)
+        assert_parity(gpu_trace(torch, s, r), ref, o, r)
