@@ -47,7 +47,9 @@ def make_requests(torch, n_scenes, n_req, seed):
 
 
 def alone_results(torch, descs, reqs):
-    scenes = [lrx.Scene(d) for d in descs]
+    # the server builds the plain LBVH (no treelet passes); any-hit results
+    # depend on the tree, so the reference uses the same build
+    scenes = [lrx.Scene(d, treelet_passes=0) for d in descs]
     out = []
     st = torch.cuda.current_stream().cuda_stream
     for sid, d_r, _, n, mode in reqs:
@@ -100,7 +102,7 @@ def test_results_same_alone_and_in_the_mix(torch_cuda, policy):
 def test_lru_eviction_under_a_tight_budget(torch_cuda):
     torch = torch_cuda
     descs = scene_set()
-    probe = [lrx.Scene(d) for d in descs]
+    probe = [lrx.Scene(d, treelet_passes=0) for d in descs]  # the server's build
     sizes = [p.info()["device_bytes"] for p in probe]
     for p in probe:
         p.close()
