@@ -232,10 +232,11 @@ def count_kernel_launches(stream_handle, fn):
 # CPU arm (the reference's CPU accelerator, restated)
 # ---------------------------------------------------------------------------
 
-def cpu_measure(scene, sets, threads: int):
-    """Times the oracle's BVHAccel::Intersect over the given ray sets."""
+def cpu_measure(scene, sets, threads: int, accel: str = "bvh"):
+    """Times the oracle's BVHAccel::Intersect (or MBVHAccel::Intersect for
+    instanced scenes) over the given ray sets."""
     from oracle import pyoracle as po
-    o = po.OracleScene(scene, po.ACCEL_BVH)
+    o = po.OracleScene(scene, po.ACCEL_MBVH if accel == "mbvh" else po.ACCEL_BVH)
     total, secs = 0, 0.0
     for rays in sets:
         _, s = o.intersect(rays, n_threads=threads)
@@ -539,6 +540,140 @@ def run_lrx(args):
 
 
 # ---------------------------------------------------------------------------
+# Instanced two-level scene: 16 x 200,000-triangle icospheres, 4,096 instances
+# ---------------------------------------------------------------------------
+
+def run_instanced(args):
+    """16 displaced icospheres of 200,000 triangles under 4,096 random affine
+    instances (819,200,000 effective triangles) in [0,10]^3; per step
+    8,388,608 closest-hit and 8,388,608 any-hit rays (maxt U[0.5, 5])."""
+    import torch
+
+    from luxcore_gb300 import lrx
+
+    torch.cuda.set_device(0)
+    t0 = time.perf_counter()
+    scene_desc, closest, anyr = W.config3(n_rays=args.inst_rays)
+    log(f"[instanced] {time.strftime('%H:%M:%S')} scene and rays generated in {time.perf_counter() - t0:.1f}s")
+    stream = torch.cuda.Stream()
+    st = stream.cuda_stream
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        scene = lrx.Scene(scene_desc, stream=st)
+    build_s = time.perf_counter() - t0
+    info = scene.info()
+    log(f"[instanced] scene built {info}")
+    dev = []
+    for name, r, mode in (("closest", closest, lrx.LRX_TRACE_CLOSEST), ("any", anyr, lrx.LRX_TRACE_ANY)):
+        dr = torch.from_numpy(np.ascontiguousarray(r).view(np.uint8).reshape(-1).copy()).cuda()
+        dh = torch.empty(r.shape[0] * HIT_BYTES, dtype=torch.uint8, device="cuda")
+        dev.append((name, dr, dh, r.shape[0], mode))
+    rays_per_step = sum(x[3] for x in dev)
+    counts, alg = {}, {}
+    cbuf = torch.zeros(4, dtype=torch.int64, device="cuda")
+    for name, dr, dh, n, mode in dev:
+        cbuf.zero_()
+        torch.cuda.synchronize()
+        scene.trace_counted(dr.data_ptr(), dh.data_ptr(), n, mode, cbuf.data_ptr(), st)
+        stream.synchronize()
+        nn, nt, ni, _ = cbuf.cpu().tolist()
+        counts[name] = (nn / n, nt / n, ni / n)
+        alg[name] = n * (RAY_BYTES + HIT_BYTES + nn / n * NODE_BYTES + nt / n * TRI_BYTES + ni / n * INST_BYTES)
+    # size-independent check at full size: any-hit hit/miss equals closest-hit hit/miss
+    name, dr, dh, n, _ = dev[1]
+    dh_c = torch.empty_like(dh)
+    scene.trace(dr.data_ptr(), dh_c.data_ptr(), n, lrx.LRX_TRACE_CLOSEST, st)
+    scene.trace(dr.data_ptr(), dh.data_ptr(), n, lrx.LRX_TRACE_ANY, st)
+    stream.synchronize()
+    mi_any = dh.view(torch.int32).view(-1, 5)[:, 3].cpu().numpy().view(np.uint32)
+    mi_cl = dh_c.view(torch.int32).view(-1, 5)[:, 3].cpu().numpy().view(np.uint32)
+    hit_any, hit_cl = mi_any != W.NULL_INDEX, mi_cl != W.NULL_INDEX
+    anyhit_consistent = bool(np.array_equal(hit_any, hit_cl))
+    del dh_c
+
+    def step(evs=None):
+        for k, (name, dr, dh, n, mode) in enumerate(dev):
+            if evs is not None:
+                evs[k][0].record(stream)
+            scene.trace(dr.data_ptr(), dh.data_ptr(), n, mode, st)
+            if evs is not None:
+                evs[k][1].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    stream.synchronize()
+    if scene.device_status(st) != 0:
+        raise RuntimeError("device status word set during warm-up")
+    launches_per_step = count_kernel_launches(st, step)
+    ev = [[(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in dev]
+          for _ in range(args.steps)]
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(0)
+    torch.cuda.synchronize()
+    clocks.start()
+    start.record(stream)
+    for k in range(args.steps):
+        step(ev[k])
+    end.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    if scene.device_status(st) != 0:
+        raise RuntimeError("device status word set during the timed steps")
+    elapsed_ms = start.elapsed_time(end)
+    kern_ms = {name: statistics.mean(ev[k][j][0].elapsed_time(ev[k][j][1]) for k in range(args.steps))
+               for j, (name, *_rest) in enumerate(dev)}
+    value = rays_per_step * args.steps / (elapsed_ms / 1e3) / 1e6
+    peak, peak_kind = load_peaks()
+    achieved = sum(alg.values()) / (sum(kern_ms.values()) / 1e3) / 1e9
+    cpu = None
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        frac = args.ref_fraction * 64
+        sample = [closest[::frac], anyr[::frac]]
+        n_s, secs = cpu_measure(scene_desc, sample, threads, accel="mbvh")
+        cpu = {"value": round(n_s / secs / 1e6, 3), "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"every {frac}th ray of both sets ({n_s} rays), oracle MBVHAccel::Intersect restatement "
+                         f"(closest hit for both), {threads} threads"}
+    line = {
+        "metric": "Mrays/s closest/any-hit on the instanced two-level scene (1 GB300, % HBM roofline)",
+        "value": round(value, 3), "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(elapsed_ms / args.steps, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {
+            "workload": f"instanced: {info['blas_count']} meshes x 200000 tris, {info['instance_count']} instances "
+                        f"({info['triangle_count']} effective tris); {dev[0][3]} closest + {dev[1][3]} any-hit rays",
+            "rays_per_step": rays_per_step, "build_ms": round(info["build_ms"], 1),
+            "scene_build_wall_s": round(build_s, 3), "wide_nodes": info["node_count"],
+            "device_MB": round(info["device_bytes"] / 1e6, 1),
+            "per_set_ms": {k: round(v, 4) for k, v in kern_ms.items()},
+            "per_set_Mrays": {name: round(n / (kern_ms[name] / 1e3) / 1e6, 1) for name, _, _, n, _ in dev},
+            "nodes_tris_insts_per_ray": {k: [round(x, 2) for x in v] for k, v in counts.items()},
+            "hit_rate": {"closest": round(float((dh_hits(dev[0]) != W.NULL_INDEX).mean()), 4),
+                         "any": round(float(hit_any.mean()), 4)},
+            "anyhit_hitmiss_equals_closest": anyhit_consistent,
+            "l2": "inputs larger than L2 (rays 805 MB + hits 336 MB per step)",
+        },
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": None, "peak_kind": peak_kind,
+                     "bytes_per_ray": round(sum(alg.values()) / rays_per_step, 1)},
+        "cpu_baseline": cpu,
+        "gpu_launches": (launches_per_step if launches_per_step is not None else len(dev)) * args.steps,
+        "gpu_launches_per_step": launches_per_step,
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    scene.close()
+    return 0
+
+
+def dh_hits(entry):
+    """meshIndex column of a device hit buffer (host copy)."""
+    import torch
+    _name, _dr, dh, _n, _mode = entry
+    return dh.view(torch.int32).view(-1, 5)[:, 3].cpu().numpy().view(np.uint32)
+
+
+# ---------------------------------------------------------------------------
 # Uneven batches over several resident scenes: plain vs queue kernel
 # ---------------------------------------------------------------------------
 
@@ -836,9 +971,10 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=2.0)
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[2000.0, 800.0])
     ap.add_argument("--serve-streams", type=int, default=4)
-    ap.add_argument("--workload", default="heightfield", choices=["heightfield", "batching", "serving"],
+    ap.add_argument("--workload", default="heightfield", choices=["heightfield", "batching", "serving", "instanced"],
                     help="heightfield = the headline line; batching = uneven batches, plain vs queue kernel")
     ap.add_argument("--batches", type=int, default=512)
+    ap.add_argument("--inst-rays", type=int, default=1 << 23, help="instanced workload: rays per set")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--ref-fraction", type=int, default=4,
                     help="CPU legs trace every Nth ray of each set")
@@ -860,6 +996,8 @@ def main():
         return run_serving(args)
     if args.workload == "batching" and args.impl == "lrx":
         return run_batching(args)
+    if args.workload == "instanced" and args.impl == "lrx":
+        return run_instanced(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_lrx(args)
