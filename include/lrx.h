@@ -180,6 +180,8 @@ typedef struct lrx_trace_config {
                                           (one radix pass, caller order kept within an octant) */
 #define LRX_VARIANT_PERSISTENT 0x40u   /* persistent warps claim rays from a device counter
                                           (ballot + shuffle) and refill idle lanes; blocks <= 128 */
+#define LRX_VARIANT_SMEM_STACK 0x80u   /* top 8 traversal-stack entries per ray in shared memory
+                                          (deeper entries in local memory) */
 
 /* Sets / reads the launch configuration lrx_trace uses for this scene.
  * No reference counterpart (the reference fixes 32-thread blocks,

@@ -118,7 +118,8 @@ constexpr uint32_t kTraceBlock = 128;
 constexpr uint32_t kVarSortRays = 0x10u;   // reorder rays by octant + origin before tracing
 constexpr uint32_t kVarSortOctantOnly = 0x20u;  // ... by direction octant only (one radix pass)
 constexpr uint32_t kVarPersistent = 0x40u;  // persistent warps with warp-level ray fetch
-constexpr uint32_t kVarAll = 0x7fu;        // every defined variant bit
+constexpr uint32_t kVarSmemStack = 0x80u;  // top of the traversal stack in shared memory
+constexpr uint32_t kVarAll = 0xffu;        // every defined variant bit
 constexpr uint32_t kSortMinRays = 32768;   // smaller batches are traced in caller order
 
 lrx_status launch_trace(const TraceArgs &a, cudaStream_t stream);

@@ -203,8 +203,27 @@ struct TravState {
 };
 // The traversal stack lives apart from TravState so that the state's scalars
 // stay in registers (a dynamically indexed member would put the whole
-// struct in local memory).
+// struct in local memory).  With LRX_VARIANT_SMEM_STACK its first
+// kSmemStack entries -- the top of a short stack, where nearly all pushes
+// and pops land -- are in shared memory instead, thread t's entry e at
+// top[e * blockDim.x] (consecutive lanes in consecutive 8-byte words, no
+// bank conflicts); deeper entries stay in local memory.
 typedef uint2 TravStack[kStackSize];
+constexpr int kSmemStack = 8;
+struct StackTop {
+	uint2 *top;
+	uint32_t stride;
+};
+template <bool SMEM>
+__device__ __forceinline__ void stack_put(TravStack &st, StackTop t, int i, uint2 v) {
+	if (SMEM && i < kSmemStack) t.top[i * t.stride] = v;
+	else st[i] = v;
+}
+template <bool SMEM>
+__device__ __forceinline__ uint2 stack_get(const TravStack &st, StackTop t, int i) {
+	if (SMEM && i < kSmemStack) return t.top[i * t.stride];
+	return st[i];
+}
 
 enum : int { kRayMasked = 0, kRayAnswered = 1, kRayTraverse = 2 };
 
@@ -251,16 +270,16 @@ __device__ __forceinline__ int ray_begin(const TraceArgs &a, uint32_t i, bool st
 // status word).  Every trip either expands a node -- at most visit_limit of
 // them -- or consumes a stack entry or an instance bit, so a ray finishes in
 // a bounded number of trips.
-template <bool ANY, bool TWO_LEVEL, bool COUNT, bool MM3>
+template <bool ANY, bool TWO_LEVEL, bool COUNT, bool MM3, bool SMEM = false>
 __device__ __forceinline__ bool ray_step(const TraceArgs &a, TravState &s, TravStack &stack, bool keep, uint64_t pol,
-		Counts &c) {
+		Counts &c, StackTop top = StackTop{nullptr, 0}) {
 #define LRX_PUSH(V)                                          \
 	{                                                        \
 		if (s.sp >= kStackSize) {                            \
 			atomicOr(a.status, kStatusStackOverflow);        \
 			return true;                                     \
 		}                                                    \
-		stack[s.sp++] = (V);                                 \
+		stack_put<SMEM>(stack, top, s.sp++, (V));            \
 	}
 	if (s.ng.y > 0x00ffffffu) {
 		const uint32_t j = __ffs(s.ng.y >> 24) - 1;
@@ -341,7 +360,7 @@ __device__ __forceinline__ bool ray_step(const TraceArgs &a, TravState &s, TravS
 			make_active(s.ray, s.wo, s.wd);
 		}
 		if (s.sp == 0) return true;
-		s.ng = stack[--s.sp];
+		s.ng = stack_get<SMEM>(stack, top, --s.sp);
 	}
 	return false;
 #undef LRX_PUSH
@@ -367,8 +386,10 @@ __device__ __forceinline__ void ray_write(const TraceArgs &a, uint32_t i, const 
 // Traces ray `tid` of the batch `a` (through a.order when set) and writes its
 // hit.  Shared by the one-batch kernel and the multi-batch queue kernel.
 template <bool ANY, bool TWO_LEVEL, bool COUNT, uint32_t CV>
-__device__ __forceinline__ void trace_ray(const TraceArgs &a, uint32_t tid, bool active, Counts &cnt) {
+__device__ __forceinline__ void trace_ray(const TraceArgs &a, uint32_t tid, bool active, Counts &cnt,
+		StackTop top = StackTop{nullptr, 0}) {
 	constexpr bool MM3 = (CV & kVarMinMax3) != 0;
+	constexpr bool SMEM = (CV & kVarSmemStack) != 0;
 	if (!active) return;
 	const uint32_t i = a.order ? a.order[tid] : tid;  // the ray this thread traces
 	const bool keep = (a.variant & kVarSceneEvictLast) != 0;
@@ -379,7 +400,7 @@ __device__ __forceinline__ void trace_ray(const TraceArgs &a, uint32_t tid, bool
 	const int k = ray_begin(a, i, stream, s);
 	if (k == kRayMasked) return;
 	if (k == kRayTraverse)
-		while (!ray_step<ANY, TWO_LEVEL, COUNT, MM3>(a, s, stack, keep, pol, cnt)) {
+		while (!ray_step<ANY, TWO_LEVEL, COUNT, MM3, SMEM>(a, s, stack, keep, pol, cnt, top)) {
 		}
 	ray_write(a, i, s, stream);
 	if (COUNT) cnt.rays += 1;
@@ -388,10 +409,11 @@ __device__ __forceinline__ void trace_ray(const TraceArgs &a, uint32_t tid, bool
 template <bool ANY, bool TWO_LEVEL, bool COUNT, uint32_t CV>
 __global__ void __launch_bounds__((CV & kVarOccupancy) ? 64 : 1024, (CV & kVarOccupancy) ? 20 : 0)
 k_trace(TraceArgs a) {
+	extern __shared__ uint2 s_stack_top[];  // kSmemStack entries per thread with SMEM_STACK, else empty
 	const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
 	if (!COUNT && tid >= a.count) return;
 	Counts cnt{0, 0, 0, 0};
-	trace_ray<ANY, TWO_LEVEL, COUNT, CV>(a, tid, tid < a.count, cnt);
+	trace_ray<ANY, TWO_LEVEL, COUNT, CV>(a, tid, tid < a.count, cnt, StackTop{s_stack_top + threadIdx.x, blockDim.x});
 	if (COUNT) {
 		// every lane of the block reaches this point in the counting variant
 		unsigned long long v[4] = {cnt.nodes, cnt.tris, cnt.insts, cnt.rays};
@@ -454,6 +476,9 @@ uint32_t next_queue_slot() {
 template <bool ANY, bool TWO_LEVEL, uint32_t CV>
 __global__ void __launch_bounds__(kTraceBlock, 8) k_trace_fetch(TraceArgs a, uint32_t slot_index, uint32_t refill) {
 	constexpr bool MM3 = (CV & kVarMinMax3) != 0;
+	constexpr bool SMEM = (CV & kVarSmemStack) != 0;
+	extern __shared__ uint2 s_stack_top[];  // kSmemStack entries per thread with SMEM_STACK, else empty
+	const StackTop top{s_stack_top + threadIdx.x, blockDim.x};
 	uint32_t *slot = g_queue[slot_index];
 	const bool keep = (a.variant & kVarSceneEvictLast) != 0;
 	const bool stream = (a.variant & kVarStreamRays) != 0;
@@ -487,7 +512,7 @@ __global__ void __launch_bounds__(kTraceBlock, 8) k_trace_fetch(TraceArgs a, uin
 			if (drained) break;
 			continue;  // every lane idle: the next trip claims 32 rays
 		}
-		if (rid != kNull && ray_step<ANY, TWO_LEVEL, false, MM3>(a, s, stack, keep, pol, cnt)) {
+		if (rid != kNull && ray_step<ANY, TWO_LEVEL, false, MM3, SMEM>(a, s, stack, keep, pol, cnt, top)) {
 			ray_write(a, rid, s, stream);
 			rid = kNull;
 		}
@@ -760,6 +785,7 @@ lrx_status launch_trace_queue(const QueueParams &p, cudaStream_t st) {
 // most one ray per thread), all sharing one counter slot.
 template <bool ANY, bool TWO_LEVEL, uint32_t CV>
 static lrx_status launch_fetch(const TraceArgs &a, uint32_t bs, cudaStream_t st) {
+	const size_t smem_bytes = (CV & kVarSmemStack) ? sizeof(uint2) * kSmemStack * bs : 0;
 	static int resident[kTraceBlock / 32] = {0};  // blocks per SM for bs = 32, 64, 96, 128
 	static int sms = 0;
 	int &per_sm = resident[bs / 32 - 1];
@@ -767,13 +793,14 @@ static lrx_status launch_fetch(const TraceArgs &a, uint32_t bs, cudaStream_t st)
 		int dev = 0, n = 0, r = 0;
 		LRX_CUDA(cudaGetDevice(&dev));
 		LRX_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
-		LRX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_trace_fetch<ANY, TWO_LEVEL, CV>, (int)bs, 0));
+		LRX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_trace_fetch<ANY, TWO_LEVEL, CV>, (int)bs,
+				smem_bytes));
 		sms = n;
 		per_sm = std::max(1, r);
 	}
 	const uint32_t grid = (uint32_t)std::min<uint64_t>(((uint64_t)a.count + bs - 1) / bs, (uint64_t)sms * per_sm);
 	const uint32_t refill = a.refill == 0 ? 16u : std::min(32u, a.refill);
-	k_trace_fetch<ANY, TWO_LEVEL, CV><<<grid, bs, 0, st>>>(a, next_queue_slot(), refill);
+	k_trace_fetch<ANY, TWO_LEVEL, CV><<<grid, bs, smem_bytes, st>>>(a, next_queue_slot(), refill);
 	LRX_CUDA(cudaGetLastError());
 	return LRX_OK;
 }
@@ -791,7 +818,10 @@ lrx_status launch_trace(const TraceArgs &a, cudaStream_t st) {
 		// persistent warps with ray fetch; block size capped at kTraceBlock
 		const uint32_t fbs = std::min(bs, kTraceBlock);
 		const bool mm3 = (a.variant & kVarMinMax3) != 0;
-#define LRX_FETCH(A, T) (mm3 ? launch_fetch<A, T, kVarMinMax3>(a, fbs, st) : launch_fetch<A, T, 0u>(a, fbs, st))
+		const bool smem = (a.variant & kVarSmemStack) != 0;
+#define LRX_FETCH(A, T)                                                                           \
+	(smem ? launch_fetch<A, T, kVarSmemStack>(a, fbs, st)                                          \
+		  : (mm3 ? launch_fetch<A, T, kVarMinMax3>(a, fbs, st) : launch_fetch<A, T, 0u>(a, fbs, st)))
 		if (a.any_hit) return a.two_level ? LRX_FETCH(true, true) : LRX_FETCH(true, false);
 		return a.two_level ? LRX_FETCH(false, true) : LRX_FETCH(false, false);
 #undef LRX_FETCH
@@ -799,10 +829,13 @@ lrx_status launch_trace(const TraceArgs &a, cudaStream_t st) {
 	// compile-time variants; the occupancy-bounded build only takes <= 64-thread blocks
 	uint32_t cv = a.variant & (kVarMinMax3 | kVarOccupancy);
 	if (bs > 64) cv &= ~kVarOccupancy;
+	if (a.variant & kVarSmemStack) cv = kVarSmemStack;  // a build of its own (no other compile-time bits)
 	if (cnt) cv = 0;
-#define LRX_LAUNCH(A, T, C, V) k_trace<A, T, C, V><<<grid, bs, 0, st>>>(a)
+	const size_t smem = cv == kVarSmemStack ? sizeof(uint2) * kSmemStack * bs : 0;
+#define LRX_LAUNCH(A, T, C, V) k_trace<A, T, C, V><<<grid, bs, smem, st>>>(a)
 #define LRX_LAUNCH_V(A, T)                                         \
 	switch (cv) {                                                  \
+	case kVarSmemStack: LRX_LAUNCH(A, T, false, kVarSmemStack); break; \
 	case kVarMinMax3: LRX_LAUNCH(A, T, false, kVarMinMax3); break; \
 	case kVarOccupancy: LRX_LAUNCH(A, T, false, kVarOccupancy); break; \
 	case kVarMinMax3 | kVarOccupancy: LRX_LAUNCH(A, T, false, kVarMinMax3 | kVarOccupancy); break; \

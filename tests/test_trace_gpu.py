@@ -26,11 +26,12 @@ SENT = 0xDEADBEEF
 KERNELS = pytest.mark.parametrize("kernel", [(128, 0, 0), (64, 8, 0), (256, 24, 0), (64, 8, 0xF), (128, 8, 0x7),
                                              (64, 8, 0x10), (32, 8, 0x1F), (64, 8, 0x30),
                                              (64, 8, 0x40), (128, 0, 0x41, 1), (32, 8, 0x46, 32),
-                                             (64, 8, 0x50, 8)],
+                                             (64, 8, 0x50, 8), (64, 8, 0xC0, 8), (256, 8, 0x80), (64, 8, 0x90)],
                                   ids=["b128", "b64-p8", "b256-p24", "b64-p8-allvariants", "b128-p8-mm3-hints",
                                        "b64-p8-sorted", "b32-p8-sorted-all", "b64-p8-octsort",
                                        "b64-p8-persistent", "b128-persistent-refill1",
-                                       "b32-p8-persistent-refill32-hints", "b64-p8-sorted-persistent-refill8"])
+                                       "b32-p8-persistent-refill32-hints", "b64-p8-sorted-persistent-refill8",
+                                       "b64-p8-persistent-smemstack", "b256-p8-smemstack", "b64-p8-sorted-smemstack"])
 
 
 def make_scene(desc, kernel=(64, 8, 0), **kw):
@@ -316,7 +317,7 @@ def test_trace_config_struct_versions(torch_cuda):
     got = lrx.TraceConfig(20, 0, 0, 0, 0, 77)
     assert L.lrx_scene_get_trace_config(s.handle, ctypes.byref(got)) == 0
     assert (got.struct_size, got.block_size, got.refill) == (20, 64, 77)  # nothing past 20 bytes written
-    for bad in [lrx.TraceConfig(16, 64, 8, 0, 0, 0), lrx.TraceConfig(24, 64, 8, 0x80, 0, 0),
+    for bad in [lrx.TraceConfig(16, 64, 8, 0, 0, 0), lrx.TraceConfig(24, 64, 8, 0x100, 0, 0),
                 lrx.TraceConfig(24, 64, 8, 0x40, 0, 33), lrx.TraceConfig(24, 48, 8, 0, 0, 0)]:
         assert L.lrx_scene_set_trace_config(s.handle, ctypes.byref(bad)) == lrx.LRX_ERR_INVALID_ARGUMENT
 
