@@ -317,7 +317,7 @@ def test_trace_config_struct_versions(torch_cuda):
     got = lrx.TraceConfig(20, 0, 0, 0, 0, 77)
     assert L.lrx_scene_get_trace_config(s.handle, ctypes.byref(got)) == 0
     assert (got.struct_size, got.block_size, got.refill) == (20, 64, 77)  # nothing past 20 bytes written
-    for bad in [lrx.TraceConfig(16, 64, 8, 0, 0, 0), lrx.TraceConfig(24, 64, 8, 0x100, 0, 0),
+    for bad in [lrx.TraceConfig(16, 64, 8, 0, 0, 0), lrx.TraceConfig(24, 64, 8, 0x80000000, 0, 0),
                 lrx.TraceConfig(24, 64, 8, 0x40, 0, 33), lrx.TraceConfig(24, 48, 8, 0, 0, 0)]:
         assert L.lrx_scene_set_trace_config(s.handle, ctypes.byref(bad)) == lrx.LRX_ERR_INVALID_ARGUMENT
 
