@@ -443,6 +443,29 @@ def run_lrx(args):
         log(f"[bench] {time.strftime('%H:%M:%S')} build sweep done")
 
     if args.sweep:
+        # compaction: the bounce set with half of its rays masked (finished paths)
+        name, dr, dh, n, mode = dev[1]
+        half = dr.clone()
+        words = half.view(torch.int32).view(-1, 12)
+        g = torch.Generator(device=f"cuda:{local}")
+        g.manual_seed(5)
+        words[:, 9] = torch.where(torch.rand(n, generator=g, device=f"cuda:{local}") < 0.5,
+                                  torch.ones_like(words[:, 9]), words[:, 9])
+        alt["bounce-half-masked"] = {}
+        for key, var in (("persistent", 64), ("persistent+compact", 64 | 256)):
+            scene.set_trace_config(64, 8, var, modes=1, refill=8)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            scene.trace(half.data_ptr(), dh.data_ptr(), n, mode, st)
+            e0.record(stream)
+            for _ in range(5):
+                scene.trace(half.data_ptr(), dh.data_ptr(), n, mode, st)
+            e1.record(stream)
+            e1.synchronize()
+            alt["bounce-half-masked"][key + "_ms"] = round(e0.elapsed_time(e1) / 5, 4)
+        c = saved_cfg[lrx.LRX_TRACE_CLOSEST]
+        scene.set_trace_config(c["block_size"], c["postpone"], c["variant"], modes=1, refill=c["refill"])
+        del half
+
         # each set as a one-batch lrx_trace_batches call (the queue kernel)
         alt["queue-1batch"] = {}
         for name, dr, dh, n, mode in dev:

@@ -182,6 +182,9 @@ typedef struct lrx_trace_config {
                                           (ballot + shuffle) and refill idle lanes; blocks <= 128 */
 #define LRX_VARIANT_SMEM_STACK 0x80u   /* top 8 traversal-stack entries per ray in shared memory
                                           (deeper entries in local memory) */
+#define LRX_VARIANT_COMPACT 0x100u     /* with PERSISTENT: compact the indices of the unmasked rays
+                                          first (stable) and trace only those -- for wavefront
+                                          buffers where finished paths leave masked rays */
 
 /* Sets / reads the launch configuration lrx_trace uses for this scene.
  * No reference counterpart (the reference fixes 32-thread blocks,

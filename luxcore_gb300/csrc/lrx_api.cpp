@@ -678,6 +678,8 @@ static lrx_status trace_common(lrx_scene *s, const void *d_rays, void *d_hits, u
 	a.refill = cfg.refill;
 	if ((a.variant & kVarSortRays) && count >= kSortMinRays && s->root != kNull)
 		return launch_trace_sorted(a, s->bounds_lo, s->bounds_hi, st);
+	if ((a.variant & kVarCompact) && (a.variant & kVarPersistent) && !d_counters && count < 0x80000000u)
+		return launch_trace_compacted(a, st);
 	return launch_trace(a, st);
 }
 

@@ -113,13 +113,15 @@ struct TraceArgs {
 	uint32_t visit_limit = 1u << 24;  // node visits after which a ray is abandoned (status bit 1)
 	const uint32_t *order = nullptr;  // thread i traces ray order[i] (sorted launches)
 	uint32_t refill = 0;           // persistent fetch: idle lanes that trigger a warp's claim (0 = 16)
+	const uint32_t *count_dev = nullptr;  // persistent fetch: rays to claim, read on the device (<= count)
 };
 constexpr uint32_t kTraceBlock = 128;
 constexpr uint32_t kVarSortRays = 0x10u;   // reorder rays by octant + origin before tracing
 constexpr uint32_t kVarSortOctantOnly = 0x20u;  // ... by direction octant only (one radix pass)
 constexpr uint32_t kVarPersistent = 0x40u;  // persistent warps with warp-level ray fetch
 constexpr uint32_t kVarSmemStack = 0x80u;  // top of the traversal stack in shared memory
-constexpr uint32_t kVarAll = 0xffu;        // every defined variant bit
+constexpr uint32_t kVarCompact = 0x100u;   // with kVarPersistent: trace only the unmasked rays, compacted first
+constexpr uint32_t kVarAll = 0x1ffu;       // every defined variant bit
 constexpr uint32_t kSortMinRays = 32768;   // smaller batches are traced in caller order
 
 lrx_status launch_trace(const TraceArgs &a, cudaStream_t stream);
@@ -174,6 +176,12 @@ lrx_status launch_trace_queue(const QueueParams &p, cudaStream_t stream);
 // Sorts the rays (octant, origin Morton code in [lo, hi]) and traces them in
 // that order; scratch from a stream-ordered pool.  Hits land in caller order.
 lrx_status launch_trace_sorted(const TraceArgs &a, const float lo[3], const float hi[3], cudaStream_t stream);
+
+// Compacts the indices of the rays without RAY_FLAGS_MASKED (stable) into
+// pool scratch and traces them with the persistent kernel, which reads the
+// compacted count on the device.  Masked rays are neither read by the
+// traversal nor written.
+lrx_status launch_trace_compacted(const TraceArgs &a, cudaStream_t stream);
 
 // One batch of a queue launch to reorder: its rays, count, the scene box and
 // the offset of its permutation in the launch's concatenated order array.

@@ -14,6 +14,8 @@
 #include <vector>
 
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_select.cuh>
+#include <thrust/iterator/counting_iterator.h>
 
 #include "lrx_common.cuh"
 #include "lrx_internal.h"
@@ -151,6 +153,45 @@ lrx_status sort_queue_batches(const std::vector<SortBatch> &batches, uint32_t to
 	}
 	*scratch = base;
 	return LRX_OK;
+}
+
+// Stable selection predicate: ray i is traced unless RAY_FLAGS_MASKED is set
+// (its flags word is the 10th of the 12-word record).
+struct RayUnmasked {
+	const uint32_t *words;
+	__device__ __forceinline__ bool operator()(uint32_t i) const {
+		return (__ldg(words + 12 * (size_t)i + 9) & LRX_RAY_FLAGS_MASKED) == 0u;
+	}
+};
+
+lrx_status launch_trace_compacted(const TraceArgs &a_in, cudaStream_t st) {
+	TraceArgs a = a_in;
+	const uint32_t n = a.count;
+	int dev = 0;
+	LRX_CUDA(cudaGetDevice(&dev));
+	cudaMemPool_t pool;
+	lrx_status rc = stream_pool(dev, &pool);
+	if (rc != LRX_OK) return rc;
+	const RayUnmasked pred{static_cast<const uint32_t *>(a.rays)};
+	thrust::counting_iterator<uint32_t> first(0u);
+	size_t temp_bytes = 0;
+	LRX_CUDA(cub::DeviceSelect::If(nullptr, temp_bytes, first, static_cast<uint32_t *>(nullptr),
+			static_cast<uint32_t *>(nullptr), (int)n, pred, st));
+	const size_t idx_bytes = ((sizeof(uint32_t) * (size_t)n + 255) / 256) * 256;
+	void *base = nullptr;
+	LRX_CUDA(cudaMallocFromPoolAsync(&base, idx_bytes + 256 + temp_bytes, pool, st));
+	unsigned char *p = static_cast<unsigned char *>(base);
+	uint32_t *idx = reinterpret_cast<uint32_t *>(p);
+	uint32_t *n_sel = reinterpret_cast<uint32_t *>(p + idx_bytes);
+	cudaError_t e = cub::DeviceSelect::If(p + idx_bytes + 256, temp_bytes, first, idx, n_sel, (int)n, pred, st);
+	if (e == cudaSuccess) {
+		a.order = idx;
+		a.count_dev = n_sel;
+		rc = launch_trace(a, st);
+	}
+	cudaFreeAsync(base, st);  // ordered after the trace on the same stream
+	if (e != cudaSuccess) return cuda_fail(e, "ray compaction");
+	return rc;
 }
 
 lrx_status launch_trace_sorted(const TraceArgs &a_in, const float lo[3], const float hi[3], cudaStream_t st) {

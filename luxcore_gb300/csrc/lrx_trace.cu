@@ -489,6 +489,7 @@ __global__ void __launch_bounds__(kTraceBlock, 8) k_trace_fetch(TraceArgs a, uin
 	Counts cnt{0, 0, 0, 0};
 	uint32_t rid = kNull;  // ray this lane traces (kNull: idle)
 	bool drained = false;  // warp-uniform: the counter has passed the batch
+	const uint32_t count = a.count_dev ? min(*a.count_dev, a.count) : a.count;  // rays to claim
 	for (;;) {
 		const uint32_t idle = __ballot_sync(0xffffffffu, rid == kNull);
 		const uint32_t nidle = __popc(idle);
@@ -497,10 +498,10 @@ __global__ void __launch_bounds__(kTraceBlock, 8) k_trace_fetch(TraceArgs a, uin
 			uint32_t base = 0;
 			if (lane == leader) base = atomicAdd(&slot[0], nidle);
 			base = __shfl_sync(0xffffffffu, base, leader);
-			drained = base + nidle >= a.count;
+			drained = base + nidle >= count;
 			if (rid == kNull) {
 				const uint32_t idx = base + __popc(idle & ((1u << lane) - 1u));
-				if (idx < a.count) {
+				if (idx < count) {
 					const uint32_t i = a.order ? a.order[idx] : idx;
 					const int k = ray_begin(a, i, stream, s);
 					if (k == kRayTraverse) rid = i;

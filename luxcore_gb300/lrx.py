@@ -33,6 +33,7 @@ LRX_VARIANT_SORT_RAYS = 0x10
 LRX_VARIANT_SORT_OCTANT = 0x20
 LRX_VARIANT_PERSISTENT = 0x40
 LRX_VARIANT_SMEM_STACK = 0x80
+LRX_VARIANT_COMPACT = 0x100
 
 STATUS_NAMES = {0: "LRX_OK", 1: "LRX_ERR_INVALID_ARGUMENT", 2: "LRX_ERR_CUDA", 3: "LRX_ERR_OUT_OF_MEMORY",
                 4: "LRX_ERR_BUILD", 5: "LRX_ERR_DEVICE", 6: "LRX_ERR_NOT_SUPPORTED", 7: "LRX_ERR_BUDGET",

@@ -26,12 +26,14 @@ SENT = 0xDEADBEEF
 KERNELS = pytest.mark.parametrize("kernel", [(128, 0, 0), (64, 8, 0), (256, 24, 0), (64, 8, 0xF), (128, 8, 0x7),
                                              (64, 8, 0x10), (32, 8, 0x1F), (64, 8, 0x30),
                                              (64, 8, 0x40), (128, 0, 0x41, 1), (32, 8, 0x46, 32),
-                                             (64, 8, 0x50, 8), (64, 8, 0xC0, 8), (256, 8, 0x80), (64, 8, 0x90)],
+                                             (64, 8, 0x50, 8), (64, 8, 0xC0, 8), (256, 8, 0x80), (64, 8, 0x90),
+                                             (64, 8, 0x140, 8)],
                                   ids=["b128", "b64-p8", "b256-p24", "b64-p8-allvariants", "b128-p8-mm3-hints",
                                        "b64-p8-sorted", "b32-p8-sorted-all", "b64-p8-octsort",
                                        "b64-p8-persistent", "b128-persistent-refill1",
                                        "b32-p8-persistent-refill32-hints", "b64-p8-sorted-persistent-refill8",
-                                       "b64-p8-persistent-smemstack", "b256-p8-smemstack", "b64-p8-sorted-smemstack"])
+                                       "b64-p8-persistent-smemstack", "b256-p8-smemstack", "b64-p8-sorted-smemstack",
+                                       "b64-p8-persistent-compact"])
 
 
 def make_scene(desc, kernel=(64, 8, 0), **kw):
@@ -420,3 +422,22 @@ def test_treelet_restructured_builds_keep_parity(torch_cuda, passes):
         o = po.OracleScene(tiny)
         ref, _ = o.intersect(r)
         assert_parity(gpu_trace(torch, s, r), ref, o, r)
+
+
+@pytest.mark.parametrize("masked_frac", [0.0, 0.5, 0.97, 1.0])
+def test_compaction_skips_masked_rays(torch_cuda, masked_frac):
+    """The compacting launch traces only unmasked rays: their hits equal the
+    plain launch's, masked rays' hit records stay untouched (all masked:
+    nothing is written)."""
+    torch = torch_cuda
+    scene, rays = W.config1(n_tris=20000, n_rays=60000, seed=801)
+    rng = np.random.default_rng(802)
+    rays["flags"][rng.random(rays.shape[0]) < masked_frac] = W.RAY_FLAGS_MASKED
+    plain = make_scene(scene, (64, 8, lrx.LRX_VARIANT_PERSISTENT, 8))
+    comp = make_scene(scene, (64, 8, lrx.LRX_VARIANT_PERSISTENT | lrx.LRX_VARIANT_COMPACT, 8))
+    for mode in (lrx.LRX_TRACE_CLOSEST, lrx.LRX_TRACE_ANY):
+        a = gpu_trace(torch, plain, rays, mode)
+        b = gpu_trace(torch, comp, rays, mode)
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+        masked = (rays["flags"] & W.RAY_FLAGS_MASKED) != 0
+        assert (b.view(np.uint32).reshape(-1, 5)[masked] == SENT).all()
