@@ -327,6 +327,46 @@ lrx_status lrx_trace_counted(lrx_scene *scene, const void *d_rays, void *d_hits,
  * word: 0 = no fault; bit 0 = traversal stack limit; bit 1 = visit limit. */
 lrx_status lrx_scene_device_status(lrx_scene *scene, uint32_t *status, void *stream);
 
+/* ---- Scene ingestion and the BVH blob cache ---------------------------- */
+
+/* A triangle mesh read from a file; vertices xyz per vertex, three indices
+ * per triangle -- directly usable as an lrx_mesh_desc.  Owned by the
+ * library until lrx_ply_free. */
+typedef struct lrx_ply_mesh {
+	float *vertices;
+	uint32_t *triangles;
+	uint32_t vertex_count;
+	uint32_t triangle_count;
+} lrx_ply_mesh;
+
+/* Reads the geometry of an ascii / binary little-endian / binary big-endian
+ * PLY file: vertex x, y, z (any numeric type, stored as float) and the face
+ * list "vertex_indices" -- triangles kept, quads split into (0,1,2) and
+ * (0,2,3), other polygons dropped.  No host CUDA call.
+ * Replaces: the geometry part of ExtTriangleMesh::LoadPly
+ * (src/luxrays/core/exttrianglemeshfile.cpp:207-290). */
+lrx_status lrx_ply_load(const char *path, lrx_ply_mesh *mesh);
+void lrx_ply_free(lrx_ply_mesh *mesh);
+
+/* 64-bit content key of a scene's inputs (geometry, objects, build options)
+ * for caching built scenes: equal inputs give equal keys.  No CUDA call. */
+lrx_status lrx_scene_key(const lrx_mesh_desc *meshes, uint32_t mesh_count,
+		const lrx_object_desc *objects, uint32_t object_count,
+		const lrx_build_opts *opts, uint64_t *key);
+
+/* Serialises a built scene -- its device node, triangle and instance arrays
+ * and the host metadata instance updates need -- into host memory.  Call
+ * with blob NULL to get the size in *bytes; then with a buffer of that size.
+ * Synchronises `stream`.  No reference counterpart (the reference rebuilds
+ * its accelerators). */
+lrx_status lrx_scene_save(const lrx_scene *scene, void *blob, size_t *bytes, void *stream);
+
+/* Creates a scene on the current device from a blob written by
+ * lrx_scene_save (checked: magic, version, sizes, checksum) without
+ * building: the arrays are uploaded as they are.  Traces equal the saved
+ * scene's bit for bit. */
+lrx_status lrx_scene_load(const void *blob, size_t bytes, void *stream, lrx_scene **out_scene);
+
 #ifdef __cplusplus
 }
 #endif

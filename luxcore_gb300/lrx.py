@@ -46,7 +46,8 @@ EXPORTED = ["lrx_abi_version", "lrx_last_error", "lrx_scene_create", "lrx_scene_
             "lrx_scene_set_trace_config", "lrx_scene_get_trace_config", "lrx_trace_batches",
             "lrx_scene_autotune", "lrx_trace_batches_ex", "lrx_server_create", "lrx_server_destroy",
             "lrx_server_add_scene",
-            "lrx_server_submit", "lrx_server_wait", "lrx_server_get_stats", "lrx_server_reset_stats"]
+            "lrx_server_submit", "lrx_server_wait", "lrx_server_get_stats", "lrx_server_reset_stats",
+            "lrx_ply_load", "lrx_ply_free", "lrx_scene_key", "lrx_scene_save", "lrx_scene_load"]
 LRX_SERVE_BATCHED = 0
 LRX_SERVE_PLAIN = 1
 LRX_NOALLOC_MAX_RAYS = 131072
@@ -77,6 +78,11 @@ class TraceConfig(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_uint32), ("block_size", ctypes.c_uint32),
                 ("postpone", ctypes.c_uint32), ("variant", ctypes.c_uint32), ("modes", ctypes.c_uint32),
                 ("refill", ctypes.c_uint32)]
+
+
+class PlyMesh(ctypes.Structure):
+    _fields_ = [("vertices", ctypes.POINTER(ctypes.c_float)), ("triangles", ctypes.POINTER(ctypes.c_uint32)),
+                ("vertex_count", ctypes.c_uint32), ("triangle_count", ctypes.c_uint32)]
 
 
 class SceneInfo(ctypes.Structure):
@@ -150,6 +156,16 @@ def load(path: str | None = None):
         L.lrx_trace_counted.argtypes = [vp, vp, vp, u32, u32, vp, vp]
         L.lrx_scene_device_status.restype = st
         L.lrx_scene_device_status.argtypes = [vp, ctypes.POINTER(u32), vp]
+        L.lrx_ply_load.restype = st
+        L.lrx_ply_load.argtypes = [ctypes.c_char_p, ctypes.POINTER(PlyMesh)]
+        L.lrx_ply_free.restype = None
+        L.lrx_ply_free.argtypes = [ctypes.POINTER(PlyMesh)]
+        L.lrx_scene_key.restype = st
+        L.lrx_scene_key.argtypes = [vp, u32, vp, u32, vp, ctypes.POINTER(u64)]
+        L.lrx_scene_save.restype = st
+        L.lrx_scene_save.argtypes = [vp, vp, ctypes.POINTER(ctypes.c_size_t), vp]
+        L.lrx_scene_load.restype = st
+        L.lrx_scene_load.argtypes = [vp, ctypes.c_size_t, vp, ctypes.POINTER(vp)]
         _lib = L
         return L
 
@@ -281,21 +297,56 @@ def _object_array(scene: W.SceneDesc):
     return objs
 
 
+def ply_load(path: str) -> W.Mesh:
+    """lrx_ply_load: the geometry of a PLY file as a Mesh."""
+    L = load()
+    pm = PlyMesh()
+    check(L.lrx_ply_load(os.fsencode(path), ctypes.byref(pm)))
+    try:
+        v = np.ctypeslib.as_array(pm.vertices, shape=(pm.vertex_count, 3)).copy()
+        t = np.ctypeslib.as_array(pm.triangles, shape=(pm.triangle_count, 3)).copy()
+    finally:
+        L.lrx_ply_free(ctypes.byref(pm))
+    return W.Mesh(v, t)
+
+
+def _mesh_descs(scene: W.SceneDesc, keep: list):
+    meshes = (MeshDesc * max(1, len(scene.meshes)))()
+    for i, m in enumerate(scene.meshes):
+        v = np.ascontiguousarray(m.vertices, np.float32)
+        t = np.ascontiguousarray(m.triangles, np.uint32)
+        keep += [v, t]
+        meshes[i].vertices = v.ctypes.data
+        meshes[i].triangles = t.ctypes.data
+        meshes[i].vertex_count = v.shape[0]
+        meshes[i].triangle_count = t.shape[0]
+    return meshes
+
+
+def scene_key(scene: W.SceneDesc, leaf_max: int = 3, treelet_passes: int = 2) -> int:
+    """lrx_scene_key: content key of a scene's inputs and build options."""
+    keep = []
+    meshes = _mesh_descs(scene, keep)
+    objs = _object_array(scene)
+    opts = BuildOpts(ctypes.sizeof(BuildOpts), leaf_max, treelet_passes, 0)
+    k = ctypes.c_uint64()
+    check(load().lrx_scene_key(meshes, len(scene.meshes), objs, len(scene.objects), ctypes.byref(opts),
+                               ctypes.byref(k)))
+    return k.value
+
+
 class Scene:
     """A device-resident scene (lrx_scene): meshes + objects of a SceneDesc."""
 
-    def __init__(self, scene: W.SceneDesc, stream: int = 0, leaf_max: int = 3, treelet_passes: int = 2):
+    def __init__(self, scene: W.SceneDesc | None, stream: int = 0, leaf_max: int = 3, treelet_passes: int = 2,
+                 _handle=None):
         L = load()
+        if _handle is not None:  # from_blob
+            self.handle = _handle
+            self.desc = scene
+            return
         self._keep = []
-        meshes = (MeshDesc * max(1, len(scene.meshes)))()
-        for i, m in enumerate(scene.meshes):
-            v = np.ascontiguousarray(m.vertices, np.float32)
-            t = np.ascontiguousarray(m.triangles, np.uint32)
-            self._keep += [v, t]
-            meshes[i].vertices = v.ctypes.data
-            meshes[i].triangles = t.ctypes.data
-            meshes[i].vertex_count = v.shape[0]
-            meshes[i].triangle_count = t.shape[0]
+        meshes = _mesh_descs(scene, self._keep)
         objs = _object_array(scene)
         opts = BuildOpts(ctypes.sizeof(BuildOpts), leaf_max, treelet_passes, 0)
         h = ctypes.c_void_p()
@@ -315,6 +366,23 @@ class Scene:
             self.close()
         except Exception:
             pass
+
+    def save(self, stream: int = 0) -> bytes:
+        """lrx_scene_save: the built scene as a blob."""
+        L = load()
+        n = ctypes.c_size_t(0)
+        check(L.lrx_scene_save(self.handle, None, ctypes.byref(n), ctypes.c_void_p(stream)))
+        buf = ctypes.create_string_buffer(n.value)
+        check(L.lrx_scene_save(self.handle, buf, ctypes.byref(n), ctypes.c_void_p(stream)))
+        return buf.raw[:n.value]
+
+    @classmethod
+    def from_blob(cls, blob: bytes, stream: int = 0, desc: W.SceneDesc | None = None) -> "Scene":
+        """lrx_scene_load: a scene from a blob of lrx_scene_save, without a build."""
+        h = ctypes.c_void_p()
+        buf = ctypes.create_string_buffer(bytes(blob), len(blob))
+        check(load().lrx_scene_load(buf, len(blob), ctypes.c_void_p(stream), ctypes.byref(h)))
+        return cls(desc, _handle=h)
 
     def info(self) -> dict:
         inf = SceneInfo()

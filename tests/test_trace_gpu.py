@@ -441,3 +441,41 @@ def test_compaction_skips_masked_rays(torch_cuda, masked_frac):
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
         masked = (rays["flags"] & W.RAY_FLAGS_MASKED) != 0
         assert (b.view(np.uint32).reshape(-1, 5)[masked] == SENT).all()
+
+
+def test_scene_blob_round_trip(torch_cuda):
+    """lrx_scene_save / lrx_scene_load: a loaded scene traces bit-for-bit like
+    the saved one (flat and two-level, both modes), keeps its trace configs
+    and takes instance updates; corrupt or truncated blobs are rejected."""
+    torch = torch_cuda
+    flat, rays = W.config1(n_tris=20000, n_rays=30000, seed=901)
+    inst, closest, anyr = W.config3(n_rays=1 << 14, n_meshes=3, freq=10, n_inst=120, extent=3.0, scale=(0.1, 0.4))
+    for desc, r in ((flat, rays), (inst, closest)):
+        a = lrx.Scene(desc)
+        a.set_trace_config(128, 0, lrx.LRX_VARIANT_PERSISTENT, modes=1, refill=4)
+        blob = a.save()
+        b = lrx.Scene.from_blob(blob, desc=desc)
+        assert b.trace_config(lrx.LRX_TRACE_CLOSEST) == a.trace_config(lrx.LRX_TRACE_CLOSEST)
+        ia, ib = a.info(), b.info()
+        assert {k: ia[k] for k in ia if k != "build_ms"} == {k: ib[k] for k in ib if k != "build_ms"}
+        for mode in (lrx.LRX_TRACE_CLOSEST, lrx.LRX_TRACE_ANY):
+            ha, hb = gpu_trace(torch, a, r, mode), gpu_trace(torch, b, r, mode)
+            assert np.array_equal(ha.view(np.uint32), hb.view(np.uint32))
+        for bad in (blob[:-1], blob[:30], blob[:100] + bytes([blob[100] ^ 1]) + blob[101:], b"x" * 64):
+            with pytest.raises(lrx.LrxError):
+                lrx.Scene.from_blob(bad)
+    # instance update on the loaded scene equals the update on the original
+    rng = np.random.default_rng(902)
+    moved = []
+    for mi, m in inst.objects:
+        m2 = m.copy()
+        m2[:3, 3] += rng.uniform(-0.2, 0.2, 3).astype(np.float32)
+        moved.append((mi, m2))
+    moved = W.SceneDesc(inst.meshes, moved)
+    a = lrx.Scene(inst)
+    b = lrx.Scene.from_blob(a.save(), desc=inst)
+    a.update_instances(moved)
+    b.update_instances(moved)
+    for mode in (lrx.LRX_TRACE_CLOSEST, lrx.LRX_TRACE_ANY):
+        ha, hb = gpu_trace(torch, a, anyr, mode), gpu_trace(torch, b, anyr, mode)
+        assert np.array_equal(ha.view(np.uint32), hb.view(np.uint32))
