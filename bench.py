@@ -898,8 +898,9 @@ def run_serving(args):
         sess = g.integers(0, n_sess, t.size)
         return list(zip(t.tolist(), sess.tolist(), sizes.tolist()))
 
-    def one_run(policy, budget, rate):
-        server = lrx.Server(policy=policy, budget_bytes=budget, streams=args.serve_streams)
+    def one_run(policy, budget, rate, cache=True):
+        server = lrx.Server(policy=policy, budget_bytes=budget, streams=args.serve_streams,
+                            host_cache_bytes=0 if cache else 2 ** 64 - 1)
         ids = [server.add_scene(d) for d in descs]
         if not budget or budget >= (150 << 30):
             for k in range(len(descs)):  # make every scene resident before the clock starts
@@ -946,6 +947,7 @@ def run_serving(args):
                 "Mrays_per_s": round(st["rays_done"] / max(wall, 1e-9) / 1e6, 1),
                 "wall_s": round(wall, 3), "launches": st["launches"], "failed": st["requests_failed"],
                 "builds": st["scene_builds"], "evictions": st["scene_evictions"],
+                "reloads_from_blob_cache": st["scene_reloads"],
                 "peak_resident_GB": round(st["peak_resident_bytes"] / 2 ** 30, 3)}
 
     full = 150 << 30
@@ -956,13 +958,15 @@ def run_serving(args):
     # scaled budget: ~40 % of the scene bytes, so scenes are evicted and rebuilt
     probe_total, probe_max = 0, 0
     for d in descs:
-        s = lrx.Scene(d)
+        s = lrx.Scene(d, treelet_passes=0)  # as the server builds
         probe_total += s.info()["device_bytes"]
         probe_max = max(probe_max, s.info()["device_bytes"])
         s.close()
     small = int(max(probe_total * 0.4, probe_max * 1.25))  # the largest scene must still fit
     low_rate = min(args.serve_rates)
     res[f"batched@{low_rate}-budget40pct"] = one_run(lrx.LRX_SERVE_BATCHED, small, low_rate)
+    res[f"batched@{low_rate}-budget40pct-no-blob-cache"] = one_run(lrx.LRX_SERVE_BATCHED, small, low_rate,
+                                                                   cache=False)
     head = res[f"batched@{args.serve_rates[0]}"]
     plain = res[f"plain@{args.serve_rates[0]}"]
     line = {

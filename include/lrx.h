@@ -258,6 +258,9 @@ typedef struct lrx_server_opts {
 	uint64_t budget_bytes;     /* device memory for resident scenes (0 = unlimited) */
 	uint32_t streams;          /* concurrent launches in flight (0 = 4) */
 	uint32_t max_requests_per_launch;  /* (0 = 384) */
+	uint64_t host_cache_bytes; /* host memory for blobs of evicted scenes, reloaded instead of rebuilt
+	                              (0 = 16 GiB; UINT64_MAX = no cache).  Added in ABI 2: the 24-byte
+	                              ABI 1 struct is accepted and gets the default */
 } lrx_server_opts;
 
 typedef struct lrx_server_stats {
@@ -268,6 +271,8 @@ typedef struct lrx_server_stats {
 	uint64_t launches;
 	double latency_p50_us, latency_p99_us, latency_mean_us, latency_max_us;
 	double busy_seconds;       /* wall time from the first submit to the last completion */
+	uint64_t scene_reloads;    /* admissions served from the blob cache instead of a build (ABI 2) */
+	uint64_t host_cache_bytes; /* blobs held (ABI 2) */
 } lrx_server_stats;
 
 lrx_status lrx_server_create(const lrx_server_opts *opts, lrx_server **out_server);

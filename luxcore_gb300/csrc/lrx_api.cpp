@@ -749,11 +749,11 @@ lrx_status lrx_scene_key(const lrx_mesh_desc *meshes, uint32_t mesh_count, const
 	return LRX_OK;
 }
 
-// Blob layout: magic, version, checksum of the rest, then the host metadata
-// and the three device arrays.
+// Blob layout: magic, version, checksum of everything after it, the host
+// metadata, then the node, triangle and instance arrays (each a u64 byte
+// count and the bytes), copied straight between the blob and device memory.
 extern "C++" {
-static void write_blob(const lrx_scene *s, BlobWriter &w, const std::vector<unsigned char> &nodes,
-		const std::vector<unsigned char> &tris, const std::vector<unsigned char> &insts) {
+static void write_meta(const lrx_scene *s, BlobWriter &w) {
 	w.value((uint32_t)(s->two_level ? 1u : 0u));
 	w.value(s->root);
 	w.vec(s->blas);
@@ -770,11 +770,14 @@ static void write_blob(const lrx_scene *s, BlobWriter &w, const std::vector<unsi
 	w.value(s->info);
 	w.value(s->bounds_lo);
 	w.value(s->bounds_hi);
-	w.vec(nodes);
-	w.vec(tris);
-	w.vec(insts);
 }
 }  // extern "C++"
+
+static size_t blob_size(const lrx_scene *s) {
+	BlobWriter w{nullptr};
+	write_meta(s, w);
+	return 20 + w.n + 3 * 8 + s->nodes.bytes + s->tris.bytes + s->insts.bytes;
+}
 
 lrx_status lrx_scene_save(const lrx_scene *s_, void *blob, size_t *bytes, void *stream) {
 	if (!s_ || !bytes) {
@@ -783,61 +786,40 @@ lrx_status lrx_scene_save(const lrx_scene *s_, void *blob, size_t *bytes, void *
 	}
 	lrx_scene *s = const_cast<lrx_scene *>(s_);
 	std::lock_guard<std::mutex> lk(s->mu);
-	DeviceGuard g(s->device);
-	cudaStream_t st = (cudaStream_t)stream;
-	try {
-		std::vector<unsigned char> nodes, tris, insts;
-		if (blob) {
-			nodes.resize(s->nodes.bytes);
-			tris.resize(s->tris.bytes);
-			insts.resize(s->insts.bytes);
-			if (s->nodes.bytes) LRX_CUDA(cudaMemcpyAsync(nodes.data(), s->nodes.ptr, s->nodes.bytes, cudaMemcpyDeviceToHost, st));
-			if (s->tris.bytes) LRX_CUDA(cudaMemcpyAsync(tris.data(), s->tris.ptr, s->tris.bytes, cudaMemcpyDeviceToHost, st));
-			if (s->insts.bytes) LRX_CUDA(cudaMemcpyAsync(insts.data(), s->insts.ptr, s->insts.bytes, cudaMemcpyDeviceToHost, st));
-			LRX_CUDA(cudaStreamSynchronize(st));
-		}
-		BlobWriter count{nullptr};  // sizes only: the metadata with empty arrays, plus the array bytes
-		count.bytes(kBlobMagic, 8);
-		count.value(kBlobVersion);
-		count.value((uint64_t)0);
-		{
-			BlobWriter body{nullptr};
-			std::vector<unsigned char> n0, t0, i0;
-			write_blob(s, body, n0, t0, i0);
-			count.n += body.n + s->nodes.bytes + s->tris.bytes + s->insts.bytes;
-		}
-		if (!blob) {
-			*bytes = count.n;
-			return LRX_OK;
-		}
-		if (*bytes < count.n) {
-			set_error("lrx_scene_save: buffer too small (" + std::to_string(count.n) + " bytes needed)");
-			*bytes = count.n;
-			return LRX_ERR_INVALID_ARGUMENT;
-		}
-		unsigned char *out = static_cast<unsigned char *>(blob);
-		BlobWriter w{out};
-		w.bytes(kBlobMagic, 8);
-		w.value(kBlobVersion);
-		const size_t sum_at = w.n;
-		w.value((uint64_t)0);
-		write_blob(s, w, nodes, tris, insts);
-		Hash64 h;
-		h.words(out + sum_at + 8, w.n - sum_at - 8);
-		std::memcpy(out + sum_at, &h.h, 8);
-		*bytes = w.n;
+	const size_t need = blob_size(s);
+	if (!blob) {
+		*bytes = need;
 		return LRX_OK;
-	} catch (const std::bad_alloc &) {
-		set_error("lrx_scene_save: host allocation failed");
-		return LRX_ERR_OUT_OF_MEMORY;
 	}
-}
-
-lrx_status lrx_scene_load(const void *blob, size_t bytes, void *stream, lrx_scene **out_scene) {
-	if (!blob || !out_scene) {
-		set_error("lrx_scene_load: null argument");
+	if (*bytes < need) {
+		set_error("lrx_scene_save: buffer too small (" + std::to_string(need) + " bytes needed)");
+		*bytes = need;
 		return LRX_ERR_INVALID_ARGUMENT;
 	}
+	DeviceGuard g(s->device);
+	cudaStream_t st = (cudaStream_t)stream;
+	unsigned char *out = static_cast<unsigned char *>(blob);
+	BlobWriter w{out};
+	w.bytes(kBlobMagic, 8);
+	w.value(kBlobVersion);
+	w.value((uint64_t)0);  // checksum, below
+	write_meta(s, w);
+	for (const DevBuf *d : {&s->nodes, &s->tris, &s->insts}) {
+		w.value((uint64_t)d->bytes);
+		if (d->bytes) LRX_CUDA(cudaMemcpyAsync(out + w.n, d->ptr, d->bytes, cudaMemcpyDeviceToHost, st));
+		w.n += d->bytes;
+	}
+	LRX_CUDA(cudaStreamSynchronize(st));
+	Hash64 h;
+	h.words(out + 20, w.n - 20);
+	std::memcpy(out + 12, &h.h, 8);
+	*bytes = w.n;
+	return LRX_OK;
+}
+
+// Creates a scene from a blob; verify = false skips the checksum (the
+// server's own cache of blobs it wrote).
+static lrx_status scene_from_blob(const void *blob, size_t bytes, cudaStream_t st, bool verify, lrx_scene **out_scene) {
 	*out_scene = nullptr;
 	const unsigned char *b = static_cast<const unsigned char *>(blob);
 	if (bytes < 20 || std::memcmp(b, kBlobMagic, 8) != 0) {
@@ -852,15 +834,16 @@ lrx_status lrx_scene_load(const void *blob, size_t bytes, void *stream, lrx_scen
 		set_error("lrx_scene_load: blob version " + std::to_string(version) + " is not supported");
 		return LRX_ERR_NOT_SUPPORTED;
 	}
-	Hash64 h;
-	h.words(b + 20, bytes - 20);
-	if (h.h != sum) {
-		set_error("lrx_scene_load: checksum mismatch (corrupt or truncated blob)");
-		return LRX_ERR_INVALID_ARGUMENT;
+	if (verify) {
+		Hash64 h;
+		h.words(b + 20, bytes - 20);
+		if (h.h != sum) {
+			set_error("lrx_scene_load: checksum mismatch (corrupt or truncated blob)");
+			return LRX_ERR_INVALID_ARGUMENT;
+		}
 	}
 	int dev = 0;
 	LRX_CUDA(cudaGetDevice(&dev));
-	cudaStream_t st = (cudaStream_t)stream;
 	try {
 		lrx_scene *s = new lrx_scene();
 		std::unique_ptr<lrx_scene> guard(s);
@@ -883,25 +866,27 @@ lrx_status lrx_scene_load(const void *blob, size_t bytes, void *stream, lrx_scen
 		s->info = r.value<lrx_scene_info>();
 		for (int c = 0; c < 3; ++c) s->bounds_lo[c] = r.value<float>();
 		for (int c = 0; c < 3; ++c) s->bounds_hi[c] = r.value<float>();
-		std::vector<unsigned char> nodes, tris, insts;
-		r.vec(nodes, lim);
-		r.vec(tris, lim);
-		r.vec(insts, lim);
-		if (!r.ok || r.n != r.size || nodes.size() % sizeof(WideNode) || tris.size() % sizeof(TriRecord) ||
-				insts.size() % sizeof(InstRecord) || s->obj_blas.size() != s->obj_flags.size() ||
-				(s->root != kNull && (uint64_t)s->root * sizeof(WideNode) >= nodes.size())) {
+		const unsigned char *arr[3];
+		uint64_t len[3];
+		for (int k = 0; k < 3; ++k) {
+			len[k] = r.value<uint64_t>();
+			arr[k] = r.take(len[k]);
+		}
+		if (!r.ok || r.n != r.size || len[0] % sizeof(WideNode) || len[1] % sizeof(TriRecord) ||
+				len[2] % sizeof(InstRecord) || s->obj_blas.size() != s->obj_flags.size() ||
+				(s->root != kNull && (uint64_t)s->root * sizeof(WideNode) >= len[0])) {
 			set_error("lrx_scene_load: malformed blob");
 			return LRX_ERR_INVALID_ARGUMENT;
 		}
 		lrx_status rc;
-		if ((rc = s->nodes.alloc(std::max<size_t>(nodes.size(), sizeof(WideNode)))) != LRX_OK) return rc;
-		if ((rc = s->tris.alloc(std::max<size_t>(tris.size(), sizeof(TriRecord)))) != LRX_OK) return rc;
-		if (!insts.empty() && (rc = s->insts.alloc(insts.size())) != LRX_OK) return rc;
+		if ((rc = s->nodes.alloc(std::max<size_t>(len[0], sizeof(WideNode)))) != LRX_OK) return rc;
+		if ((rc = s->tris.alloc(std::max<size_t>(len[1], sizeof(TriRecord)))) != LRX_OK) return rc;
+		if (len[2] && (rc = s->insts.alloc(len[2])) != LRX_OK) return rc;
 		if ((rc = s->status.alloc(64)) != LRX_OK) return rc;
 		LRX_CUDA(cudaMemsetAsync(s->status.ptr, 0, 64, st));
-		if (!nodes.empty()) LRX_CUDA(cudaMemcpyAsync(s->nodes.ptr, nodes.data(), nodes.size(), cudaMemcpyHostToDevice, st));
-		if (!tris.empty()) LRX_CUDA(cudaMemcpyAsync(s->tris.ptr, tris.data(), tris.size(), cudaMemcpyHostToDevice, st));
-		if (!insts.empty()) LRX_CUDA(cudaMemcpyAsync(s->insts.ptr, insts.data(), insts.size(), cudaMemcpyHostToDevice, st));
+		DevBuf *dst[3] = {&s->nodes, &s->tris, &s->insts};
+		for (int k = 0; k < 3; ++k)
+			if (len[k]) LRX_CUDA(cudaMemcpyAsync(dst[k]->ptr, arr[k], len[k], cudaMemcpyHostToDevice, st));
 		LRX_CUDA(cudaStreamSynchronize(st));
 		s->info.device_bytes = s->nodes.bytes + s->tris.bytes + s->insts.bytes + s->status.bytes;
 		*out_scene = guard.release();
@@ -910,6 +895,19 @@ lrx_status lrx_scene_load(const void *blob, size_t bytes, void *stream, lrx_scen
 		set_error("lrx_scene_load: host allocation failed");
 		return LRX_ERR_OUT_OF_MEMORY;
 	}
+}
+
+lrx_status lrx_scene_load(const void *blob, size_t bytes, void *stream, lrx_scene **out_scene) {
+	if (!blob || !out_scene) {
+		set_error("lrx_scene_load: null argument");
+		return LRX_ERR_INVALID_ARGUMENT;
+	}
+	return scene_from_blob(blob, bytes, (cudaStream_t)stream, true, out_scene);
+}
+
+extern "C++" lrx_status lrx::scene_load_trusted(const void *blob, size_t bytes, cudaStream_t stream,
+		lrx_scene **out_scene) {
+	return scene_from_blob(blob, bytes, stream, false, out_scene);
 }
 
 // A correct walk visits each node at most once per BLAS entry, so a ray never

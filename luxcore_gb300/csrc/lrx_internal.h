@@ -201,4 +201,8 @@ lrx_status sort_queue_batches(const std::vector<SortBatch> &batches, uint32_t to
 // CUDA device a scene was built on.
 int scene_device(const lrx_scene *scene);
 
+// lrx_scene_load without the checksum pass, for blobs the library wrote and
+// kept in its own memory (the server's cache of evicted scenes).
+lrx_status scene_load_trusted(const void *blob, size_t bytes, cudaStream_t stream, lrx_scene **out_scene);
+
 }  // namespace lrx

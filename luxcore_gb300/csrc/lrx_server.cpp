@@ -15,6 +15,7 @@
 #include <atomic>
 #include <chrono>
 #include <condition_variable>
+#include <cstddef>
 #include <cstring>
 #include <deque>
 #include <memory>
@@ -41,6 +42,7 @@ struct SceneEntry {
 	uint64_t est_bytes = 0;                     // estimate until built, then exact
 	bool exact = false;                         // est_bytes is a measured size
 	lrx_scene *scene = nullptr;                 // resident when not null
+	std::vector<unsigned char> blob;            // the built scene, kept on eviction (lrx_scene_save)
 	uint64_t bytes = 0;
 	uint64_t last_used = 0;
 	uint32_t inflight = 0;                      // requests of this scene on the GPU
@@ -100,7 +102,8 @@ struct lrx_server {
 	std::thread worker;
 	// statistics (under mu)
 	std::vector<double> lat_us;
-	uint64_t done_req = 0, done_rays = 0, failed = 0, builds = 0, evictions = 0, launches = 0;
+	uint64_t done_req = 0, done_rays = 0, failed = 0, builds = 0, evictions = 0, launches = 0, reloads = 0;
+	uint64_t cache_bytes = 0;  // blob bytes held
 	uint64_t resident = 0, peak_resident = 0;
 	bool any_submit = false;
 	Clock::time_point first_submit, last_done;
@@ -110,6 +113,7 @@ struct lrx_server {
 	bool launch_one(std::unique_lock<std::mutex> &lk);
 	void finish(const Request &r, lrx_status st, const std::string &err);
 	bool make_room(uint64_t need, const std::vector<uint32_t> &pinned);
+	void keep_blob(SceneEntry *e);
 	lrx_status make_resident(std::unique_lock<std::mutex> &lk, uint32_t id, const std::vector<uint32_t> &pinned);
 };
 
@@ -130,6 +134,34 @@ void lrx_server::finish(const Request &r, lrx_status st, const std::string &err)
 	}
 }
 
+// Keeps an evicted scene's built arrays as a blob in host memory (mu held)
+// so its next admission is an upload, not a build; within host_cache_bytes,
+// dropping the blobs of the least recently used scenes first.  A scene that
+// alone exceeds the cache is not kept.
+void lrx_server::keep_blob(SceneEntry *e) {
+	if (!e->blob.empty() || opts.host_cache_bytes == UINT64_MAX) return;
+	size_t n = 0;
+	if (lrx_scene_save(e->scene, nullptr, &n, build_stream) != LRX_OK || n > opts.host_cache_bytes) return;
+	while (cache_bytes + n > opts.host_cache_bytes) {
+		SceneEntry *old = nullptr;
+		for (auto &p : scenes)
+			if (!p->blob.empty() && (!old || p->last_used < old->last_used)) old = p.get();
+		if (!old) break;
+		cache_bytes -= old->blob.size();
+		std::vector<unsigned char>().swap(old->blob);
+	}
+	try {
+		e->blob.resize(n);
+	} catch (const std::bad_alloc &) {
+		return;
+	}
+	if (lrx_scene_save(e->scene, e->blob.data(), &n, build_stream) != LRX_OK) {
+		std::vector<unsigned char>().swap(e->blob);
+		return;
+	}
+	cache_bytes += e->blob.size();
+}
+
 // Evicts least-recently-used resident scenes with nothing in flight (and not
 // in `pinned`) until `need` more bytes fit the budget (mu held).
 bool lrx_server::make_room(uint64_t need, const std::vector<uint32_t> &pinned) {
@@ -142,6 +174,7 @@ bool lrx_server::make_room(uint64_t need, const std::vector<uint32_t> &pinned) {
 			if (!victim || e->last_used < victim->last_used) victim = e;
 		}
 		if (!victim) return false;
+		keep_blob(victim);
 		lrx_scene_destroy(victim->scene);
 		victim->scene = nullptr;
 		resident -= victim->bytes;
@@ -165,15 +198,21 @@ lrx_status lrx_server::make_resident(std::unique_lock<std::mutex> &lk, uint32_t 
 	if (!make_room(need, pinned)) return LRX_ERR_BUSY;
 	lk.unlock();
 	lrx_scene *sc = nullptr;
-	// Admission builds the plain LBVH (no treelet passes): a scene evicted
-	// under the budget is rebuilt on its next request, and that build is on
-	// the request's latency.
-	lrx_build_opts bo{};
-	bo.struct_size = sizeof(bo);
-	bo.leaf_max = 3;
-	bo.treelet_passes = 0;
-	lrx_status rc = lrx_scene_create(e->meshes.data(), (uint32_t)e->meshes.size(),
-			e->has_objects ? e->objects.data() : nullptr, (uint32_t)e->objects.size(), &bo, build_stream, &sc);
+	lrx_status rc;
+	const bool reload = !e->blob.empty();
+	if (reload) {
+		// an evicted scene comes back from its blob: one upload, no build
+		rc = lrx::scene_load_trusted(e->blob.data(), e->blob.size(), build_stream, &sc);
+	} else {
+		// Admission builds the plain LBVH (no treelet passes): the first
+		// build is on the first request's latency.
+		lrx_build_opts bo{};
+		bo.struct_size = sizeof(bo);
+		bo.leaf_max = 3;
+		bo.treelet_passes = 0;
+		rc = lrx_scene_create(e->meshes.data(), (uint32_t)e->meshes.size(),
+				e->has_objects ? e->objects.data() : nullptr, (uint32_t)e->objects.size(), &bo, build_stream, &sc);
+	}
 	lrx_scene_info info{};
 	if (rc == LRX_OK) lrx_scene_get_info(sc, &info);
 	lk.lock();
@@ -188,7 +227,8 @@ lrx_status lrx_server::make_resident(std::unique_lock<std::mutex> &lk, uint32_t 
 	e->bytes = info.device_bytes;
 	resident += e->bytes;
 	peak_resident = std::max(peak_resident, resident);
-	++builds;
+	if (reload) ++reloads;
+	else ++builds;
 	return LRX_OK;
 }
 
@@ -368,11 +408,15 @@ lrx_status lrx_server_create(const lrx_server_opts *opts, lrx_server **out) {
 		s->opts.policy = LRX_SERVE_BATCHED;
 		s->opts.streams = 4;
 		s->opts.max_requests_per_launch = 384;
+		s->opts.host_cache_bytes = 16ull << 30;
 		if (opts) {
-			if (opts->struct_size < sizeof(lrx_server_opts) || opts->policy > LRX_SERVE_PLAIN || opts->streams > 64) {
+			if (opts->struct_size < offsetof(lrx_server_opts, host_cache_bytes) || opts->policy > LRX_SERVE_PLAIN ||
+					opts->streams > 64) {
 				lrx::set_error("lrx_server_create: bad options");
 				return LRX_ERR_INVALID_ARGUMENT;
 			}
+			if (opts->struct_size >= sizeof(lrx_server_opts) && opts->host_cache_bytes)
+				s->opts.host_cache_bytes = opts->host_cache_bytes;
 			s->opts.policy = opts->policy;
 			s->opts.budget_bytes = opts->budget_bytes;
 			if (opts->streams) s->opts.streams = opts->streams;
@@ -542,6 +586,8 @@ lrx_status lrx_server_get_stats(lrx_server *s, lrx_server_stats *out) {
 	r.latency_max_us = mx;
 	r.busy_seconds = (s->any_submit && s->done_req)
 			? std::chrono::duration<double>(s->last_done - s->first_submit).count() : 0.0;
+	r.scene_reloads = s->reloads;
+	r.host_cache_bytes = s->cache_bytes;
 	*out = r;
 	return LRX_OK;
 }
@@ -553,7 +599,7 @@ lrx_status lrx_server_reset_stats(lrx_server *s) {
 	}
 	std::lock_guard<std::mutex> lk(s->mu);
 	s->lat_us.clear();
-	s->done_req = s->done_rays = s->failed = s->builds = s->evictions = s->launches = 0;
+	s->done_req = s->done_rays = s->failed = s->builds = s->evictions = s->launches = s->reloads = 0;
 	s->peak_resident = s->resident;
 	s->any_submit = false;
 	return LRX_OK;

@@ -202,7 +202,8 @@ def trace_batches(batches, stream: int = 0, arr=None):
 
 class ServerOpts(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_uint32), ("policy", ctypes.c_uint32), ("budget_bytes", ctypes.c_uint64),
-                ("streams", ctypes.c_uint32), ("max_requests_per_launch", ctypes.c_uint32)]
+                ("streams", ctypes.c_uint32), ("max_requests_per_launch", ctypes.c_uint32),
+                ("host_cache_bytes", ctypes.c_uint64)]
 
 
 class ServerStats(ctypes.Structure):
@@ -212,7 +213,8 @@ class ServerStats(ctypes.Structure):
                 ("peak_resident_bytes", ctypes.c_uint64), ("launches", ctypes.c_uint64),
                 ("latency_p50_us", ctypes.c_double), ("latency_p99_us", ctypes.c_double),
                 ("latency_mean_us", ctypes.c_double), ("latency_max_us", ctypes.c_double),
-                ("busy_seconds", ctypes.c_double)]
+                ("busy_seconds", ctypes.c_double), ("scene_reloads", ctypes.c_uint64),
+                ("host_cache_bytes", ctypes.c_uint64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -238,8 +240,11 @@ class Server:
     launch per request (LRX_SERVE_PLAIN)."""
 
     def __init__(self, policy: int = LRX_SERVE_BATCHED, budget_bytes: int = 0, streams: int = 0,
-                 max_requests_per_launch: int = 0):
-        o = ServerOpts(ctypes.sizeof(ServerOpts), policy, budget_bytes, streams, max_requests_per_launch)
+                 max_requests_per_launch: int = 0, host_cache_bytes: int = 0):
+        """host_cache_bytes: blobs of evicted scenes (0 = library default,
+        2**64 - 1 = no cache)."""
+        o = ServerOpts(ctypes.sizeof(ServerOpts), policy, budget_bytes, streams, max_requests_per_launch,
+                       host_cache_bytes)
         h = ctypes.c_void_p()
         check(load().lrx_server_create(ctypes.byref(o), ctypes.byref(h)))
         self.handle = h

@@ -99,7 +99,10 @@ def test_results_same_alone_and_in_the_mix(torch_cuda, policy):
     server.close()
 
 
-def test_lru_eviction_under_a_tight_budget(torch_cuda):
+@pytest.mark.parametrize("cache", [True, False], ids=["blob-cache", "rebuild"])
+def test_lru_eviction_under_a_tight_budget(torch_cuda, cache):
+    """Scenes are evicted (LRU) and brought back -- from the host blob cache,
+    or rebuilt without it -- with unchanged results."""
     torch = torch_cuda
     descs = scene_set()
     probe = [lrx.Scene(d, treelet_passes=0) for d in descs]  # the server's build
@@ -109,15 +112,20 @@ def test_lru_eviction_under_a_tight_budget(torch_cuda):
     budget = max(sizes) + min(sizes) // 2                    # one scene at a time, roughly
     reqs = make_requests(torch, len(descs), 40, 12)
     ref = alone_results(torch, descs, reqs)
-    server = lrx.Server(budget_bytes=budget, streams=2)
+    server = lrx.Server(budget_bytes=budget, streams=2, host_cache_bytes=0 if cache else 2**64 - 1)
     ids = [server.add_scene(d) for d in descs]
     got = []
-    for r in reqs:                                           # scene changes force rebuilds
+    for r in reqs:                                           # scene changes force evictions
         got += serve_all(server, ids, [r])
     for k, (a, b) in enumerate(zip(ref, got)):
         assert np.array_equal(a, b), k
     st = server.stats()
-    assert st["scene_evictions"] > 0 and st["scene_builds"] > len(descs)
+    assert st["scene_evictions"] > 0
+    if cache:   # each scene built once, then reloaded from its blob
+        assert st["scene_builds"] == len(set(r[0] for r in reqs)) and st["scene_reloads"] > 0
+        assert st["host_cache_bytes"] > 0
+    else:
+        assert st["scene_builds"] > len(descs) and st["scene_reloads"] == 0
     assert st["peak_resident_bytes"] <= budget + max(sizes)
     server.close()
 
