@@ -398,8 +398,8 @@ def run_lrx(args):
     # for comparison; outside the timed region
     alt = {}
     if args.sweep:
-        for bs, pp, var, rf in [(64, 8, 0, 0), (64, 8, 64, 8), (64, 8, 64, 16), (128, 8, 64, 8), (64, 8, 192, 8),
-                                (64, 8, 128, 0), (64, 8, 16, 0), (64, 8, 144, 0), (64, 8, 80, 8)]:
+        for bs, pp, var, rf in [(64, 8, 64, 8), (64, 8, 72, 8), (128, 8, 72, 8), (64, 0, 72, 8), (64, 8, 65, 8),
+                                (64, 8, 16, 0), (64, 8, 80, 8)]:
             scene.set_trace_config(bs, pp, var, refill=rf)
             key = f"b{bs}-p{pp}-v{var}-r{rf}"
             alt[key] = {}
