@@ -565,18 +565,25 @@ def run_lrx(args):
 # Instanced two-level scene: 16 x 200,000-triangle icospheres, 4,096 instances
 # ---------------------------------------------------------------------------
 
-def run_instanced(args):
+def run_instanced(args, motion: bool = False):
     """16 displaced icospheres of 200,000 triangles under 4,096 random affine
     instances (819,200,000 effective triangles) in [0,10]^3; per step
-    8,388,608 closest-hit and 8,388,608 any-hit rays (maxt U[0.5, 5])."""
+    8,388,608 closest-hit and 8,388,608 any-hit rays (maxt U[0.5, 5]).
+    motion: the same meshes under W.motion_scene's instances -- a third each
+    translating (two keyframes), turning/scaling/moving (three keyframes)
+    and static -- with ray times uniform over the shutter [0, 1]."""
     import torch
 
     from luxcore_gb300 import lrx
 
     torch.cuda.set_device(0)
     t0 = time.perf_counter()
-    scene_desc, closest, anyr = W.config3(n_rays=args.inst_rays)
-    log(f"[instanced] {time.strftime('%H:%M:%S')} scene and rays generated in {time.perf_counter() - t0:.1f}s")
+    if motion:
+        scene_desc, closest, anyr = W.config_motion(n_rays=args.inst_rays)
+    else:
+        scene_desc, closest, anyr = W.config3(n_rays=args.inst_rays)
+    tag = "motion" if motion else "instanced"
+    log(f"[{tag}] {time.strftime('%H:%M:%S')} scene and rays generated in {time.perf_counter() - t0:.1f}s")
     stream = torch.cuda.Stream()
     st = stream.cuda_stream
     t0 = time.perf_counter()
@@ -584,7 +591,7 @@ def run_instanced(args):
         scene = lrx.Scene(scene_desc, stream=st)
     build_s = time.perf_counter() - t0
     info = scene.info()
-    log(f"[instanced] scene built {info}")
+    log(f"[{tag}] scene built {info}")
     dev = []
     for name, r, mode in (("closest", closest, lrx.LRX_TRACE_CLOSEST), ("any", anyr, lrx.LRX_TRACE_ANY)):
         dr = torch.from_numpy(np.ascontiguousarray(r).view(np.uint8).reshape(-1).copy()).cuda()
@@ -657,13 +664,16 @@ def run_instanced(args):
                "sample": f"every {frac}th ray of both sets ({n_s} rays), oracle MBVHAccel::Intersect restatement "
                          f"(closest hit for both), {threads} threads"}
     line = {
-        "metric": "Mrays/s closest/any-hit on the instanced two-level scene (1 GB300, % HBM roofline)",
+        "metric": ("Mrays/s closest/any-hit on motion-blurred instances (1 GB300, % HBM roofline)" if motion else
+                   "Mrays/s closest/any-hit on the instanced two-level scene (1 GB300, % HBM roofline)"),
         "value": round(value, 3), "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(elapsed_ms / args.steps, 4), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {
-            "workload": f"instanced: {info['blas_count']} meshes x 200000 tris, {info['instance_count']} instances "
-                        f"({info['triangle_count']} effective tris); {dev[0][3]} closest + {dev[1][3]} any-hit rays",
+            "workload": f"{tag}: {info['blas_count']} meshes x 200000 tris, {info['instance_count']} instances "
+                        f"({info['triangle_count']} effective tris"
+                        + ("; 1/3 translating, 1/3 turning+scaling+moving, 1/3 static, ray time U[0,1)" if motion else "")
+                        + f"); {dev[0][3]} closest + {dev[1][3]} any-hit rays",
             "rays_per_step": rays_per_step, "build_ms": round(info["build_ms"], 1),
             "scene_build_wall_s": round(build_s, 3), "wide_nodes": info["node_count"],
             "device_MB": round(info["device_bytes"] / 1e6, 1),
@@ -677,7 +687,8 @@ def run_instanced(args):
         },
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4), "traffic": None, "peak_kind": peak_kind,
-                     "bytes_per_ray": round(sum(alg.values()) / rays_per_step, 1)},
+                     "bytes_per_ray": round(sum(alg.values()) / rays_per_step, 1),
+                     **({"note": "motion intervals read at instance entry are not counted"} if motion else {})},
         "cpu_baseline": cpu,
         "gpu_launches": (launches_per_step if launches_per_step is not None else len(dev)) * args.steps,
         "gpu_launches_per_step": launches_per_step,
@@ -997,7 +1008,8 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=2.0)
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[2000.0, 800.0])
     ap.add_argument("--serve-streams", type=int, default=4)
-    ap.add_argument("--workload", default="heightfield", choices=["heightfield", "batching", "serving", "instanced"],
+    ap.add_argument("--workload", default="heightfield", choices=["heightfield", "batching", "serving", "instanced",
+                                                                      "motion"],
                     help="heightfield = the headline line; batching = uneven batches, plain vs queue kernel")
     ap.add_argument("--batches", type=int, default=512)
     ap.add_argument("--inst-rays", type=int, default=1 << 23, help="instanced workload: rays per set")
@@ -1024,6 +1036,8 @@ def main():
         return run_batching(args)
     if args.workload == "instanced" and args.impl == "lrx":
         return run_instanced(args)
+    if args.workload == "motion" and args.impl == "lrx":
+        return run_instanced(args, motion=True)
     if args.impl == "reference":
         return run_reference(args)
     return run_lrx(args)

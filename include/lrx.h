@@ -123,6 +123,31 @@ lrx_status lrx_scene_create(const lrx_mesh_desc *meshes, uint32_t mesh_count,
 		const lrx_object_desc *objects, uint32_t object_count,
 		const lrx_build_opts *opts, void *stream, lrx_scene **out_scene);
 
+/* The motion system of one motion-blurred instance: `count` keyframes with
+ * strictly increasing times and row-major 4x4 matrices in the convention of
+ * the reference's MotionTriangleMesh -- the motion system MBVHAccel samples
+ * at the ray's time and applies to the ray (world to the mesh's local
+ * space, mbvhaccel.cpp:326-327).  The object it names must be an instance;
+ * its `transform` is then not used. */
+typedef struct lrx_motion_desc {
+	uint32_t object;          /* index into the objects array */
+	uint32_t count;           /* keyframes, >= 1 */
+	const float *times;       /* count times */
+	const float *transforms;  /* count x 16 floats */
+} lrx_motion_desc;
+
+/* lrx_scene_create with motion-blurred instances: each ray is traced against
+ * the instance transform interpolated at its `time` (translation and scale
+ * lerped, rotation slerped between decomposed keyframes), and the instance's
+ * box in the top-level BVH is its swept bound.
+ * Replaces: MBVHAccel::Init / Intersect with MotionTriangleMesh leaves
+ * (mbvhaccel.cpp:145-172, 323-328) and MotionSystem / InterpolatedTransform
+ * (src/luxrays/core/geometry/motionsystem.cpp:33-345). */
+lrx_status lrx_scene_create_motion(const lrx_mesh_desc *meshes, uint32_t mesh_count,
+		const lrx_object_desc *objects, uint32_t object_count,
+		const lrx_motion_desc *motions, uint32_t motion_count,
+		const lrx_build_opts *opts, void *stream, lrx_scene **out_scene);
+
 /* Frees the scene's device memory (Accelerator destructor). */
 lrx_status lrx_scene_destroy(lrx_scene *scene);
 
@@ -220,8 +245,9 @@ typedef struct lrx_batch {
  * warp's lanes may then hold rays of different batches); otherwise 64-thread
  * blocks claim 64-ray tiles.  Batches whose scene config has
  * LRX_VARIANT_SORT_RAYS and at least 32,768 rays are reordered first (one
- * radix sort per launch).  Results equal lrx_trace on each batch.
- * Asynchronous on `stream`; graph-capturable (no host synchronisation; the
+ * radix sort per launch).  Batches on scenes with motion-blurred instances
+ * are traced by a launch of their own each, in batch order.  Results equal
+ * lrx_trace on each batch.  Asynchronous on `stream`; graph-capturable (no host synchronisation; the
  * sort scratch is stream-ordered pool memory).
  * Replaces: a sequence of HardwareIntersectionKernel::EnqueueTraceRayBuffer
  * calls (hardwareintersectiondevice.h:67-68), one per RayBuffer. */

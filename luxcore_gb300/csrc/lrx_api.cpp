@@ -14,6 +14,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "lrx_common.cuh"
@@ -99,6 +100,8 @@ static bool matrix_inverse(const float in[16], float out[16]) {
 	return true;
 }
 
+bool host_matrix_inverse(const float in[16], float out[16]) { return matrix_inverse(in, out); }
+
 // MachineEpsilon::E (include/luxrays/core/epsilon.h:50-55)
 static float machine_eps_host(float v) {
 	uint32_t u;
@@ -127,6 +130,17 @@ static void xform_point_host(const float m[16], const float p[3], float out[3]) 
 	out[2] = r[2];
 }
 
+// Expands a world box by MachineEpsilon::E as MBVHAccel::Init does
+// (mbvhaccel.cpp:189-193), then one more ulp outward.
+static void pad_box(float olo[3], float ohi[3]) {
+	float e = 0.f;
+	for (int k = 0; k < 3; ++k) e = std::max(e, std::max(machine_eps_host(olo[k]), machine_eps_host(ohi[k])));
+	for (int k = 0; k < 3; ++k) {
+		olo[k] = std::nextafter(olo[k] - e, -INFINITY);
+		ohi[k] = std::nextafter(ohi[k] + e, INFINITY);
+	}
+}
+
 // World box of an instance: the 8 transformed corners of the BLAS box,
 // expanded by MachineEpsilon::E as MBVHAccel::Init does (mbvhaccel.cpp:189-193).
 static void instance_box(const float m[16], const float lo[3], const float hi[3], float olo[3], float ohi[3]) {
@@ -143,12 +157,13 @@ static void instance_box(const float m[16], const float lo[3], const float hi[3]
 			ohi[k] = std::max(ohi[k], q[k]);
 		}
 	}
-	float e = 0.f;
-	for (int k = 0; k < 3; ++k) e = std::max(e, std::max(machine_eps_host(olo[k]), machine_eps_host(ohi[k])));
-	for (int k = 0; k < 3; ++k) {
-		olo[k] = std::nextafter(olo[k] - e, -INFINITY);
-		ohi[k] = std::nextafter(ohi[k] + e, INFINITY);
-	}
+	pad_box(olo, ohi);
+}
+
+static float bits_as_float(uint32_t u) {
+	float f;
+	std::memcpy(&f, &u, 4);
+	return f;
 }
 
 static bool all_finite(const float *v, int n) {
@@ -195,6 +210,15 @@ struct lrx_scene {
 	BuildScratch scratch;
 	std::mutex mu;
 	float bounds_lo[3] = {0, 0, 0}, bounds_hi[3] = {0, 0, 0};  // world box of the root
+	// motion-blurred instances: per object an index into motions (kNull: none)
+	struct Motion {
+		std::vector<MotionInterval> its;  // keyframes + 1 intervals (the device gets the first keyframes)
+		uint32_t offset16 = 0;            // device copy, in 16-byte units from the instance array's base
+		bool have_box = false;
+		float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};  // swept world box, padded
+	};
+	std::vector<uint32_t> obj_motion;
+	std::vector<Motion> motions;
 };
 
 int lrx::scene_device(const lrx_scene *scene) { return scene->device; }
@@ -296,6 +320,40 @@ lrx_status build_tlas(lrx_scene *s, const lrx_object_desc *objects, uint32_t n_o
 	std::vector<InstRecord> recs;
 	std::vector<float4> blo, bhi;
 	recs.reserve(n_objects + 1);
+	{
+		// swept boxes of motion instances not bounded yet (1025 samples per
+		// interval each), spread over the host's cores
+		std::vector<uint32_t> todo;
+		for (uint32_t i = 0; i < n_objects; ++i)
+			if ((s->obj_flags[i] & LRX_OBJECT_INSTANCE) && s->obj_blas[i] != kNull && s->obj_motion[i] != kNull &&
+					!s->motions[s->obj_motion[i]].have_box)
+				todo.push_back(i);
+		std::atomic<uint32_t> next{0};
+		std::atomic<int> failed{0};
+		auto work = [&]() {
+			for (uint32_t k; (k = next.fetch_add(1)) < todo.size();) {
+				const uint32_t i = todo[k];
+				const Blas &b = s->blas[s->obj_blas[i]];
+				lrx_scene::Motion &mo = s->motions[s->obj_motion[i]];
+				if (motion_bound(mo.its, b.lo, b.hi, mo.lo, mo.hi) != LRX_OK) {
+					failed = 1;
+					continue;
+				}
+				pad_box(mo.lo, mo.hi);
+				mo.have_box = true;
+			}
+		};
+		const uint32_t nt = std::min<uint32_t>((uint32_t)todo.size() / 64 + 1,
+				std::max(1u, std::min(32u, std::thread::hardware_concurrency())));
+		std::vector<std::thread> pool;
+		for (uint32_t t = 1; t < nt; ++t) pool.emplace_back(work);
+		work();
+		for (std::thread &t : pool) t.join();
+		if (failed) {
+			set_error("motion system: a sampled matrix is singular");
+			return LRX_ERR_INVALID_ARGUMENT;
+		}
+	}
 	if (s->plain_blas != kNull) {
 		const Blas &b = s->blas[s->plain_blas];
 		InstRecord r{};
@@ -313,6 +371,18 @@ lrx_status build_tlas(lrx_scene *s, const lrx_object_desc *objects, uint32_t n_o
 		const uint32_t bi = s->obj_blas[i];
 		if (bi == kNull) continue;
 		const Blas &b = s->blas[bi];
+		if (s->obj_motion[i] != kNull) {
+			// motion instance: the traversal samples its transform at the ray's time
+			const lrx_scene::Motion &mo = s->motions[s->obj_motion[i]];
+			InstRecord r{};
+			const uint32_t n_its = (uint32_t)mo.its.size() - 1;
+			r.r0 = make_float4(bits_as_float(n_its), 0, 0, 0);
+			r.info = make_uint4(b.root, i, kInstMotion, mo.offset16);
+			recs.push_back(r);
+			blo.push_back(make_float4(mo.lo[0], mo.lo[1], mo.lo[2], 0));
+			bhi.push_back(make_float4(mo.hi[0], mo.hi[1], mo.hi[2], 0));
+			continue;
+		}
 		float inv[16];
 		lrx_status rc = object_inverse(objects[i], inv);
 		if (rc != LRX_OK) return rc;
@@ -374,8 +444,14 @@ const char *lrx_last_error(void) { return g_last_error.c_str(); }
 
 lrx_status lrx_scene_create(const lrx_mesh_desc *meshes, uint32_t mesh_count, const lrx_object_desc *objects,
 		uint32_t object_count, const lrx_build_opts *opts, void *stream, lrx_scene **out_scene) {
+	return lrx_scene_create_motion(meshes, mesh_count, objects, object_count, nullptr, 0, opts, stream, out_scene);
+}
+
+lrx_status lrx_scene_create_motion(const lrx_mesh_desc *meshes, uint32_t mesh_count, const lrx_object_desc *objects,
+		uint32_t object_count, const lrx_motion_desc *motions, uint32_t motion_count, const lrx_build_opts *opts,
+		void *stream, lrx_scene **out_scene) {
 	try {
-		if (!out_scene || (mesh_count && !meshes)) {
+		if (!out_scene || (mesh_count && !meshes) || (motion_count && !motions)) {
 			set_error("lrx_scene_create: null argument");
 			return LRX_ERR_INVALID_ARGUMENT;
 		}
@@ -401,12 +477,23 @@ lrx_status lrx_scene_create(const lrx_mesh_desc *meshes, uint32_t mesh_count, co
 			}
 		}
 		const uint32_t n_obj = (uint32_t)objs.size();
+		std::vector<uint32_t> obj_motion(n_obj, kNull);
+		std::vector<lrx_scene::Motion> motion_list(motion_count);
+		for (uint32_t k = 0; k < motion_count; ++k) {
+			const lrx_motion_desc &md = motions[k];
+			if (md.object >= n_obj || !(objs[md.object].flags & LRX_OBJECT_INSTANCE) || obj_motion[md.object] != kNull) {
+				set_error("motion " + std::to_string(k) + ": object out of range, not an instance, or given twice");
+				return LRX_ERR_INVALID_ARGUMENT;
+			}
+			if ((rc = motion_intervals(md.times, md.transforms, md.count, motion_list[k].its)) != LRX_OK) return rc;
+			obj_motion[md.object] = k;
+		}
 		for (uint32_t i = 0; i < n_obj; ++i) {
 			if (objs[i].mesh >= mesh_count) {
 				set_error("object " + std::to_string(i) + ": mesh index out of range");
 				return LRX_ERR_INVALID_ARGUMENT;
 			}
-			if (objs[i].flags & LRX_OBJECT_INSTANCE) {
+			if ((objs[i].flags & LRX_OBJECT_INSTANCE) && obj_motion[i] == kNull) {
 				float inv[16];
 				if ((rc = object_inverse(objs[i], inv)) != LRX_OK) return rc;
 			}
@@ -414,6 +501,8 @@ lrx_status lrx_scene_create(const lrx_mesh_desc *meshes, uint32_t mesh_count, co
 
 		lrx_scene *s = new lrx_scene();
 		std::unique_ptr<lrx_scene> guard(s);
+		s->obj_motion = std::move(obj_motion);
+		s->motions = std::move(motion_list);
 		s->device = dev;
 		s->mesh_count = mesh_count;
 		s->opts.struct_size = sizeof(lrx_build_opts);
@@ -562,7 +651,20 @@ lrx_status lrx_scene_create(const lrx_mesh_desc *meshes, uint32_t mesh_count, co
 		s->info.max_depth = max_depth;
 		s->info.node_count = node_off;
 		if (s->two_level) {
-			if ((rc = s->insts.alloc(sizeof(InstRecord) * (tlas_prims + 1))) != LRX_OK) return rc;
+			// instance records, then the motion intervals the traversal samples
+			size_t bytes = sizeof(InstRecord) * (tlas_prims + 1);
+			for (lrx_scene::Motion &mo : s->motions) {
+				mo.offset16 = (uint32_t)(bytes / 16);
+				bytes += sizeof(MotionInterval) * (mo.its.size() - 1);
+			}
+			if (bytes / 16 > 0xffffffffull) {
+				set_error("too many motion keyframes");
+				return LRX_ERR_INVALID_ARGUMENT;
+			}
+			if ((rc = s->insts.alloc(bytes)) != LRX_OK) return rc;
+			for (const lrx_scene::Motion &mo : s->motions)
+				LRX_CUDA(cudaMemcpyAsync(static_cast<char *>(s->insts.ptr) + 16ull * mo.offset16, mo.its.data(),
+						sizeof(MotionInterval) * (mo.its.size() - 1), cudaMemcpyHostToDevice, st));
 			if ((rc = build_tlas(s, objs.data(), n_obj, st)) != LRX_OK) return rc;
 		} else {
 			s->root = s->blas.empty() ? kNull : 0u;
@@ -663,7 +765,7 @@ struct Hash64 {
 };
 
 constexpr char kBlobMagic[8] = {'L', 'R', 'X', 'S', 'C', 'E', 'N', 'E'};
-constexpr uint32_t kBlobVersion = 1;
+constexpr uint32_t kBlobVersion = 2;
 
 struct BlobWriter {
 	unsigned char *p;  // null: only count
@@ -770,6 +872,15 @@ static void write_meta(const lrx_scene *s, BlobWriter &w) {
 	w.value(s->info);
 	w.value(s->bounds_lo);
 	w.value(s->bounds_hi);
+	w.vec(s->obj_motion);
+	w.value((uint64_t)s->motions.size());
+	for (const lrx_scene::Motion &mo : s->motions) {
+		w.value(mo.offset16);
+		w.value((uint32_t)(mo.have_box ? 1u : 0u));
+		w.value(mo.lo);
+		w.value(mo.hi);
+		w.vec(mo.its);
+	}
 }
 }  // extern "C++"
 
@@ -866,6 +977,19 @@ static lrx_status scene_from_blob(const void *blob, size_t bytes, cudaStream_t s
 		s->info = r.value<lrx_scene_info>();
 		for (int c = 0; c < 3; ++c) s->bounds_lo[c] = r.value<float>();
 		for (int c = 0; c < 3; ++c) s->bounds_hi[c] = r.value<float>();
+		r.vec(s->obj_motion, lim);
+		const uint64_t n_motion = r.value<uint64_t>();
+		if (n_motion > lim) r.ok = false;
+		for (uint64_t k = 0; r.ok && k < n_motion; ++k) {
+			lrx_scene::Motion mo;
+			mo.offset16 = r.value<uint32_t>();
+			mo.have_box = r.value<uint32_t>() != 0;
+			for (int c = 0; c < 3; ++c) mo.lo[c] = r.value<float>();
+			for (int c = 0; c < 3; ++c) mo.hi[c] = r.value<float>();
+			r.vec(mo.its, lim);
+			if (mo.its.size() < 2) r.ok = false;
+			s->motions.push_back(std::move(mo));
+		}
 		const unsigned char *arr[3];
 		uint64_t len[3];
 		for (int k = 0; k < 3; ++k) {
@@ -873,7 +997,7 @@ static lrx_status scene_from_blob(const void *blob, size_t bytes, cudaStream_t s
 			arr[k] = r.take(len[k]);
 		}
 		if (!r.ok || r.n != r.size || len[0] % sizeof(WideNode) || len[1] % sizeof(TriRecord) ||
-				len[2] % sizeof(InstRecord) || s->obj_blas.size() != s->obj_flags.size() ||
+				len[2] % 16 || s->obj_blas.size() != s->obj_flags.size() || s->obj_motion.size() != s->obj_flags.size() ||
 				(s->root != kNull && (uint64_t)s->root * sizeof(WideNode) >= len[0])) {
 			set_error("lrx_scene_load: malformed blob");
 			return LRX_ERR_INVALID_ARGUMENT;
@@ -943,6 +1067,7 @@ static lrx_status trace_common(lrx_scene *s, const void *d_rays, void *d_hits, u
 	a.insts = s->insts.as<InstRecord>();
 	a.root = s->root;
 	a.two_level = s->two_level ? 1u : 0u;
+	a.motion = s->motions.empty() ? 0u : 1u;
 	a.rays = d_rays;
 	a.hits = d_hits;
 	a.count = count;
@@ -1190,6 +1315,14 @@ lrx_status lrx_trace_batches_ex(const lrx_batch *batches, uint32_t n_batches, vo
 		const lrx_batch &b = batches[k];
 		if (b.count == 0) continue;
 		lrx_scene *s = b.scene;
+		if (!s->motions.empty()) {
+			// scenes with motion instances trace in a launch of their own (the
+			// queue kernels carry no motion code); its flag follows that launch
+			lrx_status rc = trace_common(s, b.d_rays, b.d_hits, b.count, b.mode, nullptr, st);
+			if (rc == LRX_OK && d_done_flags) rc = launch_set_flag(d_done_flags + k, st);
+			if (rc != LRX_OK) return rc;
+			continue;
+		}
 		const uint32_t tiles = (b.count + kTileRays - 1) / kTileRays;
 		const lrx_trace_config &cfg = s->tcfg[b.mode == LRX_TRACE_ANY ? 1 : 0];
 		const bool sort = (cfg.variant & kVarSortRays) && b.count >= kSortMinRays && s->root != kNull;

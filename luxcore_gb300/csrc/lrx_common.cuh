@@ -57,6 +57,26 @@ struct alignas(16) InstRecord {
 };
 static_assert(sizeof(InstRecord) == 80, "InstRecord is 80 bytes");
 constexpr uint32_t kInstIdentity = 1u;
+// Motion instance: its transform is sampled at the ray's time from a motion
+// system -- info.w = offset (in 16-byte units from the instance array's
+// base) of its first MotionInterval, r0.x = their count (as uint bits).
+constexpr uint32_t kInstMotion = 2u;
+
+// One InterpolatedTransform of a motion system (motionsystem.cpp:33-160),
+// decomposed on the host: start/end matrices, the rotation matrix of the
+// start decomposition, scales, translations and unit quaternions (w,x,y,z).
+struct alignas(16) MotionInterval {
+	uint32_t flags;
+	float start_time, end_time, pad;
+	float start_m[16], end_m[16], start_r[16];
+	float s0[3], t0[3], s1[3], t1[3];
+	float q0[4], q1[4];
+};
+static_assert(sizeof(MotionInterval) == 288, "MotionInterval is 288 bytes");
+// MotionInterval::flags
+constexpr uint32_t kMiActive = 1u, kMiRotation = 2u, kMiTransX = 4u, kMiTransY = 8u, kMiTransZ = 16u,
+		   kMiScaleX = 32u, kMiScaleY = 64u, kMiScaleZ = 128u;
+constexpr uint32_t kMiTrans = kMiTransX | kMiTransY | kMiTransZ, kMiScale = kMiScaleX | kMiScaleY | kMiScaleZ;
 
 #if defined(__CUDACC__)
 // ---------------------------------------------------------------------------

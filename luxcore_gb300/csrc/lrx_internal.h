@@ -114,6 +114,7 @@ struct TraceArgs {
 	const uint32_t *order = nullptr;  // thread i traces ray order[i] (sorted launches)
 	uint32_t refill = 0;           // persistent fetch: idle lanes that trigger a warp's claim (0 = 16)
 	const uint32_t *count_dev = nullptr;  // persistent fetch: rays to claim, read on the device (<= count)
+	uint32_t motion = 0;           // two-level scene with motion instances: the kVarMotion builds trace it
 };
 constexpr uint32_t kTraceBlock = 128;
 constexpr uint32_t kVarSortRays = 0x10u;   // reorder rays by octant + origin before tracing
@@ -122,6 +123,7 @@ constexpr uint32_t kVarPersistent = 0x40u;  // persistent warps with warp-level 
 constexpr uint32_t kVarSmemStack = 0x80u;  // top of the traversal stack in shared memory
 constexpr uint32_t kVarCompact = 0x100u;   // with kVarPersistent: trace only the unmasked rays, compacted first
 constexpr uint32_t kVarAll = 0x1ffu;       // every defined variant bit
+constexpr uint32_t kVarMotion = 0x200u;    // internal build bit: instance entry samples motion systems
 constexpr uint32_t kSortMinRays = 32768;   // smaller batches are traced in caller order
 
 lrx_status launch_trace(const TraceArgs &a, cudaStream_t stream);
@@ -170,6 +172,10 @@ static_assert(sizeof(QueueParams) <= 32000, "kernel parameter limit");
 // kept for reuse); for per-call scratch that must not synchronise the device.
 lrx_status stream_pool(int dev, cudaMemPool_t *out);
 
+// Sets *flag to 1 in stream order, after a fence that orders every earlier
+// write of the stream's kernels before it (host-mapped flags allowed).
+lrx_status launch_set_flag(uint32_t *flag, cudaStream_t stream);
+
 // One launch of the persistent queue kernel over p.n batches.
 lrx_status launch_trace_queue(const QueueParams &p, cudaStream_t stream);
 
@@ -200,6 +206,20 @@ lrx_status sort_queue_batches(const std::vector<SortBatch> &batches, uint32_t to
 
 // CUDA device a scene was built on.
 int scene_device(const lrx_scene *scene);
+
+// Matrix4x4::Inverse (row-major 4x4, FP32); false for a singular matrix.
+bool host_matrix_inverse(const float in[16], float out[16]);
+
+struct MotionInterval;
+// A motion system's intervals from `count` keyframes (strictly increasing
+// times, row-major matrices): count + 1 records, of which the traversal
+// samples the first count (lrx_motion.cpp).
+lrx_status motion_intervals(const float *times, const float *mats, uint32_t count,
+		std::vector<MotionInterval> &out);
+// Swept world box of a local box under a motion system of world->local
+// keyframes (MotionSystem::Bound with storingGlobal2Local).
+lrx_status motion_bound(const std::vector<MotionInterval> &its, const float lo[3], const float hi[3], float olo[3],
+		float ohi[3]);
 
 // lrx_scene_load without the checksum pass, for blobs the library wrote and
 // kept in its own memory (the server's cache of evicted scenes).

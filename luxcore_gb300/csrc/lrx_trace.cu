@@ -195,6 +195,7 @@ struct TravState {
 	ActiveRay ray;             // in the current BVH's space (world, or an instance's local space)
 	float3 wo, wd;             // world-space origin / direction
 	float mint, best_t, best_b1, best_b2;
+	float time;                // the ray's time (motion instances)
 	uint32_t best_mesh, best_tri;
 	uint32_t inst_obj;         // object of the instance being traversed (kNull at top level)
 	uint32_t visits;
@@ -227,6 +228,112 @@ __device__ __forceinline__ uint2 stack_get(const TravStack &st, StackTop t, int 
 
 enum : int { kRayMasked = 0, kRayAnswered = 1, kRayTraverse = 2 };
 
+// ---------------------------------------------------------------------------
+// Motion instances: the transform at a ray's time, from the host-decomposed
+// intervals -- MotionSystem::Sample and InterpolatedTransform::Sample
+// (src/luxrays/core/geometry/motionsystem.cpp:56-160, 333-337; the GPU
+// kernel's MotionSystem_Sample, motionsystem_funcs.cl:21-115), with every
+// product and sum rounded separately as in the CPU code.  Slerp takes
+// CUDA's acosf / sinf, so a rotating instance's matrix can differ from the
+// CPU's in the last bits; the reference's own CPU and GPU paths differ the
+// same way.
+// ---------------------------------------------------------------------------
+
+struct MotionRows {
+	float4 r0, r1, r2, r3;
+};
+
+__device__ __forceinline__ float lerp_rn(float t, float a, float b) {
+	return __fadd_rn(a, __fmul_rn(t, __fsub_rn(b, a)));
+}
+
+__device__ __forceinline__ MotionRows motion_sample(const MotionInterval *its, uint32_t n, float time) {
+	uint32_t k = n - 1;  // the interval ending after `time` (upper_bound over the keyframe times)
+	for (uint32_t i = 0; i < n; ++i)
+		if (time < __ldg(&its[i].end_time)) {
+			k = i;
+			break;
+		}
+	const MotionInterval *it = its + k;
+	const uint32_t f = __ldg(&it->flags);
+	const float st = __ldg(&it->start_time), et = __ldg(&it->end_time);
+	float m[16];
+	if (!(f & kMiActive) || time <= st || time >= et) {
+		const float *src = (!(f & kMiActive) || time <= st) ? it->start_m : it->end_m;
+#pragma unroll
+		for (int j = 0; j < 16; ++j) m[j] = __ldg(src + j);
+	} else {
+		const float le = __fdiv_rn(__fsub_rn(time, st), __fsub_rn(et, st));
+		if ((f & kMiTrans) && !(f & (kMiScale | kMiRotation))) {  // translation only
+#pragma unroll
+			for (int j = 0; j < 16; ++j) m[j] = __ldg(it->start_m + j);
+			if (f & kMiTransX) m[3] = lerp_rn(le, __ldg(&it->t0[0]), __ldg(&it->t1[0]));
+			if (f & kMiTransY) m[7] = lerp_rn(le, __ldg(&it->t0[1]), __ldg(&it->t1[1]));
+			if (f & kMiTransZ) m[11] = lerp_rn(le, __ldg(&it->t0[2]), __ldg(&it->t1[2]));
+		} else {
+			if (f & kMiRotation) {
+				// Slerp (quaternion.cpp:143-165) then ToMatrix (:116-141)
+				const float aw = __ldg(&it->q0[0]), ax = __ldg(&it->q0[1]), ay = __ldg(&it->q0[2]), az = __ldg(&it->q0[3]);
+				const float bw = __ldg(&it->q1[0]), bx = __ldg(&it->q1[1]), by = __ldg(&it->q1[2]), bz = __ldg(&it->q1[3]);
+				float cos_phi = __fadd_rn(__fmul_rn(aw, bw),
+						__fadd_rn(__fadd_rn(__fmul_rn(ax, bx), __fmul_rn(ay, by)), __fmul_rn(az, bz)));
+				const float sign = cos_phi > 0.f ? 1.f : -1.f;
+				cos_phi = __fmul_rn(cos_phi, sign);
+				float f1, f2;
+				if (__fsub_rn(1.f, cos_phi) > 1e-6f) {
+					const float phi = acosf(cos_phi);
+					const float sin_phi = sinf(phi);
+					f1 = __fdiv_rn(sinf(__fmul_rn(__fsub_rn(1.f, le), phi)), sin_phi);
+					f2 = __fdiv_rn(sinf(__fmul_rn(le, phi)), sin_phi);
+				} else {
+					f1 = __fsub_rn(1.f, le);
+					f2 = le;
+				}
+				const float g = __fmul_rn(sign, f2);
+				const float w = __fadd_rn(__fmul_rn(aw, f1), __fmul_rn(bw, g));
+				const float x = __fadd_rn(__fmul_rn(f1, ax), __fmul_rn(g, bx));
+				const float y = __fadd_rn(__fmul_rn(f1, ay), __fmul_rn(g, by));
+				const float z = __fadd_rn(__fmul_rn(f1, az), __fmul_rn(g, bz));
+				const float xx = __fmul_rn(x, x), yy = __fmul_rn(y, y), zz = __fmul_rn(z, z);
+				const float xy = __fmul_rn(x, y), xz = __fmul_rn(x, z), yz = __fmul_rn(y, z);
+				const float xw = __fmul_rn(x, w), yw = __fmul_rn(y, w), zw = __fmul_rn(z, w);
+				m[0] = __fsub_rn(1.f, __fmul_rn(2.f, __fadd_rn(yy, zz)));
+				m[4] = __fmul_rn(2.f, __fsub_rn(xy, zw));
+				m[8] = __fmul_rn(2.f, __fadd_rn(xz, yw));
+				m[1] = __fmul_rn(2.f, __fadd_rn(xy, zw));
+				m[5] = __fsub_rn(1.f, __fmul_rn(2.f, __fadd_rn(xx, zz)));
+				m[9] = __fmul_rn(2.f, __fsub_rn(yz, xw));
+				m[2] = __fmul_rn(2.f, __fsub_rn(xz, yw));
+				m[6] = __fmul_rn(2.f, __fadd_rn(yz, xw));
+				m[10] = __fsub_rn(1.f, __fmul_rn(2.f, __fadd_rn(xx, yy)));
+				m[3] = m[7] = m[11] = 0.f;
+				m[12] = m[13] = m[14] = 0.f;
+				m[15] = 1.f;
+			} else {
+#pragma unroll
+				for (int j = 0; j < 16; ++j) m[j] = __ldg(it->start_r + j);
+			}
+			float S[3];
+#pragma unroll
+			for (int c = 0; c < 3; ++c)
+				S[c] = (f & kMiScale) ? lerp_rn(le, __ldg(&it->s0[c]), __ldg(&it->s1[c])) : __ldg(&it->s0[c]);
+#pragma unroll
+			for (int row = 0; row < 3; ++row)
+#pragma unroll
+				for (int j = 0; j < 3; ++j) m[4 * row + j] = __fmul_rn(S[row], m[4 * row + j]);
+			m[3] = (f & kMiTransX) ? lerp_rn(le, __ldg(&it->t0[0]), __ldg(&it->t1[0])) : __ldg(&it->t0[0]);
+			m[7] = (f & kMiTransY) ? lerp_rn(le, __ldg(&it->t0[1]), __ldg(&it->t1[1])) : __ldg(&it->t0[1]);
+			m[11] = (f & kMiTransZ) ? lerp_rn(le, __ldg(&it->t0[2]), __ldg(&it->t1[2])) : __ldg(&it->t0[2]);
+		}
+	}
+	MotionRows r;
+	r.r0 = make_float4(m[0], m[1], m[2], m[3]);
+	r.r1 = make_float4(m[4], m[5], m[6], m[7]);
+	r.r2 = make_float4(m[8], m[9], m[10], m[11]);
+	r.r3 = make_float4(m[12], m[13], m[14], m[15]);
+	return r;
+}
+
 // Reads ray i and sets up its traversal.  kRayMasked: skip it and write
 // nothing (bvh.cl:243-244); kRayAnswered: the initial miss (t = maxt) is the
 // answer -- empty scene, NaN/infinite origin or direction, NaN maxt;
@@ -248,6 +355,7 @@ __device__ __forceinline__ int ray_begin(const TraceArgs &a, uint32_t i, bool st
 	s.wd = make_float3(r0.w, r1.x, r1.y);
 	s.mint = r1.z;
 	s.best_t = r1.w;
+	s.time = r2.x;
 	s.best_b1 = 0.f;
 	s.best_b2 = 0.f;
 	s.best_mesh = kNull;
@@ -270,7 +378,7 @@ __device__ __forceinline__ int ray_begin(const TraceArgs &a, uint32_t i, bool st
 // status word).  Every trip either expands a node -- at most visit_limit of
 // them -- or consumes a stack entry or an instance bit, so a ray finishes in
 // a bounded number of trips.
-template <bool ANY, bool TWO_LEVEL, bool COUNT, bool MM3, bool SMEM = false>
+template <bool ANY, bool TWO_LEVEL, bool COUNT, bool MM3, bool SMEM = false, bool MOTION = false>
 __device__ __forceinline__ bool ray_step(const TraceArgs &a, TravState &s, TravStack &stack, bool keep, uint64_t pol,
 		Counts &c, StackTop top = StackTop{nullptr, 0}) {
 #define LRX_PUSH(V)                                          \
@@ -312,6 +420,11 @@ __device__ __forceinline__ bool ray_step(const TraceArgs &a, TravState &s, TravS
 			s.inst_obj = info.y;
 			if (info.z & kInstIdentity) {
 				make_active(s.ray, s.wo, s.wd);
+			} else if (MOTION && (info.z & kInstMotion)) {
+				const MotionRows m = motion_sample(
+						reinterpret_cast<const MotionInterval *>(reinterpret_cast<const char *>(a.insts) + 16ull * info.w),
+						__float_as_uint(__ldg(&ir->r0.x)), s.time);
+				make_active(s.ray, xform_point(m.r0, m.r1, m.r2, m.r3, s.wo), xform_vector(m.r0, m.r1, m.r2, s.wd));
 			} else {
 				const float4 m0 = __ldg(&ir->r0), m1 = __ldg(&ir->r1), m2 = __ldg(&ir->r2), m3 = __ldg(&ir->r3);
 				make_active(s.ray, xform_point(m0, m1, m2, m3, s.wo), xform_vector(m0, m1, m2, s.wd));
@@ -390,6 +503,7 @@ __device__ __forceinline__ void trace_ray(const TraceArgs &a, uint32_t tid, bool
 		StackTop top = StackTop{nullptr, 0}) {
 	constexpr bool MM3 = (CV & kVarMinMax3) != 0;
 	constexpr bool SMEM = (CV & kVarSmemStack) != 0;
+	constexpr bool MOTION = (CV & kVarMotion) != 0;
 	if (!active) return;
 	const uint32_t i = a.order ? a.order[tid] : tid;  // the ray this thread traces
 	const bool keep = (a.variant & kVarSceneEvictLast) != 0;
@@ -400,7 +514,7 @@ __device__ __forceinline__ void trace_ray(const TraceArgs &a, uint32_t tid, bool
 	const int k = ray_begin(a, i, stream, s);
 	if (k == kRayMasked) return;
 	if (k == kRayTraverse)
-		while (!ray_step<ANY, TWO_LEVEL, COUNT, MM3, SMEM>(a, s, stack, keep, pol, cnt, top)) {
+		while (!ray_step<ANY, TWO_LEVEL, COUNT, MM3, SMEM, MOTION>(a, s, stack, keep, pol, cnt, top)) {
 		}
 	ray_write(a, i, s, stream);
 	if (COUNT) cnt.rays += 1;
@@ -477,6 +591,7 @@ template <bool ANY, bool TWO_LEVEL, uint32_t CV>
 __global__ void __launch_bounds__(kTraceBlock, 8) k_trace_fetch(TraceArgs a, uint32_t slot_index, uint32_t refill) {
 	constexpr bool MM3 = (CV & kVarMinMax3) != 0;
 	constexpr bool SMEM = (CV & kVarSmemStack) != 0;
+	constexpr bool MOTION = (CV & kVarMotion) != 0;
 	extern __shared__ uint2 s_stack_top[];  // kSmemStack entries per thread with SMEM_STACK, else empty
 	const StackTop top{s_stack_top + threadIdx.x, blockDim.x};
 	uint32_t *slot = g_queue[slot_index];
@@ -513,7 +628,7 @@ __global__ void __launch_bounds__(kTraceBlock, 8) k_trace_fetch(TraceArgs a, uin
 			if (drained) break;
 			continue;  // every lane idle: the next trip claims 32 rays
 		}
-		if (rid != kNull && ray_step<ANY, TWO_LEVEL, false, MM3, SMEM>(a, s, stack, keep, pol, cnt, top)) {
+		if (rid != kNull && ray_step<ANY, TWO_LEVEL, false, MM3, SMEM, MOTION>(a, s, stack, keep, pol, cnt, top)) {
 			ray_write(a, rid, s, stream);
 			rid = kNull;
 		}
@@ -742,6 +857,17 @@ __global__ void __launch_bounds__(kTraceBlock, 7) k_trace_queue_fetch(const __gr
 	release_slot(slot);
 }
 
+__global__ void k_set_flag(uint32_t *flag) {
+	__threadfence_system();
+	*reinterpret_cast<volatile uint32_t *>(flag) = 1u;
+}
+
+lrx_status launch_set_flag(uint32_t *flag, cudaStream_t st) {
+	k_set_flag<<<1, 1, 0, st>>>(flag);
+	LRX_CUDA(cudaGetLastError());
+	return LRX_OK;
+}
+
 lrx_status launch_trace_queue(const QueueParams &p, cudaStream_t st) {
 	if (p.total_tiles == 0) return LRX_OK;
 	static int resident = 0;  // 64-thread blocks resident per GB300 at this kernel's occupancy
@@ -815,6 +941,24 @@ lrx_status launch_trace(const TraceArgs &a, cudaStream_t st) {
 	}
 	const uint32_t grid = (a.count + bs - 1) / bs;
 	const bool cnt = a.counters != nullptr;
+	if (a.motion && a.two_level) {
+		// motion scenes: builds of their own (no MINMAX3 / SMEM_STACK / occupancy
+		// forms), so the static builds carry no motion code
+		if ((a.variant & kVarPersistent) && !cnt && a.count < 0x80000000u) {
+			const uint32_t fbs = std::min(bs, kTraceBlock);
+			return a.any_hit ? launch_fetch<true, true, kVarMotion>(a, fbs, st)
+					: launch_fetch<false, true, kVarMotion>(a, fbs, st);
+		}
+		if (a.any_hit) {
+			if (cnt) k_trace<true, true, true, kVarMotion><<<grid, bs, 0, st>>>(a);
+			else k_trace<true, true, false, kVarMotion><<<grid, bs, 0, st>>>(a);
+		} else {
+			if (cnt) k_trace<false, true, true, kVarMotion><<<grid, bs, 0, st>>>(a);
+			else k_trace<false, true, false, kVarMotion><<<grid, bs, 0, st>>>(a);
+		}
+		LRX_CUDA(cudaGetLastError());
+		return LRX_OK;
+	}
 	if ((a.variant & kVarPersistent) && !cnt && a.count < 0x80000000u) {
 		// persistent warps with ray fetch; block size capped at kTraceBlock
 		const uint32_t fbs = std::min(bs, kTraceBlock);

@@ -47,7 +47,8 @@ EXPORTED = ["lrx_abi_version", "lrx_last_error", "lrx_scene_create", "lrx_scene_
             "lrx_scene_autotune", "lrx_trace_batches_ex", "lrx_server_create", "lrx_server_destroy",
             "lrx_server_add_scene",
             "lrx_server_submit", "lrx_server_wait", "lrx_server_get_stats", "lrx_server_reset_stats",
-            "lrx_ply_load", "lrx_ply_free", "lrx_scene_key", "lrx_scene_save", "lrx_scene_load"]
+            "lrx_ply_load", "lrx_ply_free", "lrx_scene_key", "lrx_scene_save", "lrx_scene_load",
+            "lrx_scene_create_motion"]
 LRX_SERVE_BATCHED = 0
 LRX_SERVE_PLAIN = 1
 LRX_NOALLOC_MAX_RAYS = 131072
@@ -78,6 +79,11 @@ class TraceConfig(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_uint32), ("block_size", ctypes.c_uint32),
                 ("postpone", ctypes.c_uint32), ("variant", ctypes.c_uint32), ("modes", ctypes.c_uint32),
                 ("refill", ctypes.c_uint32)]
+
+
+class MotionDesc(ctypes.Structure):
+    _fields_ = [("object", ctypes.c_uint32), ("count", ctypes.c_uint32), ("times", ctypes.c_void_p),
+                ("transforms", ctypes.c_void_p)]
 
 
 class PlyMesh(ctypes.Structure):
@@ -118,6 +124,8 @@ def load(path: str | None = None):
         L.lrx_last_error.restype = ctypes.c_char_p
         L.lrx_scene_create.restype = st
         L.lrx_scene_create.argtypes = [vp, u32, vp, u32, vp, vp, ctypes.POINTER(vp)]
+        L.lrx_scene_create_motion.restype = st
+        L.lrx_scene_create_motion.argtypes = [vp, u32, vp, u32, vp, u32, vp, vp, ctypes.POINTER(vp)]
         L.lrx_scene_destroy.restype = st
         L.lrx_scene_destroy.argtypes = [vp]
         L.lrx_scene_update_instances.restype = st
@@ -192,12 +200,17 @@ def batch_array(batches):
     return arr
 
 
-def trace_batches(batches, stream: int = 0, arr=None):
+def trace_batches(batches, stream: int = 0, d_tile_counters: int = 0, d_done_flags: int = 0, arr=None):
     """lrx_trace_batches over (Scene, d_rays, d_hits, count, mode) tuples (or a
-    prebuilt batch_array)."""
+    prebuilt batch_array); with device addresses of per-batch counters and
+    flags, lrx_trace_batches_ex."""
     if arr is None:
         arr = batch_array(batches)
-    check(load().lrx_trace_batches(arr, len(batches), ctypes.c_void_p(stream)))
+    if d_tile_counters or d_done_flags:
+        check(load().lrx_trace_batches_ex(arr, len(batches), ctypes.c_void_p(stream), ctypes.c_void_p(d_tile_counters),
+                                          ctypes.c_void_p(d_done_flags)))
+    else:
+        check(load().lrx_trace_batches(arr, len(batches), ctypes.c_void_p(stream)))
 
 
 class ServerOpts(ctypes.Structure):
@@ -261,6 +274,8 @@ class Server:
             pass
 
     def add_scene(self, scene: W.SceneDesc) -> int:
+        if scene.has_motion:
+            raise ValueError("the server's scene registry takes static scenes only (no motion systems)")
         meshes, keep = _mesh_array(scene)
         objs = _object_array(scene)
         has_inst = scene.has_instances
@@ -294,12 +309,31 @@ def _object_array(scene: W.SceneDesc):
     objs = (ObjectDesc * max(1, len(scene.objects)))()
     for i, (mi, m) in enumerate(scene.objects):
         objs[i].mesh = mi
-        if m is not None:
+        if isinstance(m, W.Motion):
+            objs[i].flags = LRX_OBJECT_INSTANCE  # the motion system replaces the transform
+        elif m is not None:
             objs[i].flags = LRX_OBJECT_INSTANCE
             flat = np.asarray(m, np.float32).reshape(16)
             for k in range(16):
                 objs[i].transform[k] = float(flat[k])
     return objs
+
+
+def _motion_array(scene: W.SceneDesc, keep: list):
+    """lrx_motion_desc array of the scene's Motion objects."""
+    ms = [(i, m) for i, (_, m) in enumerate(scene.objects) if isinstance(m, W.Motion)]
+    arr = (MotionDesc * max(1, len(ms)))()
+    for k, (i, m) in enumerate(ms):
+        t = np.ascontiguousarray(m.times, np.float32).reshape(-1)
+        x = np.ascontiguousarray(m.transforms, np.float32).reshape(-1)
+        if x.size != 16 * t.size:
+            raise ValueError("motion: one 4x4 matrix per keyframe time")
+        keep += [t, x]
+        arr[k].object = i
+        arr[k].count = t.size
+        arr[k].times = t.ctypes.data
+        arr[k].transforms = x.ctypes.data
+    return arr, len(ms)
 
 
 def ply_load(path: str) -> W.Mesh:
@@ -355,8 +389,13 @@ class Scene:
         objs = _object_array(scene)
         opts = BuildOpts(ctypes.sizeof(BuildOpts), leaf_max, treelet_passes, 0)
         h = ctypes.c_void_p()
-        check(L.lrx_scene_create(meshes, len(scene.meshes), objs, len(scene.objects), ctypes.byref(opts),
-                                 ctypes.c_void_p(stream), ctypes.byref(h)))
+        if scene.has_motion:
+            motions, n_motion = _motion_array(scene, self._keep)
+            check(L.lrx_scene_create_motion(meshes, len(scene.meshes), objs, len(scene.objects), motions, n_motion,
+                                            ctypes.byref(opts), ctypes.c_void_p(stream), ctypes.byref(h)))
+        else:
+            check(L.lrx_scene_create(meshes, len(scene.meshes), objs, len(scene.objects), ctypes.byref(opts),
+                                     ctypes.c_void_p(stream), ctypes.byref(h)))
         self._keep = None  # the library copied the geometry
         self.handle = h
         self.desc = scene

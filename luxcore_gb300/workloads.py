@@ -73,11 +73,20 @@ class Mesh:
 
 
 @dataclass
+class Motion:
+    """Keyframes of a motion-blurred instance (a MotionTriangleMesh's motion
+    system): strictly increasing times and (n, 4, 4) row-major matrices that
+    map world space to the mesh's local space, sampled at each ray's time."""
+    times: np.ndarray
+    transforms: np.ndarray
+
+
+@dataclass
 class SceneDesc:
     """A luxrays DataSet: meshes plus ordered objects (plain or instanced).
 
-    objects[i] = (mesh index, 4x4 row-major local-to-world matrix or None);
-    meshIndex in a RayHit is the object's position in this list.
+    objects[i] = (mesh index, 4x4 row-major local-to-world matrix, a Motion,
+    or None); meshIndex in a RayHit is the object's position in this list.
     """
     meshes: list
     objects: list = field(default_factory=list)
@@ -89,6 +98,10 @@ class SceneDesc:
     @property
     def has_instances(self) -> bool:
         return any(m is not None for _, m in self.objects)
+
+    @property
+    def has_motion(self) -> bool:
+        return any(isinstance(m, Motion) for _, m in self.objects)
 
     def triangle_count(self) -> int:
         """Effective triangles (instances counted once per instance)."""
@@ -396,6 +409,66 @@ def config3(n_rays: int = 1 << 23, seed: int = BASE_SEED + 2, **kw):
     closest = random_rays(n_rays, seed, extent=ext, stream=8)
     anyhit = random_rays(n_rays, seed, extent=ext, stream=9)
     anyhit["maxt"] = Rng(seed, 10).uniform(n_rays, 0.5, 5.0)
+    return scene, closest, anyhit
+
+
+def motion_scene(n_meshes: int = 16, freq: int = 100, n_inst: int = 4096, seed: int = BASE_SEED + 4,
+                 scale=(0.01, 0.05), extent: float = 10.0, kinds=("translate", "rigid", "static"),
+                 speed: float = 0.05) -> SceneDesc:
+    """instanced_scene with motion blur: instance k becomes a Motion of kind
+    kinds[k % len(kinds)] over the shutter [0, 1] --
+      "translate": two keyframes moving by up to `speed` * extent (the
+                   world->local matrices differ in translation only);
+      "rigid":     three keyframes (times 0, 0.5, 1) turning about a random
+                   axis by up to 90 degrees, scaling by up to 1.5x and moving;
+      "static":    a plain instance (its local->world matrix).
+    Keyframes are world->local: the float64 inverse of the local->world
+    matrix at that time, rounded to float32."""
+    base = instanced_scene(n_meshes, freq, n_inst, seed, scale, extent)
+    rng = Rng(seed, 12)
+    cz = rng.uniform(n_inst, -1.0, 1.0).astype(np.float64)
+    az = rng.uniform(n_inst, 0.0, 2.0 * math.pi).astype(np.float64)
+    axis = np.stack([np.sqrt(1 - cz * cz) * np.cos(az), np.sqrt(1 - cz * cz) * np.sin(az), cz], 1)
+    ang = rng.uniform(n_inst, 0.0, 0.5 * math.pi).astype(np.float64)
+    grow = rng.uniform(n_inst, 1.0, 1.5).astype(np.float64)
+    move = rng.uniform(3 * n_inst, -1.0, 1.0).reshape(n_inst, 3).astype(np.float64) * speed * extent
+
+    def turn(k, a):
+        x, y, z = axis[k]
+        c, s = math.cos(a), math.sin(a)
+        return np.array([[c + x * x * (1 - c), x * y * (1 - c) - z * s, x * z * (1 - c) + y * s],
+                         [y * x * (1 - c) + z * s, c + y * y * (1 - c), y * z * (1 - c) - x * s],
+                         [z * x * (1 - c) - y * s, z * y * (1 - c) + x * s, c + z * z * (1 - c)]])
+
+    objects = []
+    for k, (mi, m) in enumerate(base.objects):
+        kind = kinds[k % len(kinds)]
+        m = m.astype(np.float64)
+        if kind == "static":
+            objects.append((mi, m.astype(np.float32)))
+            continue
+        times = [0.0, 1.0] if kind == "translate" else [0.0, 0.5, 1.0]
+        keys = []
+        for t in times:
+            lw = m.copy()
+            if kind == "rigid":
+                lw[:3, :3] = turn(k, ang[k] * t) @ m[:3, :3] * (1.0 + (grow[k] - 1.0) * t)
+            lw[:3, 3] = m[:3, 3] + move[k] * t
+            keys.append(np.linalg.inv(lw))
+        objects.append((mi, Motion(np.asarray(times, np.float32), np.stack(keys).astype(np.float32))))
+    return SceneDesc(base.meshes, objects)
+
+
+def config_motion(n_rays: int = 1 << 23, seed: int = BASE_SEED + 4, time_range=(0.0, 1.0), **kw):
+    """Motion-blurred instances (motion_scene) with closest-hit and any-hit
+    rays whose times are uniform over `time_range`."""
+    scene = motion_scene(seed=seed, **kw)
+    ext = kw.get("extent", 10.0)
+    closest = random_rays(n_rays, seed, extent=ext, stream=13)
+    anyhit = random_rays(n_rays, seed, extent=ext, stream=14)
+    anyhit["maxt"] = Rng(seed, 15).uniform(n_rays, 0.5, 5.0)
+    closest["time"] = Rng(seed, 16).uniform(n_rays, *time_range)
+    anyhit["time"] = Rng(seed, 17).uniform(n_rays, *time_range)
     return scene, closest, anyhit
 
 

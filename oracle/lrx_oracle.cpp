@@ -20,6 +20,8 @@
 #include <thread>
 #include <vector>
 
+#include "lrx_oracle_motion.h"
+
 namespace orc {
 
 static const uint32_t NULL_INDEX = 0xffffffffu;
@@ -509,14 +511,37 @@ struct Object {
 	uint32_t mesh;
 	bool instance;
 	float m[4][4], mInv[4][4];
+	int motion = -1;  // index of the object's MotionSystem (a MotionTriangleMesh), else -1
 };
+
+// MotionSystem::Bound / InterpolatedTransform::Bound (motionsystem.cpp:74-86,
+// :356-365) with storingGlobal2Local: every sampled world->local matrix is
+// inverted and the box transformed by it.
+static BBox motion_bound(const orc_motion::MotionSystem &ms, const BBox &ibox) {
+	BBox result;
+	for (const orc_motion::InterpolatedTransform &it : ms.interpolatedTransforms) {
+		BBox tbox;
+		const float N = 1024.f;
+		for (float i = 0; i <= N; ++i) {
+			const float t = orc_motion::Lerp(i / N, it.startTime, it.endTime);
+			float m[4][4], inv[4][4];
+			it.Sample(t, m);
+			if (!matrix_inverse(m, inv)) throw std::runtime_error("Singular matrix in motion bound");
+			tbox = Union(tbox, xform_bbox(inv, ibox));
+		}
+		result = Union(result, tbox);
+	}
+	return result;
+}
 
 struct MBVHAccel {
 	const std::vector<Object> *objects = nullptr;
 	const std::vector<Mesh> *meshes = nullptr;
+	const std::vector<orc_motion::MotionSystem> *motions = nullptr;
 	std::vector<BVHAccel> uniqueLeafs;
 	std::vector<std::vector<const Mesh *>> leafMeshLists;
 	std::vector<uint32_t> uniqueLeafsTransform;  // object index of each transform
+	std::vector<uint32_t> uniqueLeafsMotionSystem;  // object index of each motion system
 	std::vector<ArrayNode> root;
 
 	// trianglemesh.cpp:72-83 and :241-248
@@ -525,24 +550,27 @@ struct MBVHAccel {
 		BBox b;
 		for (uint32_t i = 0; i < m.nVerts; ++i) b = Union(b, m.verts[i]);
 		if (o.instance) b = xform_bbox(o.m, b);
+		else if (o.motion >= 0) b = motion_bound((*motions)[o.motion], b);  // trianglemesh.cpp:268-275
 		return b;
 	}
 
 	// mbvhaccel.cpp:58-216
-	void init(const std::vector<Object> &objs, const std::vector<Mesh> &ms, const Params &params) {
+	void init(const std::vector<Object> &objs, const std::vector<Mesh> &ms,
+			const std::vector<orc_motion::MotionSystem> &mss, const Params &params) {
 		objects = &objs;
 		meshes = &ms;
+		motions = &mss;
 		size_t totalTris = 0;
 		for (const Object &o : objs) totalTris += ms[o.mesh].nTris;
 		if (totalTris == 0) return;
 		const uint32_t nLeafs = (uint32_t)objs.size();
-		std::vector<uint32_t> leafsIndex, leafsTransformIndex;
+		std::vector<uint32_t> leafsIndex, leafsTransformIndex, leafsMotionSystemIndex;
 		std::map<uint32_t, uint32_t> uniqueLeafIndexByMesh;
 		uniqueLeafs.reserve(nLeafs);
 		leafMeshLists.reserve(nLeafs);
 		for (uint32_t i = 0; i < nLeafs; ++i) {
 			const Object &o = objs[i];
-			if (!o.instance) {
+			if (!o.instance && o.motion < 0) {
 				const uint32_t u = (uint32_t)uniqueLeafs.size();
 				leafMeshLists.push_back({&ms[o.mesh]});
 				uniqueLeafs.emplace_back();
@@ -550,6 +578,7 @@ struct MBVHAccel {
 				uniqueLeafIndexByMesh[o.mesh] = u;
 				leafsIndex.push_back(u);
 				leafsTransformIndex.push_back(NULL_INDEX);
+				leafsMotionSystemIndex.push_back(NULL_INDEX);
 			} else {
 				auto it = uniqueLeafIndexByMesh.find(o.mesh);
 				if (it == uniqueLeafIndexByMesh.end()) {
@@ -562,8 +591,15 @@ struct MBVHAccel {
 				} else {
 					leafsIndex.push_back(it->second);
 				}
-				leafsTransformIndex.push_back((uint32_t)uniqueLeafsTransform.size());
-				uniqueLeafsTransform.push_back(i);
+				if (o.instance) {
+					leafsTransformIndex.push_back((uint32_t)uniqueLeafsTransform.size());
+					uniqueLeafsTransform.push_back(i);
+					leafsMotionSystemIndex.push_back(NULL_INDEX);
+				} else {
+					leafsTransformIndex.push_back(NULL_INDEX);
+					leafsMotionSystemIndex.push_back((uint32_t)uniqueLeafsMotionSystem.size());
+					uniqueLeafsMotionSystem.push_back(i);
+				}
 			}
 		}
 		// leafMeshLists must not reallocate after init() captured pointers
@@ -577,20 +613,28 @@ struct MBVHAccel {
 			l->bbox.expand(eps(l->bbox));
 			l->a = leafsIndex[i];
 			l->b = leafsTransformIndex[i];
-			l->c = NULL_INDEX;
+			l->c = leafsMotionSystemIndex[i];
 			l->d = i;
 			bvhLeafsList[i] = l;
 		}
 		root = build_bvh_nodes(params, nullptr, bvhLeafsList);
 	}
 
-	// transform.h:259-262 via mbvhaccel.cpp:325
-	Ray local_ray(const Ray &ray, uint32_t transformIndex) const {
-		if (transformIndex == NULL_INDEX) return ray;
-		const Object &o = (*objects)[uniqueLeafsTransform[transformIndex]];
+	// transform.h:259-262 via mbvhaccel.cpp:324-327; a motion leaf applies
+	// its system's Sample(ray.time) (matrix4x4op.h:80-82)
+	Ray local_ray(const Ray &ray, uint32_t transformIndex, uint32_t motionIndex) const {
 		Ray r = ray;
-		r.o = xform_point(o.mInv, ray.o);
-		r.d = xform_vector(o.mInv, ray.d);
+		if (transformIndex != NULL_INDEX) {
+			const Object &o = (*objects)[uniqueLeafsTransform[transformIndex]];
+			r.o = xform_point(o.mInv, ray.o);
+			r.d = xform_vector(o.mInv, ray.d);
+		} else if (motionIndex != NULL_INDEX) {
+			const Object &o = (*objects)[uniqueLeafsMotionSystem[motionIndex]];
+			float m[4][4];
+			(*motions)[o.motion].Sample(ray.time, m);
+			r.o = xform_point(m, ray.o);
+			r.d = xform_vector(m, ray.d);
+		}
 		return r;
 	}
 
@@ -650,7 +694,7 @@ struct MBVHAccel {
 				} else {
 					currentLeaf = &uniqueLeafs[node.bvhLeaf.leafIndex];
 					currentTree = currentLeaf->tree.data();
-					currentRay = local_ray(ray, node.bvhLeaf.transformIndex);
+					currentRay = local_ray(ray, node.bvhLeaf.transformIndex, node.bvhLeaf.motionIndex);
 					currentRay.maxt = hit->t;
 					currentMeshOffset = node.bvhLeaf.meshOffsetIndex;
 					currentRootNode = currentNode + 1;
@@ -674,6 +718,7 @@ struct Scene {
 	std::vector<uint32_t> tris;
 	std::vector<Mesh> meshes;
 	std::vector<Object> objects;
+	std::vector<orc_motion::MotionSystem> motions;
 	int accel = ORC_ACCEL_BVH;
 	BVHAccel bvh;
 	std::vector<const Mesh *> bvhMeshes;
@@ -687,10 +732,16 @@ struct Scene {
 	// Ray in the local space of object `oi`, as MBVHAccel::Intersect forms it
 	Ray object_ray(const Ray &r, uint32_t oi) const {
 		const Object &o = objects[oi];
-		if (!o.instance) return r;
 		Ray lr = r;
-		lr.o = xform_point(o.mInv, r.o);
-		lr.d = xform_vector(o.mInv, r.d);
+		if (o.instance) {
+			lr.o = xform_point(o.mInv, r.o);
+			lr.d = xform_vector(o.mInv, r.d);
+		} else if (o.motion >= 0) {
+			float m[4][4];
+			motions[o.motion].Sample(r.time, m);
+			lr.o = xform_point(m, r.o);
+			lr.d = xform_vector(m, r.d);
+		}
 		return lr;
 	}
 };
@@ -752,6 +803,14 @@ void *orc_scene_create(const float *verts, const uint64_t *vert_offsets,
 		const uint32_t *tris, const uint64_t *tri_offsets, uint32_t n_meshes,
 		const orc_object *objs, uint32_t n_objs, int accel, int tree_type,
 		char *err, uint64_t err_len) {
+	return orc_scene_create_motion(verts, vert_offsets, tris, tri_offsets, n_meshes, objs, n_objs,
+			nullptr, 0, accel, tree_type, err, err_len);
+}
+
+void *orc_scene_create_motion(const float *verts, const uint64_t *vert_offsets,
+		const uint32_t *tris, const uint64_t *tri_offsets, uint32_t n_meshes,
+		const orc_object *objs, uint32_t n_objs, const orc_motion_desc *mds, uint32_t n_motions,
+		int accel, int tree_type, char *err, uint64_t err_len) {
 	auto fail = [&](const std::string &msg) -> void * {
 		if (err && err_len) std::snprintf(err, err_len, "%s", msg.c_str());
 		return nullptr;
@@ -789,15 +848,27 @@ void *orc_scene_create(const float *verts, const uint64_t *vert_offsets,
 			if (o.mesh >= n_meshes) { delete s; return fail("object mesh index out of range"); }
 			if (o.instance && !matrix_inverse(o.m, o.mInv)) { delete s; return fail("singular instance transform"); }
 		}
+		for (uint32_t k = 0; k < n_motions; ++k) {
+			const orc_motion_desc &md = mds[k];
+			if (md.object >= no || md.count == 0) { delete s; return fail("bad motion object or keyframe count"); }
+			Object &o = s->objects[md.object];
+			if (o.motion >= 0) { delete s; return fail("object has two motion systems"); }
+			std::vector<float> times(md.times, md.times + md.count);
+			std::vector<const float (*)[4]> mats;
+			for (uint32_t j = 0; j < md.count; ++j) mats.push_back(reinterpret_cast<const float (*)[4]>(md.transforms + 16ull * j));
+			s->motions.emplace_back(times, mats);  // throws on a singular keyframe
+			o.instance = false;
+			o.motion = (int)s->motions.size() - 1;
+		}
 		run_big_stack([&]() {
 			if (accel == ORC_ACCEL_BVH) {
 				for (const Object &o : s->objects) {
-					if (o.instance) throw std::runtime_error("BVH accelerator does not support instances");
+					if (o.instance || o.motion >= 0) throw std::runtime_error("BVH accelerator does not support instances");
 					s->bvhMeshes.push_back(&s->meshes[o.mesh]);
 				}
 				s->bvh.init(s->bvhMeshes, s->params);
 			} else {
-				s->mbvh.init(s->objects, s->meshes, s->params);
+				s->mbvh.init(s->objects, s->meshes, s->motions, s->params);
 			}
 		});
 		return s;

@@ -69,6 +69,19 @@ void *orc_scene_create(const float *verts, const uint64_t *vert_offsets,
 		const uint32_t *tris, const uint64_t *tri_offsets, uint32_t n_meshes,
 		const orc_object *objs, uint32_t n_objs, int accel, int tree_type,
 		char *err, uint64_t err_len);
+/* As orc_scene_create, with motion systems: motion k makes object
+ * mds[k].object a MotionTriangleMesh of its mesh whose MotionSystem has
+ * mds[k].count keyframes (times, row-major world->local matrices, 16 floats
+ * each). The object's has_transform is ignored. */
+typedef struct {
+	uint32_t object, count;
+	const float *times;
+	const float *transforms;
+} orc_motion_desc;
+void *orc_scene_create_motion(const float *verts, const uint64_t *vert_offsets,
+		const uint32_t *tris, const uint64_t *tri_offsets, uint32_t n_meshes,
+		const orc_object *objs, uint32_t n_objs, const orc_motion_desc *mds, uint32_t n_motions,
+		int accel, int tree_type, char *err, uint64_t err_len);
 void orc_scene_destroy(void *scene);
 
 /* Accelerator::Intersect over a ray array, split across n_threads

@@ -29,11 +29,17 @@ class OrcObject(ctypes.Structure):
                 ("m", ctypes.c_float * 16)]
 
 
+class OrcMotionDesc(ctypes.Structure):
+    _fields_ = [("object", ctypes.c_uint32), ("count", ctypes.c_uint32), ("times", ctypes.c_void_p),
+                ("transforms", ctypes.c_void_p)]
+
+
 def build(force: bool = False) -> str:
     """Compile the oracle with g++ (-O2 -ffp-contract=off, no fast math)."""
     src = os.path.join(HERE, "lrx_oracle.cpp")
+    deps = [src] + [os.path.join(HERE, h) for h in ("lrx_oracle.h", "lrx_oracle_motion.h")]
     if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= max(
-            os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "lrx_oracle.h"))):
+            os.path.getmtime(d) for d in deps):
         return LIB_PATH
     os.makedirs(os.path.dirname(LIB_PATH), exist_ok=True)
     tmp = LIB_PATH + f".tmp{os.getpid()}"
@@ -53,6 +59,9 @@ def lib():
             L.orc_scene_create.restype = vp
             L.orc_scene_create.argtypes = [vp, vp, vp, vp, u32, vp, u32, ctypes.c_int, ctypes.c_int,
                                            ctypes.c_char_p, u64]
+            L.orc_scene_create_motion.restype = vp
+            L.orc_scene_create_motion.argtypes = [vp, vp, vp, vp, u32, vp, u32, vp, u32, ctypes.c_int,
+                                                  ctypes.c_int, ctypes.c_char_p, u64]
             L.orc_scene_destroy.argtypes = [vp]
             L.orc_intersect.restype = ctypes.c_double
             L.orc_intersect.argtypes = [vp, vp, vp, u64, ctypes.c_int]
@@ -92,17 +101,28 @@ class OracleScene:
         self._vo[1:] = np.cumsum([v.shape[0] for v in verts])
         self._to[1:] = np.cumsum([t.shape[0] for t in tris])
         objs = (OrcObject * max(1, len(scene.objects)))()
+        motions = []
         for i, (mi, m) in enumerate(scene.objects):
             objs[i].mesh = mi
-            objs[i].has_transform = 0 if m is None else 1
-            if m is not None:
+            if m is not None and hasattr(m, "times"):
+                motions.append((i, m))
+            elif m is not None:
+                objs[i].has_transform = 1
                 flat = np.asarray(m, np.float32).reshape(16)
                 for k in range(16):
                     objs[i].m[k] = float(flat[k])
+        mds = (OrcMotionDesc * max(1, len(motions)))()
+        self._motion_keep = []
+        for k, (i, m) in enumerate(motions):
+            t = np.ascontiguousarray(m.times, np.float32).reshape(-1)
+            x = np.ascontiguousarray(m.transforms, np.float32).reshape(-1)
+            self._motion_keep += [t, x]
+            mds[k].object, mds[k].count = i, t.shape[0]
+            mds[k].times, mds[k].transforms = t.ctypes.data, x.ctypes.data
         err = ctypes.create_string_buffer(512)
-        self.handle = L.orc_scene_create(_ptr(self._verts), _ptr(self._vo), _ptr(self._tris), _ptr(self._to),
-                                         len(scene.meshes), objs, len(scene.objects), accel, tree_type,
-                                         err, 512)
+        self.handle = L.orc_scene_create_motion(_ptr(self._verts), _ptr(self._vo), _ptr(self._tris), _ptr(self._to),
+                                                len(scene.meshes), objs, len(scene.objects), mds, len(motions),
+                                                accel, tree_type, err, 512)
         if not self.handle:
             raise RuntimeError("oracle scene build failed: " + err.value.decode())
         self.accel = accel

@@ -1,0 +1,198 @@
+"""Motion-blurred instances (lrx_scene_create_motion) against the oracle's
+MotionSystem restatement.
+
+Translation-only keyframes take the reference's lerp path with every
+operation rounded as on the CPU, so those rays meet the full parity bar
+bit-for-bit.  Rotating keyframes go through Slerp, whose acosf / sinf are
+CUDA's on the GPU and the C library's in the oracle: the sampled matrices
+can differ in the last bits, so those rays are held to a tolerance (hits
+agree on >= 99.9 % of rays; t, b1, b2 within 1e-4 relative; every
+disagreement a near-tie or a hit the oracle confirms within 1e-4)."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+
+from luxcore_gb300 import lrx  # noqa: E402
+from luxcore_gb300 import workloads as W  # noqa: E402
+from oracle import pyoracle as po  # noqa: E402
+from parity import check_anyhit, compare  # noqa: E402
+from test_trace_gpu import SENT, gpu_trace, make_scene  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+MOTION_KERNELS = pytest.mark.parametrize("kernel", [(64, 8, 0), (128, 0, 0x40, 8), (64, 8, 0x10), (64, 8, 0x140, 8),
+                                                    (64, 8, 0x4F)],
+                                         ids=["b64-p8", "b128-persistent", "b64-sorted", "b64-persistent-compact",
+                                              "b64-allbits"])
+TOL_AGREE = 0.999
+TOL_REL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def torch_cuda(cuda_ready):
+    import torch
+    return torch
+
+
+def small_motion(kinds, time_range=(0.0, 1.0), n_rays=1 << 15, seed=W.BASE_SEED + 40):
+    return W.config_motion(n_rays=n_rays, seed=seed, n_meshes=4, freq=12, n_inst=300, extent=3.0,
+                           scale=(0.1, 0.4), kinds=kinds, time_range=time_range)
+
+
+def tolerant_compare(gpu, ref, oracle, rays):
+    """Hits of rays whose instance matrices may differ in the last bits."""
+    hg = gpu["meshIndex"] != W.NULL_INDEX
+    same = (gpu["meshIndex"] == ref["meshIndex"]) & (gpu["triangleIndex"] == ref["triangleIndex"])
+    agree = float(same.mean())
+    both = same & hg
+    rel = lambda a, b: np.abs(a.astype(np.float64) - b) <= TOL_REL * np.maximum(np.abs(b.astype(np.float64)), 1e-3)
+    vals = bool(rel(gpu["t"][both], ref["t"][both]).all() and rel(gpu["b1"][both], ref["b1"][both]).all()
+                and rel(gpu["b2"][both], ref["b2"][both]).all())
+    bad = 0
+    for i in np.nonzero(~same)[0]:
+        if hg[i]:
+            ok, t, _, _ = oracle.triangle_hit(rays[i], int(gpu["meshIndex"][i]), int(gpu["triangleIndex"][i]))
+            near = abs(float(gpu["t"][i]) - float(ref["t"][i])) <= TOL_REL * max(abs(float(ref["t"][i])), 1e-3)
+            if not (near or (ok and abs(t - float(gpu["t"][i])) <= TOL_REL * max(abs(t), 1e-3))):
+                bad += 1
+    return {"agree": agree, "values_ok": vals, "unexplained": bad,
+            "ok": agree >= TOL_AGREE and vals and bad <= max(2, int(1e-4 * gpu.shape[0]))}
+
+
+@MOTION_KERNELS
+def test_translating_instances_bit_exact(torch_cuda, kernel):
+    """Translation-only motion (and static instances beside it): full parity,
+    t bit-exact, rays before, inside and after the shutter."""
+    scene, closest, anyr = small_motion(("translate", "static"), time_range=(-0.25, 1.25))
+    s = make_scene(scene, kernel)
+    assert s.info()["two_level"] == 1
+    oracle = po.OracleScene(scene)
+    ref, _ = oracle.intersect(closest)
+    gpu = gpu_trace(torch_cuda, s, closest)
+    st = compare(gpu, ref, oracle, closest)
+    assert st["ok"] and st["hit_rate"] > 0.1, st
+    assert st["bitexact_t"] == 1.0, st
+    ref_a, _ = oracle.intersect(anyr)
+    gpu_a = gpu_trace(torch_cuda, s, anyr, lrx.LRX_TRACE_ANY)
+    a = check_anyhit(gpu_a, ref_a, oracle, anyr)
+    assert a["ok"], a
+
+
+@MOTION_KERNELS
+def test_rigid_motion_within_tolerance(torch_cuda, kernel):
+    """Rotating, scaling and moving instances with three keyframes."""
+    scene, closest, anyr = small_motion(("rigid", "translate", "static"), time_range=(-0.1, 1.1))
+    s = make_scene(scene, kernel)
+    oracle = po.OracleScene(scene)
+    ref, _ = oracle.intersect(closest)
+    gpu = gpu_trace(torch_cuda, s, closest)
+    st = tolerant_compare(gpu, ref, oracle, closest)
+    assert st["ok"], st
+    assert (ref["meshIndex"] != W.NULL_INDEX).mean() > 0.1
+    ref_a, _ = oracle.intersect(anyr)
+    gpu_a = gpu_trace(torch_cuda, s, anyr, lrx.LRX_TRACE_ANY)
+    hm = ((gpu_a["meshIndex"] != W.NULL_INDEX) == (ref_a["meshIndex"] != W.NULL_INDEX)).mean()
+    assert hm >= TOL_AGREE, hm
+
+
+def test_motion_rays_ignore_time_on_static_scenes_and_nan_time(torch_cuda):
+    """A NaN time gives NaN motion matrices (no hit on a moving instance) and
+    leaves static objects hittable, in the GPU and the oracle alike; times on
+    a scene without motion change nothing."""
+    scene, closest, _ = small_motion(("translate", "static"), n_rays=1 << 13)
+    closest["time"][::3] = np.nan
+    s = lrx.Scene(scene)
+    oracle = po.OracleScene(scene)
+    ref, _ = oracle.intersect(closest)
+    gpu = gpu_trace(torch_cuda, s, closest)
+    st = compare(gpu, ref, oracle, closest)
+    assert st["ok"], st
+    nan_hits = gpu["meshIndex"][::3]
+    nan_hits = nan_hits[nan_hits != W.NULL_INDEX]
+    assert nan_hits.size and np.all(nan_hits % 2 == 1)  # only the static (odd) instances
+    static, rays = W.config1(n_tris=5000, n_rays=8192, seed=41)
+    a = lrx.Scene(static)
+    rays_t = rays.copy()
+    rays_t["time"] = np.linspace(-5, 5, rays.shape[0], dtype=np.float32)
+    assert np.array_equal(gpu_trace(torch_cuda, a, rays).view(np.uint32),
+                          gpu_trace(torch_cuda, a, rays_t).view(np.uint32))
+
+
+def test_single_keyframe_equals_static_instance(torch_cuda):
+    """One keyframe equal to the reference's Inverse(transform) samples to
+    that matrix at every time, so closest hits equal the static instance's
+    bit-for-bit."""
+    static, closest, _ = W.config3(n_rays=1 << 14, n_meshes=3, freq=10, n_inst=150, extent=3.0, scale=(0.1, 0.4))
+    objs = []
+    for mi, m in static.objects:
+        inv = po.matrix_inverse(np.asarray(m, np.float32))
+        objs.append((mi, W.Motion(np.array([0.5], np.float32), inv.reshape(1, 4, 4))))
+    moving = W.SceneDesc(static.meshes, objs)
+    closest["time"] = np.linspace(-1, 2, closest.shape[0], dtype=np.float32)
+    a, b = lrx.Scene(static), lrx.Scene(moving)
+    ha, hb = gpu_trace(torch_cuda, a, closest), gpu_trace(torch_cuda, b, closest)
+    assert (ha["meshIndex"] != W.NULL_INDEX).mean() > 0.1
+    assert np.array_equal(ha.view(np.uint32), hb.view(np.uint32))
+
+
+def test_motion_batches_blobs_and_updates(torch_cuda):
+    """Motion scenes in lrx_trace_batches (mixed with static scenes, with
+    completion flags), saved and loaded as blobs, and after an instance
+    update of their static instances: all equal plain traces."""
+    torch = torch_cuda
+    scene, closest, anyr = small_motion(("rigid", "static"), n_rays=1 << 14)
+    flat, frays = W.config1(n_tris=20000, n_rays=1 << 14, seed=42)
+    m = lrx.Scene(scene)
+    f = lrx.Scene(flat)
+    want = [gpu_trace(torch, m, closest), gpu_trace(torch, f, frays), gpu_trace(torch, m, anyr, lrx.LRX_TRACE_ANY)]
+    jobs = [(m, closest, lrx.LRX_TRACE_CLOSEST), (f, frays, lrx.LRX_TRACE_CLOSEST), (m, anyr, lrx.LRX_TRACE_ANY)]
+    bufs = []
+    for sc, r, mode in jobs:
+        d_r = torch.from_numpy(r.view(np.uint8).reshape(-1).copy()).cuda()
+        d_h = torch.empty(r.shape[0] * 20, dtype=torch.uint8, device="cuda")
+        d_h.view(torch.int32).fill_(np.int32(np.uint32(SENT).view(np.int32)).item())
+        bufs.append((sc, d_r, d_h, r.shape[0], mode))
+    tiles = torch.zeros(len(jobs), dtype=torch.int32, device="cuda")
+    flags = torch.zeros(len(jobs), dtype=torch.int32, device="cuda")
+    lrx.trace_batches([(sc, d_r.data_ptr(), d_h.data_ptr(), n, mode) for sc, d_r, d_h, n, mode in bufs],
+                      torch.cuda.current_stream().cuda_stream, tiles.data_ptr(), flags.data_ptr())
+    torch.cuda.synchronize()
+    assert flags.cpu().tolist() == [1, 1, 1]
+    for w, (_, _, d_h, _, _) in zip(want, bufs):
+        assert np.array_equal(w.view(np.uint32), d_h.cpu().numpy().view(np.uint32))
+    # blob round trip keeps the motion systems
+    b = lrx.Scene.from_blob(m.save(), desc=scene)
+    assert np.array_equal(want[0].view(np.uint32), gpu_trace(torch, b, closest).view(np.uint32))
+    # an update that leaves every instance in place changes nothing
+    m.update_instances(scene)
+    assert np.array_equal(want[0].view(np.uint32), gpu_trace(torch, m, closest).view(np.uint32))
+
+
+def test_motion_argument_errors(torch_cuda):
+    scene, _, _ = small_motion(("translate", "static"), n_rays=64)
+    k = next(i for i, (_, mo) in enumerate(scene.objects) if isinstance(mo, W.Motion))
+    mo = scene.objects[k][1]
+
+    def with_motion(new):
+        objs = list(scene.objects)
+        objs[k] = (objs[k][0], new)
+        return W.SceneDesc(scene.meshes, objs)
+
+    bad = [
+        W.Motion(np.array([1.0, 0.0], np.float32), mo.transforms),               # decreasing times
+        W.Motion(np.array([0.5, 0.5], np.float32), mo.transforms),               # repeated time
+        W.Motion(np.array([0.0, np.nan], np.float32), mo.transforms),            # NaN time
+        W.Motion(np.array([0.0, 1.0], np.float32), np.zeros((2, 4, 4), np.float32)),  # singular keyframe
+        W.Motion(np.zeros(0, np.float32), np.zeros((0, 4, 4), np.float32)),      # no keyframe
+    ]
+    for b in bad:
+        with pytest.raises(lrx.LrxError):
+            lrx.Scene(with_motion(b))
+    with pytest.raises(ValueError):
+        lrx.Server().add_scene(scene)
