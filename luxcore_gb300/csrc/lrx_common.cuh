@@ -65,17 +65,24 @@ constexpr uint32_t kInstMotion = 2u;
 // One InterpolatedTransform of a motion system (motionsystem.cpp:33-160),
 // decomposed on the host: start/end matrices, the rotation matrix of the
 // start decomposition, scales, translations and unit quaternions (w,x,y,z).
+// The parts of Slerp (quaternion.cpp:143-165) that depend only on the two
+// quaternions -- the sign of their dot product, which branch it takes, and
+// phi = acosf(|dot|), sinf(phi) -- are evaluated once on the host.
 struct alignas(16) MotionInterval {
 	uint32_t flags;
-	float start_time, end_time, pad;
+	float start_time, end_time, phi;
 	float start_m[16], end_m[16], start_r[16];
 	float s0[3], t0[3], s1[3], t1[3];
 	float q0[4], q1[4];
+	float sin_phi, pad[3];
 };
-static_assert(sizeof(MotionInterval) == 288, "MotionInterval is 288 bytes");
+static_assert(sizeof(MotionInterval) == 304, "MotionInterval is 304 bytes");
 // MotionInterval::flags
 constexpr uint32_t kMiActive = 1u, kMiRotation = 2u, kMiTransX = 4u, kMiTransY = 8u, kMiTransZ = 16u,
 		   kMiScaleX = 32u, kMiScaleY = 64u, kMiScaleZ = 128u;
+// Slerp of this interval: kMiSlerpLinear when 1 - |dot(q0, q1)| <= 1e-6
+// (plain lerp weights), kMiSlerpNegate when dot(q0, q1) <= 0 (q1 negated)
+constexpr uint32_t kMiSlerpLinear = 0x100u, kMiSlerpNegate = 0x200u;
 constexpr uint32_t kMiTrans = kMiTransX | kMiTransY | kMiTransZ, kMiScale = kMiScaleX | kMiScaleY | kMiScaleZ;
 
 #if defined(__CUDACC__)

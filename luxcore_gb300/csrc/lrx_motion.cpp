@@ -177,16 +177,28 @@ Quat quat_normalize(const Quat &q) {
 	return {q.w * f, f * q.x, f * q.y, f * q.z};
 }
 
-Quat slerp(float t, const Quat &q1, const Quat &q2) {
+// The interval's constant part of Slerp: its flags and phi, sinf(phi).
+void slerp_setup(const Quat &q1, const Quat &q2, MotionInterval &it) {
 	float cos_phi = qdot(q1, q2);
 	const float sign = (cos_phi > 0.f) ? 1.f : -1.f;
 	cos_phi *= sign;
-	float f1, f2;
+	if (sign < 0.f) it.flags |= kMiSlerpNegate;
 	if (1.f - cos_phi > 1e-6f) {
-		const float phi = std::acos(cos_phi);
-		const float sin_phi = std::sin(phi);
-		f1 = std::sin((1.f - t) * phi) / sin_phi;
-		f2 = std::sin(t * phi) / sin_phi;
+		it.phi = std::acos(cos_phi);
+		it.sin_phi = std::sin(it.phi);
+	} else {
+		it.flags |= kMiSlerpLinear;
+	}
+}
+
+// Slerp at t from the interval's quaternions and slerp_setup's constants
+Quat slerp(float t, const MotionInterval &it) {
+	const Quat q1{it.q0[0], it.q0[1], it.q0[2], it.q0[3]}, q2{it.q1[0], it.q1[1], it.q1[2], it.q1[3]};
+	const float sign = (it.flags & kMiSlerpNegate) ? -1.f : 1.f;
+	float f1, f2;
+	if (!(it.flags & kMiSlerpLinear)) {
+		f1 = std::sin((1.f - t) * it.phi) / it.sin_phi;
+		f2 = std::sin(t * it.phi) / it.sin_phi;
 	} else {
 		f1 = 1.f - t;
 		f2 = t;
@@ -246,6 +258,7 @@ bool make_interval(float st, float et, const float *s, const float *e, MotionInt
 	if (std::fabs(qdot(q0, q1) - 1.f) >= 1e-6f) f |= kMiRotation;
 	if (f) f |= kMiActive;
 	it.flags = f;
+	slerp_setup(q0, q1, it);
 	return true;
 }
 
@@ -269,8 +282,7 @@ void sample_interval(const MotionInterval &it, float time, M44 &out) {
 		return;
 	}
 	if (it.flags & kMiRotation) {
-		const Quat q = slerp(le, Quat{it.q0[0], it.q0[1], it.q0[2], it.q0[3]}, Quat{it.q1[0], it.q1[1], it.q1[2], it.q1[3]});
-		quat_to_matrix(q, out);
+		quat_to_matrix(slerp(le, it), out);
 	} else {
 		std::memcpy(out, it.start_r, sizeof(M44));
 	}

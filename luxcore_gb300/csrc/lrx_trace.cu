@@ -233,10 +233,11 @@ enum : int { kRayMasked = 0, kRayAnswered = 1, kRayTraverse = 2 };
 // intervals -- MotionSystem::Sample and InterpolatedTransform::Sample
 // (src/luxrays/core/geometry/motionsystem.cpp:56-160, 333-337; the GPU
 // kernel's MotionSystem_Sample, motionsystem_funcs.cl:21-115), with every
-// product and sum rounded separately as in the CPU code.  Slerp takes
-// CUDA's acosf / sinf, so a rotating instance's matrix can differ from the
-// CPU's in the last bits; the reference's own CPU and GPU paths differ the
-// same way.
+// product and sum rounded separately as in the CPU code.  Slerp's constant
+// part (phi = acosf(|dot|), sinf(phi)) is evaluated on the host; its two
+// time-dependent sines are CUDA's sinf, so a rotating instance's matrix can
+// differ from the CPU's in the last bits, as the reference's own CPU and GPU
+// paths differ.
 // ---------------------------------------------------------------------------
 
 struct MotionRows {
@@ -275,14 +276,13 @@ __device__ __forceinline__ MotionRows motion_sample(const MotionInterval *its, u
 				// Slerp (quaternion.cpp:143-165) then ToMatrix (:116-141)
 				const float aw = __ldg(&it->q0[0]), ax = __ldg(&it->q0[1]), ay = __ldg(&it->q0[2]), az = __ldg(&it->q0[3]);
 				const float bw = __ldg(&it->q1[0]), bx = __ldg(&it->q1[1]), by = __ldg(&it->q1[2]), bz = __ldg(&it->q1[3]);
-				float cos_phi = __fadd_rn(__fmul_rn(aw, bw),
-						__fadd_rn(__fadd_rn(__fmul_rn(ax, bx), __fmul_rn(ay, by)), __fmul_rn(az, bz)));
-				const float sign = cos_phi > 0.f ? 1.f : -1.f;
-				cos_phi = __fmul_rn(cos_phi, sign);
+				// sign, branch, phi and sinf(phi) come from the host (the same
+				// float operations as the CPU's Slerp); the two time-dependent
+				// sines are CUDA's sinf
+				const float sign = (f & kMiSlerpNegate) ? -1.f : 1.f;
 				float f1, f2;
-				if (__fsub_rn(1.f, cos_phi) > 1e-6f) {
-					const float phi = acosf(cos_phi);
-					const float sin_phi = sinf(phi);
+				if (!(f & kMiSlerpLinear)) {
+					const float phi = __ldg(&it->phi), sin_phi = __ldg(&it->sin_phi);
 					f1 = __fdiv_rn(sinf(__fmul_rn(__fsub_rn(1.f, le), phi)), sin_phi);
 					f2 = __fdiv_rn(sinf(__fmul_rn(le, phi)), sin_phi);
 				} else {
@@ -455,7 +455,12 @@ __device__ __forceinline__ bool ray_step(const TraceArgs &a, TravState &s, TravS
 				const uint32_t tri = __float_as_uint(ta.w);
 				uint32_t mesh = __float_as_uint(tb.w);
 				if (TWO_LEVEL && mesh == kNull) mesh = s.inst_obj;
-				if (ANY || t < s.best_t || mesh < s.best_mesh || (mesh == s.best_mesh && tri < s.best_tri)) {
+				// a hit counts only below the current t, as the reference's
+				// `t < rayHit->t` (a NaN t, or t == maxt with no hit yet, never
+				// does); an exact tie with an earlier hit goes to the lower
+				// (meshIndex, triangleIndex)
+				if (t < s.best_t || (!ANY && t == s.best_t && s.best_mesh != kNull &&
+						(mesh < s.best_mesh || (mesh == s.best_mesh && tri < s.best_tri)))) {
 					s.best_t = t;
 					s.best_b1 = b1;
 					s.best_b2 = b2;

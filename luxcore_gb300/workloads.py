@@ -414,10 +414,11 @@ def config3(n_rays: int = 1 << 23, seed: int = BASE_SEED + 2, **kw):
 
 def motion_scene(n_meshes: int = 16, freq: int = 100, n_inst: int = 4096, seed: int = BASE_SEED + 4,
                  scale=(0.01, 0.05), extent: float = 10.0, kinds=("translate", "rigid", "static"),
-                 speed: float = 0.05) -> SceneDesc:
+                 speed: float = 0.003) -> SceneDesc:
     """instanced_scene with motion blur: instance k becomes a Motion of kind
     kinds[k % len(kinds)] over the shutter [0, 1] --
-      "translate": two keyframes moving by up to `speed` * extent (the
+      "translate": two keyframes moving by up to `speed` * extent per axis
+                   (about an instance's size at the defaults; the
                    world->local matrices differ in translation only);
       "rigid":     three keyframes (times 0, 0.5, 1) turning about a random
                    axis by up to 90 degrees, scaling by up to 1.5x and moving;

@@ -63,6 +63,7 @@ def adversarial_rays(mesh: W.Mesh, seed: int, n_each: int = 64) -> np.ndarray:
     r = base.copy(); r["mint"] = -1e30; r["maxt"] = 1e30; out.append(r)
     r = base.copy(); r["maxt"] = 1e-3; out.append(r)
     r = base.copy(); r["maxt"] = -1.0; out.append(r)
+    r = base.copy(); r["maxt"] = np.inf; out.append(r)
     # masked rays (must not be written)
     r = base.copy(); r["flags"] = W.RAY_FLAGS_MASKED; out.append(r)
     return np.concatenate(out)

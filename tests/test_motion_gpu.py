@@ -3,11 +3,12 @@ MotionSystem restatement.
 
 Translation-only keyframes take the reference's lerp path with every
 operation rounded as on the CPU, so those rays meet the full parity bar
-bit-for-bit.  Rotating keyframes go through Slerp, whose acosf / sinf are
-CUDA's on the GPU and the C library's in the oracle: the sampled matrices
-can differ in the last bits, so those rays are held to a tolerance (hits
-agree on >= 99.9 % of rays; t, b1, b2 within 1e-4 relative; every
-disagreement a near-tie or a hit the oracle confirms within 1e-4)."""
+bit-for-bit.  Rotating keyframes go through Slerp, whose two time-dependent
+sines are CUDA's sinf on the GPU and the C library's in the oracle: the
+sampled matrices can differ in the last bits, so those rays are held to a
+tolerance (hits agree on >= 99.9 % of rays; t within 1e-4 relative (1e-5
+absolute below t = 0.1), b1 and b2 within 1e-4 absolute; every disagreement a near-tie or a hit the oracle
+confirms within 1e-4)."""
 import os
 import sys
 
@@ -32,6 +33,7 @@ MOTION_KERNELS = pytest.mark.parametrize("kernel", [(64, 8, 0), (128, 0, 0x40, 8
                                               "b64-allbits"])
 TOL_AGREE = 0.999
 TOL_REL = 1e-4
+T_FLOOR = 0.1  # t below this is compared absolutely (1e-5 scene units; the scenes span 3 units)
 
 
 @pytest.fixture(scope="module")
@@ -51,17 +53,19 @@ def tolerant_compare(gpu, ref, oracle, rays):
     same = (gpu["meshIndex"] == ref["meshIndex"]) & (gpu["triangleIndex"] == ref["triangleIndex"])
     agree = float(same.mean())
     both = same & hg
-    rel = lambda a, b: np.abs(a.astype(np.float64) - b) <= TOL_REL * np.maximum(np.abs(b.astype(np.float64)), 1e-3)
-    vals = bool(rel(gpu["t"][both], ref["t"][both]).all() and rel(gpu["b1"][both], ref["b1"][both]).all()
-                and rel(gpu["b2"][both], ref["b2"][both]).all())
+    dt = np.abs(gpu["t"][both].astype(np.float64) - ref["t"][both]) / np.maximum(np.abs(ref["t"][both]), T_FLOOR)
+    db = np.maximum(np.abs(gpu["b1"][both].astype(np.float64) - ref["b1"][both]),
+                    np.abs(gpu["b2"][both].astype(np.float64) - ref["b2"][both]))
+    vals = bool((dt <= TOL_REL).all() and (db <= TOL_REL).all())
     bad = 0
     for i in np.nonzero(~same)[0]:
         if hg[i]:
             ok, t, _, _ = oracle.triangle_hit(rays[i], int(gpu["meshIndex"][i]), int(gpu["triangleIndex"][i]))
-            near = abs(float(gpu["t"][i]) - float(ref["t"][i])) <= TOL_REL * max(abs(float(ref["t"][i])), 1e-3)
-            if not (near or (ok and abs(t - float(gpu["t"][i])) <= TOL_REL * max(abs(t), 1e-3))):
+            near = abs(float(gpu["t"][i]) - float(ref["t"][i])) <= TOL_REL * max(abs(float(ref["t"][i])), T_FLOOR)
+            if not (near or (ok and abs(t - float(gpu["t"][i])) <= TOL_REL * max(abs(t), T_FLOOR))):
                 bad += 1
-    return {"agree": agree, "values_ok": vals, "unexplained": bad,
+    return {"agree": agree, "values_ok": vals, "unexplained": bad, "max_rel_dt": float(dt.max(initial=0)),
+            "max_abs_db": float(db.max(initial=0)), "bitexact": float((gpu["t"][both] == ref["t"][both]).mean()),
             "ok": agree >= TOL_AGREE and vals and bad <= max(2, int(1e-4 * gpu.shape[0]))}
 
 
@@ -93,7 +97,7 @@ def test_rigid_motion_within_tolerance(torch_cuda, kernel):
     ref, _ = oracle.intersect(closest)
     gpu = gpu_trace(torch_cuda, s, closest)
     st = tolerant_compare(gpu, ref, oracle, closest)
-    assert st["ok"], st
+    assert st["ok"], repr(st)
     assert (ref["meshIndex"] != W.NULL_INDEX).mean() > 0.1
     ref_a, _ = oracle.intersect(anyr)
     gpu_a = gpu_trace(torch_cuda, s, anyr, lrx.LRX_TRACE_ANY)

@@ -198,6 +198,29 @@ def test_adversarial_rays(torch_cuda, kernel):
     assert a["ok"], a
 
 
+def test_maxt_equal_to_the_hit_distance_is_a_miss(torch_cuda):
+    """A ray whose maxt is exactly its closest hit's t misses that triangle
+    (the reference keeps a hit only when t < the current t, which starts at
+    maxt), in both modes; maxt one ulp above finds it again."""
+    scene, rays = W.config1(n_tris=20000, n_rays=1 << 14, seed=77)
+    oracle = po.OracleScene(scene)
+    ref, _ = oracle.intersect(rays)
+    hit = ref["meshIndex"] != W.NULL_INDEX
+    assert hit.mean() > 0.1
+    at = rays.copy()
+    at["maxt"][hit] = ref["t"][hit]
+    above = rays.copy()
+    above["maxt"][hit] = np.nextafter(ref["t"][hit], np.float32(np.inf))
+    s = lrx.Scene(scene)
+    for r in (at, above):
+        want, _ = oracle.intersect(r)
+        assert_parity(gpu_trace(torch_cuda, s, r), want, oracle, r)
+        a = check_anyhit(gpu_trace(torch_cuda, s, r, lrx.LRX_TRACE_ANY), want, oracle, r)
+        assert a["ok"], a
+    want_at, _ = oracle.intersect(at)
+    assert (want_at["meshIndex"][hit] != ref["meshIndex"][hit]).mean() > 0.99
+
+
 @pytest.mark.parametrize("n_tris", [0, 1, 2, 3, 4, 9, 25])
 @KERNELS
 def test_tiny_and_empty_scenes(torch_cuda, kernel, n_tris):
