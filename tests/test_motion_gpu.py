@@ -7,7 +7,8 @@ bit-for-bit.  Rotating keyframes go through Slerp, whose two time-dependent
 sines are CUDA's sinf on the GPU and the C library's in the oracle: the
 sampled matrices can differ in the last bits, so those rays are held to a
 tolerance (hits agree on >= 99.9 % of rays; t within 1e-4 relative (1e-5
-absolute below t = 0.1), b1 and b2 within 1e-4 absolute; every disagreement a near-tie or a hit the oracle
+absolute below t = 0.1), b1 and b2 within 1e-3 absolute, and t bit-exact
+on >= 95 % of hits; every disagreement a near-tie or a hit the oracle
 confirms within 1e-4)."""
 import os
 import sys
@@ -34,6 +35,8 @@ MOTION_KERNELS = pytest.mark.parametrize("kernel", [(64, 8, 0), (128, 0, 0x40, 8
 TOL_AGREE = 0.999
 TOL_REL = 1e-4
 T_FLOOR = 0.1  # t below this is compared absolutely (1e-5 scene units; the scenes span 3 units)
+TOL_BARY = 1e-3  # barycentrics: a last-bit matrix difference moves a hit point on a 0.1-unit triangle
+MIN_BITEXACT = 0.95  # most hits still agree to the bit: the differences are last-bit effects
 
 
 @pytest.fixture(scope="module")
@@ -56,7 +59,7 @@ def tolerant_compare(gpu, ref, oracle, rays):
     dt = np.abs(gpu["t"][both].astype(np.float64) - ref["t"][both]) / np.maximum(np.abs(ref["t"][both]), T_FLOOR)
     db = np.maximum(np.abs(gpu["b1"][both].astype(np.float64) - ref["b1"][both]),
                     np.abs(gpu["b2"][both].astype(np.float64) - ref["b2"][both]))
-    vals = bool((dt <= TOL_REL).all() and (db <= TOL_REL).all())
+    vals = bool((dt <= TOL_REL).all() and (db <= TOL_BARY).all())
     bad = 0
     for i in np.nonzero(~same)[0]:
         if hg[i]:
@@ -66,7 +69,8 @@ def tolerant_compare(gpu, ref, oracle, rays):
                 bad += 1
     return {"agree": agree, "values_ok": vals, "unexplained": bad, "max_rel_dt": float(dt.max(initial=0)),
             "max_abs_db": float(db.max(initial=0)), "bitexact": float((gpu["t"][both] == ref["t"][both]).mean()),
-            "ok": agree >= TOL_AGREE and vals and bad <= max(2, int(1e-4 * gpu.shape[0]))}
+            "ok": agree >= TOL_AGREE and vals and bad <= max(2, int(1e-4 * gpu.shape[0]))
+            and float((gpu["t"][both] == ref["t"][both]).mean()) >= MIN_BITEXACT}
 
 
 @MOTION_KERNELS
