@@ -9,6 +9,7 @@
 //   luxrays::Ray / RayHit              include/luxrays/core/geometry/ray.h:35-103
 //   luxrays::TriangleMesh              include/luxrays/core/trianglemesh.h:79-201
 //   luxrays::InstanceTriangleMesh      trianglemesh.h:203-305 (mesh + Transform)
+//   luxrays::MotionTriangleMesh        trianglemesh.h:307-410 (mesh + MotionSystem)
 //   luxrays::DataSet::Add/Preprocess   src/luxrays/core/dataset.cpp:66-94
 //   luxrays::Accelerator (ACCEL_GB300) include/luxrays/core/accelerator.h:39-59
 //   luxrays::HardwareIntersectionKernel::EnqueueTraceRayBuffer / Update
@@ -49,6 +50,15 @@ struct InstanceTriangleMesh {
 	float transform[16];
 };
 
+// A mesh moved by a motion system (MotionSystem's keyframes): strictly
+// increasing times and row-major world-to-local matrices, 16 floats each --
+// the matrices MBVHAccel applies to a ray at its time.
+struct MotionTriangleMesh {
+	const TriangleMesh *mesh;
+	std::vector<float> times;
+	std::vector<float> transforms;
+};
+
 enum AcceleratorType { ACCEL_AUTO, ACCEL_BVH, ACCEL_MBVH, ACCEL_EMBREE, ACCEL_OPTIX, ACCEL_GB300 };
 
 class HardwareIntersectionKernel;
@@ -67,9 +77,10 @@ public:
 	bool HasHWSupport() const { return true; }
 	bool DoesSupportUpdate() const { return true; }
 
-	void Init(const std::vector<lrx_mesh_desc> &meshes, const std::vector<lrx_object_desc> &objects) {
-		Check(lrx_scene_create(meshes.data(), (uint32_t)meshes.size(), objects.data(), (uint32_t)objects.size(),
-				      nullptr, nullptr, &scene),
+	void Init(const std::vector<lrx_mesh_desc> &meshes, const std::vector<lrx_object_desc> &objects,
+			const std::vector<lrx_motion_desc> &motions = {}) {
+		Check(lrx_scene_create_motion(meshes.data(), (uint32_t)meshes.size(), objects.data(),
+				      (uint32_t)objects.size(), motions.data(), (uint32_t)motions.size(), nullptr, nullptr, &scene),
 				"GB300Accel::Init");
 	}
 	bool Intersect(const Ray *, RayHit *) const {
@@ -118,6 +129,16 @@ public:
 		objects.push_back(object(meshIndexOf(inst->mesh), inst->transform));
 		return (uint32_t)objects.size() - 1;
 	}
+	// The motion system's vectors must stay alive until GetAccelerator.
+	uint32_t Add(const MotionTriangleMesh *mm) {
+		if (mm->transforms.size() != 16 * mm->times.size())
+			throw std::runtime_error("DataSet::Add: one 4x4 matrix per motion keyframe");
+		static const float identity[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
+		objects.push_back(object(meshIndexOf(mm->mesh), identity));
+		motions.push_back(lrx_motion_desc{(uint32_t)objects.size() - 1, (uint32_t)mm->times.size(),
+				mm->times.data(), mm->transforms.data()});
+		return (uint32_t)objects.size() - 1;
+	}
 	void Preprocess() { preprocessed = true; }
 	bool RequiresInstanceSupport() const {
 		for (const lrx_object_desc &o : objects)
@@ -129,7 +150,7 @@ public:
 		if (!preprocessed) throw std::runtime_error("DataSet::GetAccelerator before Preprocess");
 		if (!accel) {
 			accel.reset(new GB300Accel());
-			accel->Init(meshes, objects);
+			accel->Init(meshes, objects, motions);
 		}
 		return *accel;
 	}
@@ -160,6 +181,7 @@ private:
 	std::vector<const TriangleMesh *> sources;
 	std::vector<lrx_mesh_desc> meshes;
 	std::vector<lrx_object_desc> objects;
+	std::vector<lrx_motion_desc> motions;
 	std::unique_ptr<GB300Accel> accel;
 	bool preprocessed = false;
 };

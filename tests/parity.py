@@ -15,7 +15,8 @@ def _rel_ok(a, b, rel):
     a = a.astype(np.float64)
     b = b.astype(np.float64)
     both_nan = np.isnan(a) & np.isnan(b)
-    return both_nan | (np.abs(a - b) <= rel * np.maximum(np.abs(b), 1e-30)) | (a == b)
+    with np.errstate(invalid="ignore"):  # inf - inf (misses of rays with maxt = inf) compares by equality
+        return both_nan | (np.abs(a - b) <= rel * np.maximum(np.abs(b), 1e-30)) | (a == b)
 
 
 def compare(gpu, ref, oracle=None, rays=None):
@@ -28,7 +29,8 @@ def compare(gpu, ref, oracle=None, rays=None):
     dis = ~same
     tg = gpu["t"].astype(np.float64)
     tr = ref["t"].astype(np.float64)
-    tie = hg & hr & (np.abs(tg - tr) <= TIE_REL * np.maximum(np.abs(tr), 1e-30))
+    with np.errstate(invalid="ignore"):
+        tie = hg & hr & (np.abs(tg - tr) <= TIE_REL * np.maximum(np.abs(tr), 1e-30))
     bad_dis = dis & ~tie
     hit_same = same & hg
     vals_ok = (_rel_ok(gpu["t"][same], ref["t"][same], VAL_REL).all()
