@@ -1,6 +1,7 @@
 #!/bin/sh
-# Compiles the reference's BVH kernel text (OpenCL C, from the LuxCore source
-# tree) for the CPU through oracle/refcl_prelude.h, into oracle/_ref/.
+# Compiles the reference's BVH and MBVH kernel texts (OpenCL C, from the
+# LuxCore source tree) for the CPU through oracle/refcl_prelude.h, into
+# oracle/_ref/.
 # Test infrastructure only: the result pins the oracle (tests/golden/).
 # Usage: oracle/build_ref.sh [path to the LuxCore source tree]
 set -e
@@ -11,7 +12,14 @@ if [ ! -f "$REF/include/luxrays/accelerators/bvh.cl" ]; then
 	exit 1
 fi
 mkdir -p "$HERE/_ref"
-g++ -O2 -ffp-contract=off -fno-fast-math -fno-strict-aliasing -fPIC -shared -std=c++17 -pthread \
-	-w -I "$HERE" -I "$REF/include" "$HERE/refcl_harness.cpp" -o "$HERE/_ref/liblrx_refcl.so.tmp"
-mv "$HERE/_ref/liblrx_refcl.so.tmp" "$HERE/_ref/liblrx_refcl.so"
-echo "$HERE/_ref/liblrx_refcl.so"
+# bvh.cl (BVHKernel) and mbvh.cl (MBVHKernel with transforms and motion systems)
+for h in refcl_harness:liblrx_refcl refcl_mbvh_harness:liblrx_refcl_mbvh; do
+	src="${h%%:*}"; lib="${h##*:}"
+	g++ -O2 -ffp-contract=off -fno-fast-math -fno-strict-aliasing -fPIC -shared -std=c++17 -pthread \
+		-w -I "$HERE" -I "$REF/include" "$HERE/$src.cpp" -o "$HERE/_ref/$lib.so.tmp" &
+done
+wait
+for lib in liblrx_refcl liblrx_refcl_mbvh; do
+	mv "$HERE/_ref/$lib.so.tmp" "$HERE/_ref/$lib.so"
+	echo "$HERE/_ref/$lib.so"
+done

@@ -948,6 +948,99 @@ void orc_bvh_nodes(void *scene, orc_bvh_node *out) {
 	}
 }
 
+int orc_mbvh_export(void *scene, uint64_t counts[4], orc_bvh_node *nodes, float *verts, float *mats,
+		uint32_t *motion_ranges, orc_interval *intervals) {
+	const Scene *s = (const Scene *)scene;
+	if (s->accel != ORC_ACCEL_MBVH) return 0;
+	const MBVHAccel &mb = s->mbvh;
+	// mbvhaccelhw.cpp:64-128 / :308-440 (one page): root nodes, then every
+	// unique leaf's nodes; leaf-tree vertex indices rebased onto the
+	// concatenated vertex array, skip indices and root leaf references onto
+	// the concatenated node array
+	std::vector<uint32_t> leafNodeOffset, leafVertOffset;
+	uint64_t nn = mb.root.size(), nv = 0;
+	for (const BVHAccel &l : mb.uniqueLeafs) {
+		leafNodeOffset.push_back((uint32_t)nn);
+		leafVertOffset.push_back((uint32_t)nv);
+		nn += l.tree.size();
+		for (const Mesh *m : l.meshes) nv += m->nVerts;
+	}
+	uint64_t nits = 0;
+	for (uint32_t oi : mb.uniqueLeafsMotionSystem)
+		nits += (*mb.motions)[(*mb.objects)[oi].motion].interpolatedTransforms.size();
+	const uint64_t want[4] = {nn, nv, mb.uniqueLeafsTransform.size(), mb.uniqueLeafsMotionSystem.size()};
+	if (!nodes) {
+		std::memcpy(counts, want, sizeof(want));
+		counts[3] |= nits << 32;
+		return 1;
+	}
+	uint64_t k = 0;
+	for (ArrayNode n : mb.root) {
+		if (is_leaf(n.nodeData)) n.bvhLeaf.leafIndex = leafNodeOffset[n.bvhLeaf.leafIndex];
+		std::memcpy(&nodes[k++], &n, 32);
+	}
+	for (size_t li = 0; li < mb.uniqueLeafs.size(); ++li) {
+		const BVHAccel &l = mb.uniqueLeafs[li];
+		for (ArrayNode n : l.tree) {
+			if (is_leaf(n.nodeData)) {
+				uint32_t vb = leafVertOffset[li];
+				for (uint32_t mi = 0; mi < n.triangleLeaf.meshIndex; ++mi) vb += l.meshes[mi]->nVerts;
+				for (int j = 0; j < 3; ++j) n.triangleLeaf.v[j] += vb;
+			} else {
+				n.nodeData = skip_index(n.nodeData) + leafNodeOffset[li];
+			}
+			std::memcpy(&nodes[k++], &n, 32);
+		}
+		for (const Mesh *m : l.meshes) {
+			std::memcpy(verts, m->verts, 12ull * m->nVerts);
+			verts += 3ull * m->nVerts;
+		}
+	}
+	// mbvhaccelhw.cpp:142-151: each transform leaf gets Transform::mInv
+	for (uint32_t oi : mb.uniqueLeafsTransform) {
+		std::memcpy(mats, (*mb.objects)[oi].mInv, 64);
+		mats += 16;
+	}
+	// mbvhaccelhw.cpp:154-191: every InterpolatedTransform of each motion system
+	uint32_t first = 0;
+	for (uint32_t oi : mb.uniqueLeafsMotionSystem) {
+		const orc_motion::MotionSystem &ms = (*mb.motions)[(*mb.objects)[oi].motion];
+		*motion_ranges++ = first;
+		*motion_ranges++ = first + (uint32_t)ms.interpolatedTransforms.size() - 1;
+		first += (uint32_t)ms.interpolatedTransforms.size();
+		for (const orc_motion::InterpolatedTransform &it : ms.interpolatedTransforms) {
+			orc_interval &o = *intervals++;
+			std::memset(&o, 0, sizeof(o));
+			o.startTime = it.startTime;
+			o.endTime = it.endTime;
+			std::memcpy(o.start, it.start, 64);
+			std::memcpy(o.end, it.end, 64);
+			const orc_motion::Decomposed *d[2] = {&it.startT, &it.endT};
+			for (int e = 0; e < 2; ++e) {
+				std::memcpy(o.R[e], d[e]->R, 64);
+				const float st[6] = {d[e]->Sx, d[e]->Sy, d[e]->Sz, d[e]->Tx, d[e]->Ty, d[e]->Tz};
+				std::memcpy(o.ST[e], st, sizeof(st));
+			}
+			const orc_motion::Quaternion *q[2] = {&it.startQ, &it.endQ};
+			for (int e = 0; e < 2; ++e) {
+				const float wq[4] = {q[e]->w, q[e]->v.x, q[e]->v.y, q[e]->v.z};
+				std::memcpy(o.Q[e], wq, 16);
+			}
+			o.has[0] = it.hasRotation;
+			o.has[1] = it.hasTranslation;
+			o.has[2] = it.hasScale;
+			o.has[3] = it.hasTranslationX;
+			o.has[4] = it.hasTranslationY;
+			o.has[5] = it.hasTranslationZ;
+			o.has[6] = it.hasScaleX;
+			o.has[7] = it.hasScaleY;
+			o.has[8] = it.hasScaleZ;
+			o.has[9] = it.isActive;
+		}
+	}
+	return 1;
+}
+
 void orc_visit_stats(void *scene, const orc_ray *rays, uint64_t n,
 		double *nodes_per_ray, double *leaves_per_ray) {
 	const Scene *s = (const Scene *)scene;

@@ -107,6 +107,29 @@ int orc_triangle_hit(void *scene, const orc_ray *ray, uint32_t meshIndex,
 uint64_t orc_bvh_node_count(void *scene);
 void orc_bvh_nodes(void *scene, orc_bvh_node *out);
 
+/* One InterpolatedTransform of a motion system, as the oracle decomposed it
+ * (motionsystem.cpp:36-72): times, start/end matrices, per end the rotation
+ * matrix R, scales and translations (Sx Sy Sz Tx Ty Tz) and the quaternion
+ * (w x y z), then the flags hasRotation, hasTranslation, hasScale,
+ * hasTranslationX/Y/Z, hasScaleX/Y/Z, isActive. */
+typedef struct {
+	float startTime, endTime;
+	float start[16], end[16];
+	float R[2][16];
+	float ST[2][6];
+	float Q[2][4];
+	int32_t has[10];
+} orc_interval;
+
+/* An MBVH scene in the layout MBVHKernel uploads (mbvhaccelhw.cpp:64-191,
+ * :308-440, one page): nodes (root tree then every unique leaf's tree,
+ * rebased), the concatenated vertices, one world->local matrix per
+ * transform leaf, [first, last] interval indices per motion leaf, and the
+ * intervals.  With nodes == NULL fills counts = {nodes, vertices,
+ * matrices, motion systems | intervals << 32}.  Returns 0 for a BVH scene. */
+int orc_mbvh_export(void *scene, uint64_t counts[4], orc_bvh_node *nodes, float *verts, float *mats,
+		uint32_t *motion_ranges, orc_interval *intervals);
+
 /* Mean number of BVHArrayNode visits per ray of BVHAccel::Intersect, and of
  * leaf (triangle) visits, over the given rays (the reference-layout byte
  * accounting). */

@@ -17,6 +17,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liblrx_oracle.so")
 REF_LIB_PATH = os.path.join(HERE, "_ref", "liblrx_refcl.so")
+REF_MBVH_LIB_PATH = os.path.join(HERE, "_ref", "liblrx_refcl_mbvh.so")
 
 ACCEL_BVH, ACCEL_MBVH = 0, 1
 
@@ -27,6 +28,12 @@ _lock = threading.Lock()
 class OrcObject(ctypes.Structure):
     _fields_ = [("mesh", ctypes.c_uint32), ("has_transform", ctypes.c_uint32),
                 ("m", ctypes.c_float * 16)]
+
+
+class OrcInterval(ctypes.Structure):
+    _fields_ = [("startTime", ctypes.c_float), ("endTime", ctypes.c_float), ("start", ctypes.c_float * 16),
+                ("end", ctypes.c_float * 16), ("R", ctypes.c_float * 32), ("ST", ctypes.c_float * 12),
+                ("Q", ctypes.c_float * 8), ("has", ctypes.c_int32 * 10)]
 
 
 class OrcMotionDesc(ctypes.Structure):
@@ -72,6 +79,8 @@ def lib():
             L.orc_bvh_node_count.argtypes = [vp]
             L.orc_bvh_nodes.argtypes = [vp, vp]
             L.orc_visit_stats.argtypes = [vp, vp, u64, vp, vp]
+            L.orc_mbvh_export.restype = ctypes.c_int
+            L.orc_mbvh_export.argtypes = [vp, vp, vp, vp, vp, vp, vp]
             L.orc_matrix_inverse.restype = ctypes.c_int
             L.orc_matrix_inverse.argtypes = [vp, vp]
             L.orc_machine_epsilon.restype = ctypes.c_float
@@ -160,6 +169,23 @@ class OracleScene:
         out = np.zeros((n, 8), np.uint32)
         if n:
             lib().orc_bvh_nodes(self.handle, _ptr(out))
+        return out
+
+    def mbvh_export(self):
+        """The MBVH in MBVHKernel's upload layout: dict of nodes (n, 8) uint32,
+        verts (n, 3) float32, mats (n, 16) float32, motion ranges (n, 2)
+        uint32 and an OrcInterval array."""
+        L = lib()
+        counts = (ctypes.c_uint64 * 4)()
+        if not L.orc_mbvh_export(self.handle, counts, None, None, None, None, None):
+            raise ValueError("not an MBVH scene")
+        nn, nv, nm, packed = (int(c) for c in counts)
+        nms, nits = packed & 0xFFFFFFFF, packed >> 32
+        out = {"nodes": np.zeros((nn, 8), np.uint32), "verts": np.zeros((max(nv, 1), 3), np.float32),
+               "mats": np.zeros((max(nm, 1), 16), np.float32), "motion_ranges": np.zeros((max(nms, 1), 2), np.uint32),
+               "intervals": (OrcInterval * max(nits, 1))(), "n_mats": nm, "n_motions": nms, "n_intervals": nits}
+        L.orc_mbvh_export(self.handle, counts, _ptr(out["nodes"]), _ptr(out["verts"]), _ptr(out["mats"]),
+                          _ptr(out["motion_ranges"]), out["intervals"])
         return out
 
     def visit_stats(self, rays: np.ndarray):

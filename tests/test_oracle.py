@@ -14,13 +14,15 @@ from luxcore_gb300 import workloads as W  # noqa: E402
 from oracle import pyoracle as po  # noqa: E402
 from make_golden import SENTINEL, load  # noqa: E402
 
-GOLDEN = ["golden_random", "golden_heightfield", "golden_multimesh"]
+# bvh.cl fixtures (flat scenes) and mbvh.cl fixtures (instances; translating
+# motion systems): bit-exact pins
+GOLDEN = ["golden_random", "golden_heightfield", "golden_multimesh", "golden_instanced", "golden_motion_translate"]
 
 
 @pytest.mark.parametrize("name", GOLDEN)
 def test_oracle_matches_reference_kernel(name):
     scene, rays, ref = load(name)
-    o = po.OracleScene(scene, po.ACCEL_BVH)
+    o = po.OracleScene(scene)  # BVHAccel for flat scenes, MBVHAccel with instances
     hits, _ = o.intersect(rays, n_threads=2)
     written = ref["meshIndex"] != SENTINEL          # masked rays are not written by the reference
     masked = (rays["flags"] & W.RAY_FLAGS_MASKED) != 0
@@ -49,6 +51,49 @@ def test_oracle_matches_reference_kernel(name):
         assert ok and t == h["t"][i]
     bb = same & hit
     assert np.array_equal(h["b1"][bb], r["b1"][bb]) and np.array_equal(h["b2"][bb], r["b2"][bb])
+
+
+def test_oracle_motion_matches_reference_kernel_within_tolerance():
+    """Turning and scaling motion systems: the reference's own CPU code
+    (motionsystem.cpp, quaternion.cpp; restated by the oracle) and its
+    OpenCL kernel (motionsystem_funcs.cl, quaternion_funcs.cl; the fixture)
+    sum Slerp's dot product in different orders, so their sampled matrices
+    differ in the last bits: same triangles, t within 1e-4 relative (1e-5
+    absolute below t = 0.1), barycentrics within 1e-3."""
+    scene, rays, ref = load("golden_motion_rigid")
+    o = po.OracleScene(scene)
+    hits, _ = o.intersect(rays, n_threads=2)
+    same = (hits["meshIndex"] == ref["meshIndex"]) & (hits["triangleIndex"] == ref["triangleIndex"])
+    assert same.mean() >= 0.999
+    hit = same & (ref["meshIndex"] != W.NULL_INDEX)
+    assert hit.mean() > 0.3
+    dt = np.abs(hits["t"][hit].astype(np.float64) - ref["t"][hit]) / np.maximum(np.abs(ref["t"][hit]), 0.1)
+    assert dt.max() <= 1e-4
+    assert np.abs(hits["b1"][hit].astype(np.float64) - ref["b1"][hit]).max() <= 1e-3
+    assert np.abs(hits["b2"][hit].astype(np.float64) - ref["b2"][hit]).max() <= 1e-3
+    # translating instances of the same scene (every third object) agree to the bit
+    trans = hit & (ref["meshIndex"] % 3 == 1)
+    assert trans.any() and np.array_equal(hits["t"][trans], ref["t"][trans])
+
+
+@pytest.mark.skipif(not os.path.exists(po.REF_MBVH_LIB_PATH), reason="reference MBVH kernel not built here")
+def test_oracle_mbvh_matches_reference_kernel_live():
+    """Larger instanced and translating-motion scenes, traced by the
+    reference's mbvh.cl compiled for the CPU: bit-exact agreement."""
+    from make_golden import ref_mbvh_trace
+    for scene, rays in (W.config3(n_rays=20000, seed=31, n_meshes=4, freq=12, n_inst=400, extent=4.0,
+                                  scale=(0.1, 0.4))[:2],
+                        W.config_motion(n_rays=20000, seed=32, n_meshes=4, freq=12, n_inst=400, extent=4.0,
+                                        scale=(0.1, 0.4), kinds=("translate", "static"), speed=0.02,
+                                        time_range=(-0.2, 1.2))[:2]):
+        ref = ref_mbvh_trace(scene, rays)
+        hits, _ = po.OracleScene(scene).intersect(rays)
+        hit = ref["meshIndex"] != W.NULL_INDEX
+        assert hit.mean() > 0.3
+        assert np.array_equal(hits["meshIndex"], ref["meshIndex"])
+        assert np.array_equal(hits["triangleIndex"], ref["triangleIndex"])
+        assert np.array_equal(hits["t"], ref["t"])
+        assert np.array_equal(hits["b1"][hit], ref["b1"][hit]) and np.array_equal(hits["b2"][hit], ref["b2"][hit])
 
 
 def test_oracle_bvh_equals_brute_force():

@@ -76,9 +76,12 @@ def assert_parity(gpu, ref, oracle, rays, min_hit_rate=0.0):
 # ---------------------------------------------------------------------------
 
 
-@pytest.mark.parametrize("name", ["golden_random", "golden_heightfield", "golden_multimesh"])
+@pytest.mark.parametrize("name", ["golden_random", "golden_heightfield", "golden_multimesh", "golden_instanced",
+                                  "golden_motion_translate"])
 @KERNELS
 def test_golden_fixtures(torch_cuda, kernel, name):
+    """Hits of the reference's own kernel text (bvh.cl, or mbvh.cl for the
+    instanced and motion fixtures) compiled for the CPU."""
     from make_golden import load
     scene, rays, ref = load(name)
     s = make_scene(scene, kernel)
@@ -90,7 +93,7 @@ def test_golden_fixtures(torch_cuda, kernel, name):
     # NaN rays: misses, as BVHAccel::Intersect returns them
     assert (gpu["meshIndex"][nan_ray] == W.NULL_INDEX).all()
     keep = ~masked & ~nan_ray
-    oracle = po.OracleScene(scene, po.ACCEL_BVH)
+    oracle = po.OracleScene(scene)
     g, r, rr = gpu[keep], ref[keep], rays[keep]
     st = compare(g, r, oracle, rr)
     assert st["bad_disagreements"] == 0 and st["values_ok"] and st["ties_valid"], st
