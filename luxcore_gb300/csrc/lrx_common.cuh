@@ -109,7 +109,10 @@ __device__ __forceinline__ float3 rn_cross(float3 a, float3 b) {
 
 // Triangle::Intersect (include/luxrays/core/geometry/triangle.h:55-89) with
 // e1 = p1 - p0 and e2 = p2 - p0 precomputed (same FP32 subtraction).  The
-// reciprocal is the correctly rounded IEEE 1.f / divisor.
+// reciprocal is the correctly rounded IEEE 1.f / divisor.  The t test is
+// written so a NaN t fails it; STRICT also fails t == maxt (the caller's
+// `t < rayHit->t`, bvhaccel.cpp:233, folded in for any-hit).
+template <bool STRICT>
 __device__ __forceinline__ bool tri_intersect(float3 o, float3 d, float mint, float maxt,
 		float3 p0, float3 e1, float3 e2, float &t, float &b1, float &b2) {
 	const float3 s1 = rn_cross(d, e2);
@@ -125,8 +128,7 @@ __device__ __forceinline__ bool tri_intersect(float3 o, float3 d, float mint, fl
 	const float b0 = __fsub_rn(__fsub_rn(1.f, b1), b2);
 	if (b0 < 0.f) return false;
 	t = __fmul_rn(rn_dot(e2, s2), invDivisor);
-	if (t < mint || t > maxt) return false;
-	return true;
+	return STRICT ? (t >= mint && t < maxt) : (t >= mint && t <= maxt);
 }
 
 // InvTransform * Point (transform.h:144-156): three rows plus the w divide,

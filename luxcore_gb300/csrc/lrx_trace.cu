@@ -450,16 +450,17 @@ __device__ __forceinline__ bool ray_step(const TraceArgs &a, TravState &s, TravS
 					tc = ld_scene_f4(tp + 2, keep, pol);
 			if (COUNT) ++c.tris;
 			float t, b1, b2;
-			if (tri_intersect(s.ray.o, s.ray.d, s.mint, s.best_t, make_float3(ta.x, ta.y, ta.z),
+			if (tri_intersect<ANY>(s.ray.o, s.ray.d, s.mint, s.best_t, make_float3(ta.x, ta.y, ta.z),
 					make_float3(tb.x, tb.y, tb.z), make_float3(tc.x, tc.y, tc.z), t, b1, b2)) {
 				const uint32_t tri = __float_as_uint(ta.w);
 				uint32_t mesh = __float_as_uint(tb.w);
 				if (TWO_LEVEL && mesh == kNull) mesh = s.inst_obj;
 				// a hit counts only below the current t, as the reference's
 				// `t < rayHit->t` (a NaN t, or t == maxt with no hit yet, never
-				// does); an exact tie with an earlier hit goes to the lower
-				// (meshIndex, triangleIndex)
-				if (t < s.best_t || (!ANY && t == s.best_t && s.best_mesh != kNull &&
+				// does; tri_intersect has let only t <= best_t through, and for
+				// any-hit only t < best_t); an exact tie with an earlier hit goes
+				// to the lower (meshIndex, triangleIndex)
+				if (ANY || t < s.best_t || (s.best_mesh != kNull &&
 						(mesh < s.best_mesh || (mesh == s.best_mesh && tri < s.best_tri)))) {
 					s.best_t = t;
 					s.best_b1 = b1;
