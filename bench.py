@@ -355,7 +355,8 @@ def run_lrx(args):
         nn, nt, ni = counts[name]
         alg_bytes[name] = n * (RAY_BYTES + HIT_BYTES + nn * NODE_BYTES + nt * TRI_BYTES + ni * INST_BYTES)
 
-    def step(evs=None):
+    def seq_step(evs=None):
+        # one lrx_trace per set, back to back on one stream
         for k, (name, dr, dh, n, mode) in enumerate(dev):
             if evs is not None:
                 evs[k][0].record(stream)
@@ -363,8 +364,17 @@ def run_lrx(args):
             if evs is not None:
                 evs[k][1].record(stream)
 
+    batch_arr = lrx.batch_array([(scene, dr.data_ptr(), dh.data_ptr(), n, mode) for _nm, dr, dh, n, mode in dev])
+
+    def batched_step(evs=None):
+        # the three sets as one lrx_trace_batches call: each (>= 131,072 rays)
+        # is a launch of its own on a side stream, all three side by side
+        lrx.trace_batches([None] * len(dev), st, arr=batch_arr)
+
+    step = batched_step if args.step_form == "batched" else seq_step
     for _ in range(args.warmup):
         step()
+        seq_step()
     stream.synchronize()
     if scene.device_status(st) != 0:
         raise RuntimeError("device status word set during warm-up")
@@ -390,6 +400,18 @@ def run_lrx(args):
     d.barrier()
     elapsed_ms = start.elapsed_time(end)
     elapsed_ms = d.max(elapsed_ms)
+    if args.step_form == "batched":
+        # per-launch times: the same sets as sequential launches, each between
+        # events on its stream (outside the timed region)
+        seq_t0, seq_t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        seq_t0.record(stream)
+        for k in range(args.steps):
+            seq_step(ev[k])
+        seq_t1.record(stream)
+        torch.cuda.synchronize()
+        seq_step_ms = seq_t0.elapsed_time(seq_t1) / args.steps
+    else:
+        seq_step_ms = elapsed_ms / args.steps
     kern_ms = {name: statistics.mean(ev[k][j][0].elapsed_time(ev[k][j][1]) for k in range(args.steps))
                for j, (name, *_rest) in enumerate(dev)}
     value = rays_per_step * args.steps * ws / (elapsed_ms / 1e3) / 1e6
@@ -480,11 +502,13 @@ def run_lrx(args):
             e1.synchronize()
             alt["queue-1batch"][name] = round(n * 5 / (e0.elapsed_time(e1) / 1e3) / 1e6, 1)
 
-    # roofline of the traversal kernel: algorithmic bytes / kernel time
+    # roofline of the traversal kernels: algorithmic bytes / time -- over the
+    # timed step (the batched step's three launches run side by side), and
+    # per launch from the sequential per-set times
     peak, peak_kind = load_peaks()
     tot_alg = sum(alg_bytes.values())
-    tot_ms = sum(kern_ms.values())
-    achieved = tot_alg / (tot_ms / 1e3) / 1e9
+    achieved = tot_alg / (elapsed_ms / args.steps / 1e3) / 1e9
+    per_launch_frac = {name: round(alg_bytes[name] / (kern_ms[name] / 1e3) / 1e9 / peak, 4) for name, *_r in dev}
     tpr = load_traffic_per_ray()
     traffic = None
     if all(name in tpr for name, *_r in dev):  # DRAM bytes per trace launch, averaged over the sets
@@ -535,6 +559,9 @@ def run_lrx(args):
                 "parallelism": f"replicas x{ws}", "build_ms": round(info["build_ms"], 1),
                 "scene_build_wall_s": round(build_s, 3), "wide_nodes": info["node_count"],
                 "bvh_depth": info["max_depth"],
+                "step_form": ("one lrx_trace_batches call (3 launches on side streams)" if args.step_form == "batched"
+                              else "3 sequential lrx_trace launches"),
+                "sequential_step_Mrays": round(rays_per_step / (seq_step_ms / 1e3) / 1e6, 1),
                 "per_set_ms": {k: round(v, 4) for k, v in kern_ms.items()},
                 "per_set_Mrays": {name: round(n / (kern_ms[name] / 1e3) / 1e6, 1) for name, _, _, n, _ in dev},
                 "nodes_tris_per_ray": {k: [round(v[0], 2), round(v[1], 2)] for k, v in counts.items()},
@@ -546,7 +573,8 @@ def run_lrx(args):
             },
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": traffic,
-                         "peak_kind": peak_kind,
+                         "peak_kind": peak_kind, "scope": "the timed step (algorithmic bytes / step time)",
+                         "per_launch_frac": per_launch_frac,
                          "bytes_per_ray": round(tot_alg / rays_per_step, 1)},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
@@ -1012,6 +1040,8 @@ def main():
                                                                       "motion"],
                     help="heightfield = the headline line; batching = uneven batches, plain vs queue kernel")
     ap.add_argument("--batches", type=int, default=512)
+    ap.add_argument("--step-form", default="batched", choices=["batched", "sequential"],
+                    help="heightfield step: one lrx_trace_batches call over the 3 sets, or 3 lrx_trace calls")
     ap.add_argument("--inst-rays", type=int, default=1 << 23, help="instanced workload: rays per set")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--ref-fraction", type=int, default=4,

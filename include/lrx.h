@@ -245,9 +245,14 @@ typedef struct lrx_batch {
  * warp's lanes may then hold rays of different batches); otherwise 64-thread
  * blocks claim 64-ray tiles.  Batches whose scene config has
  * LRX_VARIANT_SORT_RAYS and at least 32,768 rays are reordered first (one
- * radix sort per launch).  Batches on scenes with motion-blurred instances
- * are traced by a launch of their own each, in batch order.  Results equal
- * lrx_trace on each batch.  Asynchronous on `stream`; graph-capturable (no host synchronisation; the
+ * radix sort per launch).  When a call holds at most 4 batches of 131,072
+ * rays or more (a wavefront's camera, bounce and shadow buffers), those --
+ * and any batch on a scene with motion-blurred instances -- are traced by
+ * launches of their own (the scene's lrx_trace path) on side streams forked
+ * from `stream` and joined back into it, so they run beside each other and
+ * beside the queue launch (the side streams are the calling thread's own,
+ * created by its first such call, which belongs outside a graph capture).  Results
+ * equal lrx_trace on each batch.  Asynchronous on `stream`; graph-capturable (no host synchronisation; the
  * sort scratch is stream-ordered pool memory).
  * Replaces: a sequence of HardwareIntersectionKernel::EnqueueTraceRayBuffer
  * calls (hardwareintersectiondevice.h:67-68), one per RayBuffer. */

@@ -1188,6 +1188,42 @@ lrx_status lrx_trace_batches(const lrx_batch *batches, uint32_t n_batches, void 
 	return lrx_trace_batches_ex(batches, n_batches, stream, nullptr, nullptr);
 }
 
+// Streams and events of the calling thread on one device for the batches
+// lrx_trace_batches launches on their own (created on first use, never
+// shared with another thread, so a graph capture on one thread cannot catch
+// another thread's work).
+struct SideStreams {
+	int dev = -1;
+	cudaStream_t s[kSideStreams] = {};
+	cudaEvent_t fork = nullptr, join[kSideStreams] = {};
+};
+
+static lrx_status side_streams(int dev, SideStreams **out) {
+	thread_local std::vector<std::unique_ptr<SideStreams>> per_dev;
+	for (auto &p : per_dev)
+		if (p->dev == dev) {
+			*out = p.get();
+			return LRX_OK;
+		}
+	std::unique_ptr<SideStreams> ss(new SideStreams());
+	ss->dev = dev;
+	for (uint32_t k = 0; k < kSideStreams; ++k) {
+		LRX_CUDA(cudaStreamCreateWithFlags(&ss->s[k], cudaStreamNonBlocking));
+		LRX_CUDA(cudaEventCreateWithFlags(&ss->join[k], cudaEventDisableTiming));
+	}
+	LRX_CUDA(cudaEventCreateWithFlags(&ss->fork, cudaEventDisableTiming));
+	*out = ss.get();
+	per_dev.push_back(std::move(ss));
+	return LRX_OK;
+}
+
+// A batch traced by a launch of its own rather than in the queue launch:
+// one on a scene with motion instances, or -- when the call holds at most
+// kSideStreams batches of kDirectBatchRays rays or more -- one of those.
+static bool direct_batch(const lrx_batch &b, bool big_direct) {
+	return b.count != 0 && ((big_direct && b.count >= kDirectBatchRays) || !b.scene->motions.empty());
+}
+
 lrx_status lrx_trace_batches_ex(const lrx_batch *batches, uint32_t n_batches, void *stream,
 		uint32_t *d_tile_counters, uint32_t *d_done_flags) {
 	if (n_batches && !batches) {
@@ -1224,16 +1260,20 @@ lrx_status lrx_trace_batches_ex(const lrx_batch *batches, uint32_t n_batches, vo
 	// Warp-level ray fetch when any batch's scene asks for persistent warps in
 	// its mode (refill from the first such config) and every batch fits one
 	// fetch launch; otherwise 64-ray tiles per block.
+	uint32_t n_big = 0;
+	for (uint32_t k = 0; k < n_batches; ++k) n_big += batches[k].count >= kDirectBatchRays ? 1u : 0u;
+	const bool big_direct = n_big <= kSideStreams;
 	uint32_t fetch = 0, refill = 16;
 	for (uint32_t k = 0; k < n_batches; ++k) {
+		if (direct_batch(batches[k], big_direct)) continue;
+		if (batches[k].count > kMaxFetchRays) {
+			fetch = 0;
+			break;
+		}
 		const lrx_trace_config &cfg = batches[k].scene->tcfg[batches[k].mode == LRX_TRACE_ANY ? 1 : 0];
 		if (!fetch && (cfg.variant & kVarPersistent)) {
 			fetch = 1;
 			if (cfg.refill) refill = std::min(32u, cfg.refill);
-		}
-		if (batches[k].count > kMaxFetchRays) {
-			fetch = 0;
-			break;
 		}
 	}
 	p.fetch = fetch;
@@ -1311,32 +1351,60 @@ lrx_status lrx_trace_batches_ex(const lrx_batch *batches, uint32_t n_batches, vo
 		pend_tiles = pend_rays = pend_sorted = 0;
 		return rc;
 	};
-	for (uint32_t k = 0; k < n_batches; ++k) {
-		const lrx_batch &b = batches[k];
-		if (b.count == 0) continue;
-		lrx_scene *s = b.scene;
-		if (!s->motions.empty()) {
-			// scenes with motion instances trace in a launch of their own (the
-			// queue kernels carry no motion code); its flag follows that launch
-			lrx_status rc = trace_common(s, b.d_rays, b.d_hits, b.count, b.mode, nullptr, st);
-			if (rc == LRX_OK && d_done_flags) rc = launch_set_flag(d_done_flags + k, st);
+	// A few large batches (at most kSideStreams of at least kDirectBatchRays
+	// rays -- a wavefront's camera, bounce and shadow buffers), and batches on
+	// scenes with motion instances (the queue kernels carry no motion code),
+	// are traced by launches of their own -- the scene's plain path -- on side
+	// streams forked from `stream` and joined back into it, so their launches
+	// run beside each other and beside the queue launch of the other batches:
+	// one launch's drain (its last, longest rays) overlaps the others' work.
+	// Many large batches stay in the queue launch, which drains once for all
+	// of them.  A direct batch's completion flag follows its launch on its
+	// side stream.
+	SideStreams *side = nullptr;
+	auto trace_all = [&]() -> lrx_status {
+		uint32_t n_direct = 0;
+		for (uint32_t k = 0; k < n_batches; ++k) {
+			const lrx_batch &b = batches[k];
+			if (!direct_batch(b, big_direct)) continue;
+			if (!side) {
+				lrx_status rc = side_streams(dev, &side);
+				if (rc != LRX_OK) return rc;
+				LRX_CUDA(cudaEventRecord(side->fork, st));
+				for (uint32_t j = 0; j < kSideStreams; ++j) LRX_CUDA(cudaStreamWaitEvent(side->s[j], side->fork, 0));
+			}
+			cudaStream_t ss = side->s[n_direct++ % kSideStreams];
+			lrx_status rc = trace_common(b.scene, b.d_rays, b.d_hits, b.count, b.mode, nullptr, ss);
+			if (rc == LRX_OK && d_done_flags) rc = launch_set_flag(d_done_flags + k, ss);
 			if (rc != LRX_OK) return rc;
-			continue;
 		}
-		const uint32_t tiles = (b.count + kTileRays - 1) / kTileRays;
-		const lrx_trace_config &cfg = s->tcfg[b.mode == LRX_TRACE_ANY ? 1 : 0];
-		const bool sort = (cfg.variant & kVarSortRays) && b.count >= kSortMinRays && s->root != kNull;
-		if (pending.size() == kMaxQueueBatches || pend_tiles + tiles > 0xffffffffull ||
-				(fetch && pend_rays + b.count > kMaxFetchRays) || (sort && pend_sorted + b.count > kMaxFetchRays)) {
-			lrx_status rc = flush();
-			if (rc != LRX_OK) return rc;
+		for (uint32_t k = 0; k < n_batches; ++k) {
+			const lrx_batch &b = batches[k];
+			if (b.count == 0 || direct_batch(b, big_direct)) continue;
+			lrx_scene *s = b.scene;
+			const uint32_t tiles = (b.count + kTileRays - 1) / kTileRays;
+			const lrx_trace_config &cfg = s->tcfg[b.mode == LRX_TRACE_ANY ? 1 : 0];
+			const bool sort = (cfg.variant & kVarSortRays) && b.count >= kSortMinRays && s->root != kNull;
+			if (pending.size() == kMaxQueueBatches || pend_tiles + tiles > 0xffffffffull ||
+					(fetch && pend_rays + b.count > kMaxFetchRays) || (sort && pend_sorted + b.count > kMaxFetchRays)) {
+				lrx_status rc = flush();
+				if (rc != LRX_OK) return rc;
+			}
+			pending.push_back({k, (b.mode == LRX_TRACE_ANY ? 2u : 0u) | (s->two_level ? 1u : 0u), sort});
+			pend_tiles += tiles;
+			pend_rays += b.count;
+			pend_sorted += sort ? b.count : 0u;
 		}
-		pending.push_back({k, (b.mode == LRX_TRACE_ANY ? 2u : 0u) | (s->two_level ? 1u : 0u), sort});
-		pend_tiles += tiles;
-		pend_rays += b.count;
-		pend_sorted += sort ? b.count : 0u;
+		return flush();
+	};
+	const lrx_status rc = trace_all();
+	if (side) {  // join every side stream back, also after an error (a capture must not stay forked)
+		for (uint32_t j = 0; j < kSideStreams; ++j) {
+			cudaEventRecord(side->join[j], side->s[j]);
+			cudaStreamWaitEvent(st, side->join[j], 0);
+		}
 	}
-	return flush();
+	return rc;
 }
 
 lrx_status lrx_trace_counted(lrx_scene *s, const void *d_rays, void *d_hits, uint32_t count, uint32_t mode,

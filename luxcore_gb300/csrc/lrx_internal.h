@@ -152,6 +152,8 @@ constexpr uint32_t kTileRays = 64;
 constexpr uint32_t kMaxQueueBatches = 384;  // keeps the parameter block under 32 KB
 constexpr uint32_t kQueueSlots = 4096;      // concurrent queue launches per device
 constexpr uint32_t kMaxFetchRays = 0x7fffffffu;  // rays per fetch-kernel launch (claims stay below 2^32)
+constexpr uint32_t kDirectBatchRays = 131072;  // lrx_trace_batches: batches this large get launches of their own
+constexpr uint32_t kSideStreams = 4;           // ... on this many side streams per thread and device
 struct QueueParams {
 	uint32_t n, total_tiles, slot;
 	uint32_t fetch;         // 1: warp-level ray fetch (k_trace_queue_fetch), 0: 64-ray tiles per block

@@ -350,7 +350,8 @@ def test_trace_config_struct_versions(torch_cuda):
         assert L.lrx_scene_set_trace_config(s.handle, ctypes.byref(bad)) == lrx.LRX_ERR_INVALID_ARGUMENT
 
 
-@pytest.mark.parametrize("queue", ["fetch", "fetch-refill1", "tiles", "fetch-sorted", "tiles-sorted"])
+@pytest.mark.parametrize("queue", ["fetch", "fetch-refill1", "tiles", "fetch-sorted", "tiles-sorted",
+                                   "fetch-many-large"])
 def test_trace_batches_equals_per_batch_traces(torch_cuda, queue):
     """lrx_trace_batches over a ragged mix of scenes, modes and sizes
     (including empty, single-ray and tile-boundary batches, and more batches
@@ -371,7 +372,11 @@ def test_trace_batches_equals_per_batch_traces(torch_cuda, queue):
         elif queue == "tiles-sorted":
             s.set_trace_config(64, 8, lrx.LRX_VARIANT_SORT_RAYS)
     rng = np.random.default_rng(302)
-    sizes = [0, 1, 63, 64, 65, 1000, 100_000, 40_000, 32_768] + rng.integers(1, 3000, 400).tolist()
+    # 131,072 rays and more: launches of their own on side streams
+    sizes = [0, 1, 63, 64, 65, 1000, 100_000, 40_000, 32_768, 131_071, 131_072, 300_000] + \
+        rng.integers(1, 3000, 400).tolist()
+    if queue == "fetch-many-large":  # more than 4 large batches: all of them stay in the queue launch
+        sizes += [140_000, 150_000, 160_000]
     st = torch.cuda.current_stream().cuda_stream
     items, refs = [], []
     for k, n in enumerate(sizes):
@@ -395,6 +400,50 @@ def test_trace_batches_equals_per_batch_traces(torch_cuda, queue):
         got = h.cpu().numpy().view(W.HIT_DTYPE)[:n]
         bad = np.nonzero(got.view(np.uint32).reshape(-1, 5) != ref.view(np.uint32).reshape(-1, 5))[0]
         assert bad.size == 0, (n, m, bad[:5], got[bad[:3]], ref[bad[:3]])
+
+
+def test_trace_batches_in_a_cuda_graph(torch_cuda):
+    """lrx_trace_batches captured in a CUDA graph -- large batches on forked
+    side streams, small ones in the queue launch -- replays to the plain
+    per-batch results, and again after new rays are written in place."""
+    torch = torch_cuda
+    flat_desc, _ = W.config1(n_tris=20000, n_rays=1, seed=311)
+    inst_desc, _, _ = W.config3(n_rays=1, n_meshes=2, freq=8, n_inst=50, extent=1.0, scale=(0.05, 0.2))
+    scenes = [lrx.Scene(flat_desc), lrx.Scene(inst_desc)]
+    sizes = [200_000, 5_000, 140_000, 777, 1, 65_536]
+    stream = torch.cuda.Stream()
+    st = stream.cuda_stream
+    items = []
+    for k, n in enumerate(sizes):
+        mode = lrx.LRX_TRACE_ANY if k % 2 else lrx.LRX_TRACE_CLOSEST
+        d_r = torch.empty(n * 48, dtype=torch.uint8, device="cuda")
+        d_h = torch.empty(n * 20, dtype=torch.uint8, device="cuda")
+        items.append((scenes[k % 2], d_r, d_h, n, mode))
+    arr = lrx.batch_array([(s, r.data_ptr(), h.data_ptr(), n, m) for s, r, h, n, m in items])
+
+    def fill(seed):
+        refs = []
+        for k, (s, d_r, d_h, n, mode) in enumerate(items):
+            rays = W.random_rays(n, seed + k)
+            d_r.copy_(torch.from_numpy(rays.view(np.uint8).reshape(-1).copy()))
+            refs.append(gpu_trace(torch, s, rays, mode))
+        torch.cuda.synchronize()
+        return refs
+
+    fill(900)
+    with torch.cuda.stream(stream):
+        lrx.trace_batches([None] * len(items), st, arr=arr)  # first call on this thread: side streams created
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=stream):
+        lrx.trace_batches([None] * len(items), st, arr=arr)
+    for seed in (910, 920):
+        refs = fill(seed)
+        g.replay()
+        torch.cuda.synchronize()
+        for (s, d_r, d_h, n, mode), ref in zip(items, refs):
+            got = d_h.cpu().numpy().view(W.HIT_DTYPE)
+            assert np.array_equal(got.view(np.uint32), ref.view(np.uint32)), (n, mode)
 
 
 def test_autotune_picks_a_valid_config_and_keeps_results(torch_cuda):
