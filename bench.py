@@ -727,6 +727,76 @@ def run_instanced(args, motion: bool = False):
     return 0
 
 
+def run_pathocl(args):
+    """PATHOCL-style wavefront loop on the heightfield (luxcore_gb300/pathocl.py):
+    1,048,576 tasks (one per pixel of a 1024 x 1024 image), one ray buffer of
+    path and shadow rays traced in place per iteration, masked tasks
+    included, advanced on the device between traces; depth limit 4.  A step
+    is 8 iterations.  Reported: unmasked rays traced per second over the
+    whole loop (trace + AdvancePaths stand-in) and over the trace launches
+    alone, for the default closest-hit config and with ray compaction."""
+    import torch
+
+    from luxcore_gb300 import lrx
+    from luxcore_gb300 import pathocl
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    st = stream.cuda_stream
+    desc = make_scene()
+    with torch.cuda.stream(stream):
+        scene = lrx.Scene(desc, stream=st)
+    iters = 8
+    forms = {}
+    for form, variant in (("persistent", lrx.LRX_VARIANT_PERSISTENT),
+                          ("persistent+compact", lrx.LRX_VARIANT_PERSISTENT | lrx.LRX_VARIANT_COMPACT)):
+        scene.set_trace_config(64, 8, variant, modes=1, refill=8)
+        with torch.cuda.stream(stream):
+            wf = pathocl.WavefrontPaths(scene, desc, 1024, 1024, max_depth=4, stream=stream)
+            wf.iterate(args.warmup * iters)
+            torch.cuda.synchronize()
+            t0 = int(wf.traced_dev)
+            ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                  for _ in range(args.steps * iters)]
+            start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            clocks = ClockSampler(0)
+            clocks.start()
+            start.record(stream)
+            for k in range(args.steps * iters):
+                ev[k][0].record(stream)
+                wf.trace()
+                ev[k][1].record(stream)
+                wf.advance()
+            end.record(stream)
+            torch.cuda.synchronize()
+            clk = clocks.stop()
+        if scene.device_status(st) != 0:
+            raise RuntimeError("device status word set during the wavefront loop")
+        rays = int(wf.traced_dev) - t0
+        loop_ms = start.elapsed_time(end)
+        trace_ms = sum(a.elapsed_time(b) for a, b in ev)
+        forms[form] = {"loop_Mrays": round(rays / (loop_ms / 1e3) / 1e6, 1),
+                       "trace_Mrays": round(rays / (trace_ms / 1e3) / 1e6, 1),
+                       "unmasked_rays_per_iteration": round(rays / (args.steps * iters)),
+                       "ms_per_iteration": round(loop_ms / (args.steps * iters), 4),
+                       "trace_ms_per_iteration": round(trace_ms / (args.steps * iters), 4), "clocks": clk}
+        del wf
+    best = forms["persistent"]
+    line = {
+        "metric": "Mrays/s traced in a PATHOCL-style wavefront loop (trace + AdvancePaths stand-in on the device)",
+        "value": best["loop_Mrays"], "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(best["ms_per_iteration"] * iters, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": "heightfield-2093058tri, 1048576 tasks (1024x1024), depth 4, one in-place buffer of "
+                               "path + shadow rays per iteration, 8 iterations per step",
+                   "forms": forms},
+        "clocks": best["clocks"],
+    }
+    print(json.dumps(line), flush=True)
+    scene.close()
+    return 0
+
+
 def dh_hits(entry):
     """meshIndex column of a device hit buffer (host copy)."""
     import torch
@@ -1037,7 +1107,7 @@ def main():
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[2000.0, 800.0])
     ap.add_argument("--serve-streams", type=int, default=4)
     ap.add_argument("--workload", default="heightfield", choices=["heightfield", "batching", "serving", "instanced",
-                                                                      "motion"],
+                                                                      "motion", "pathocl"],
                     help="heightfield = the headline line; batching = uneven batches, plain vs queue kernel")
     ap.add_argument("--batches", type=int, default=512)
     ap.add_argument("--step-form", default="batched", choices=["batched", "sequential"],
@@ -1068,6 +1138,8 @@ def main():
         return run_instanced(args)
     if args.workload == "motion" and args.impl == "lrx":
         return run_instanced(args, motion=True)
+    if args.workload == "pathocl" and args.impl == "lrx":
+        return run_pathocl(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_lrx(args)
