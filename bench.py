@@ -522,20 +522,36 @@ def run_lrx(args):
         hh = torch.empty(r.shape[0] * HIT_BYTES, dtype=torch.uint8).pin_memory()
         pinned.append((hr, hh, r.shape[0], mode))
 
-    def e2e_step():
+    def e2e_seq_step():
         for hr, hh, n, mode in pinned:
             scene.trace_host_ptr(hr.data_ptr(), hh.data_ptr(), n, mode, st)
 
+    host_arr = lrx.host_batch_array([(scene, hr.data_ptr(), hh.data_ptr(), n, mode) for hr, hh, n, mode in pinned])
+
+    def e2e_batched_step():
+        # one lrx_trace_host_batches call: each set's copies overlap the others' traces
+        lrx.trace_host_batches([None] * len(pinned), st, arr=host_arr)
+
+    e2e_step = e2e_batched_step if args.step_form == "batched" else e2e_seq_step
+    e2e_seq_value = None
     if not args.no_e2e:
         for _ in range(max(1, args.warmup)):
             e2e_step()
+            e2e_seq_step()
         d.barrier()
         t1 = time.perf_counter()
         for _ in range(args.steps):
             e2e_step()
         e2e_s = d.max(time.perf_counter() - t1)
         e2e_value = round(rays_per_step * args.steps * ws / e2e_s / 1e6, 3)
-    h2d = rays_per_step * (RAY_BYTES + HIT_BYTES)
+        t1 = time.perf_counter()
+        for _ in range(max(1, args.steps // 10)):
+            e2e_seq_step()
+        e2e_seq_value = round(rays_per_step * max(1, args.steps // 10) / (time.perf_counter() - t1) / 1e6, 3)
+    # lrx_trace_host copies rays and hits in (masked rays keep the caller's
+    # hits); lrx_trace_host_batches copies only the rays of pinned buffers
+    # (the hit buffer's masked slots -- none here -- are read back directly)
+    h2d = rays_per_step * (RAY_BYTES + (0 if args.step_form == "batched" else HIT_BYTES))
     d2h = rays_per_step * HIT_BYTES
 
     line = None
@@ -578,7 +594,10 @@ def run_lrx(args):
                          "bytes_per_ray": round(tot_alg / rays_per_step, 1)},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "api": "lrx_trace_host (pinned host buffers)"},
+                    "d2h_bytes_per_step": d2h,
+                    "api": ("lrx_trace_host_batches over the 3 sets (pinned host buffers)" if args.step_form == "batched"
+                            else "lrx_trace_host per set (pinned host buffers)"),
+                    "sequential_lrx_trace_host_value": e2e_seq_value},
             "gpu_launches": (launches_per_step if launches_per_step is not None else len(dev)) * args.steps,
             "gpu_launches_per_step": launches_per_step,
             "clocks": clk,

@@ -181,6 +181,30 @@ lrx_status lrx_trace(lrx_scene *scene, const void *d_rays, void *d_hits,
 lrx_status lrx_trace_host(lrx_scene *scene, const lrx_ray *h_rays, lrx_hit *h_hits,
 		uint32_t count, uint32_t mode, void *stream);
 
+/* One batch of lrx_trace_host_batches: host rays and hits, as lrx_trace_host. */
+typedef struct lrx_host_batch {
+	lrx_scene *scene;
+	const lrx_ray *h_rays;
+	lrx_hit *h_hits;
+	uint32_t count;
+	uint32_t mode;     /* LRX_TRACE_CLOSEST or LRX_TRACE_ANY */
+} lrx_host_batch;
+
+/* lrx_trace_host over several batches whose copies and traces overlap: the
+ * batches are cut into chunks of at most 1,048,576 rays, and each chunk is
+ * copied in, traced (its scene's lrx_trace path) and copied out on a side
+ * stream (up to 4, round robin, forked from `stream`), so one chunk's copies
+ * run while another is traced.  Returns once every hit is in host memory
+ * (`stream` synchronised).  Page-locked host buffers let the copies run
+ * asynchronously.  Masked rays keep the caller's hit contents: a mapped
+ * (page-locked) hit buffer is not copied in -- only its masked slots are
+ * read back after the trace -- while other hit buffers are copied in first.
+ * Staging comes from a stream-ordered pool (allocated on first use, kept).
+ * Replaces: a sequence of IntersectionDevice::TraceRay-style host batches
+ * (include/luxrays/core/intersectiondevice.h:65-68) -- no reference counterpart
+ * overlaps them. */
+lrx_status lrx_trace_host_batches(const lrx_host_batch *batches, uint32_t batch_count, void *stream);
+
 /* Traversal launch configuration of a scene (what the autotuner chooses). */
 typedef struct lrx_trace_config {
 	uint32_t struct_size;     /* sizeof(lrx_trace_config) */

@@ -1442,6 +1442,104 @@ lrx_status lrx_trace_host(lrx_scene *s, const lrx_ray *h_rays, lrx_hit *h_hits, 
 	return LRX_OK;
 }
 
+// Device view of host memory the device can reach directly -- pinned and
+// mapped (cudaHostAlloc, cudaHostRegister) under unified addressing -- for
+// the `bytes` bytes at h: both ends must resolve, to device addresses
+// `bytes - 1` apart.  Pageable memory (cudaMemoryTypeUnregistered) and device
+// memory give false.
+static bool mapped_host_range(const void *h, size_t bytes, void **d) {
+	cudaPointerAttributes a0, a1;
+	if (cudaPointerGetAttributes(&a0, h) != cudaSuccess) {
+		cudaGetLastError();
+		return false;
+	}
+	const void *last = static_cast<const char *>(h) + (bytes - 1);
+	if (cudaPointerGetAttributes(&a1, last) != cudaSuccess) {
+		cudaGetLastError();
+		return false;
+	}
+	if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer || !a1.devicePointer)
+		return false;
+	if (static_cast<const char *>(a1.devicePointer) - static_cast<const char *>(a0.devicePointer) !=
+			(std::ptrdiff_t)(bytes - 1))
+		return false;
+	*d = a0.devicePointer;
+	return true;
+}
+
+lrx_status lrx_trace_host_batches(const lrx_host_batch *batches, uint32_t n_batches, void *stream) {
+	if (n_batches && !batches) {
+		set_error("lrx_trace_host_batches: null batch array");
+		return LRX_ERR_INVALID_ARGUMENT;
+	}
+	int dev = -1;
+	for (uint32_t k = 0; k < n_batches; ++k) {
+		const lrx_host_batch &b = batches[k];
+		if (!b.scene || b.mode > LRX_TRACE_ANY || (b.count && (!b.h_rays || !b.h_hits))) {
+			set_error("lrx_trace_host_batches: batch " + std::to_string(k) + ": null scene or buffer, or unknown mode");
+			return LRX_ERR_INVALID_ARGUMENT;
+		}
+		if (dev < 0) dev = b.scene->device;
+		if (b.scene->device != dev) {
+			set_error("lrx_trace_host_batches: all scenes of one call must live on one device");
+			return LRX_ERR_INVALID_ARGUMENT;
+		}
+	}
+	if (dev < 0) return LRX_OK;
+	DeviceGuard g(dev);
+	cudaStream_t st = (cudaStream_t)stream;
+	SideStreams *side = nullptr;
+	lrx_status rc = side_streams(dev, &side);
+	if (rc != LRX_OK) return rc;
+	cudaMemPool_t pool;
+	if ((rc = stream_pool(dev, &pool)) != LRX_OK) return rc;
+	LRX_CUDA(cudaEventRecord(side->fork, st));
+	for (uint32_t j = 0; j < kSideStreams; ++j) LRX_CUDA(cudaStreamWaitEvent(side->s[j], side->fork, 0));
+	// Batches are cut into chunks of at most kHostChunkRays rays; each chunk
+	// runs copy in -> trace -> copy out on a side stream (round robin), so one
+	// chunk's copies overlap the other chunks' traces.  Staging comes from the
+	// stream-ordered pool and goes back after the chunk's copy out.  Masked
+	// rays keep the caller's hit contents: when the hit buffer is mapped host
+	// memory, only the masked slots are read back from it after the trace;
+	// otherwise the whole chunk of hits is copied in first.
+	auto run = [&]() -> lrx_status {
+		uint32_t used = 0;
+		for (uint32_t k = 0; k < n_batches; ++k) {
+			const lrx_host_batch &b = batches[k];
+			void *mapped_hits = nullptr;
+			const bool mapped = b.count && mapped_host_range(b.h_hits, sizeof(lrx_hit) * (size_t)b.count, &mapped_hits);
+			for (uint32_t c0 = 0; c0 < b.count; c0 += kHostChunkRays) {
+				const uint32_t n = std::min(kHostChunkRays, b.count - c0);
+				cudaStream_t ss = side->s[used++ % kSideStreams];
+				const size_t rb = sizeof(lrx_ray) * (size_t)n, hb = sizeof(lrx_hit) * (size_t)n;
+				const lrx_ray *hr = b.h_rays + c0;
+				lrx_hit *hh = b.h_hits + c0;
+				void *d_rays = nullptr, *d_hits = nullptr;
+				LRX_CUDA(cudaMallocFromPoolAsync(&d_rays, rb, pool, ss));
+				LRX_CUDA(cudaMallocFromPoolAsync(&d_hits, hb, pool, ss));
+				LRX_CUDA(cudaMemcpyAsync(d_rays, hr, rb, cudaMemcpyHostToDevice, ss));
+				if (!mapped) LRX_CUDA(cudaMemcpyAsync(d_hits, hh, hb, cudaMemcpyHostToDevice, ss));
+				lrx_status r = trace_common(b.scene, d_rays, d_hits, n, b.mode, nullptr, ss);
+				if (r == LRX_OK && mapped)
+					r = launch_restore_masked_hits(d_rays, n, static_cast<const lrx_hit *>(mapped_hits) + c0, d_hits, ss);
+				if (r == LRX_OK) LRX_CUDA(cudaMemcpyAsync(hh, d_hits, hb, cudaMemcpyDeviceToHost, ss));
+				cudaFreeAsync(d_rays, ss);
+				cudaFreeAsync(d_hits, ss);
+				if (r != LRX_OK) return r;
+			}
+		}
+		return LRX_OK;
+	};
+	rc = run();
+	for (uint32_t j = 0; j < kSideStreams; ++j) {
+		cudaEventRecord(side->join[j], side->s[j]);
+		cudaStreamWaitEvent(st, side->join[j], 0);
+	}
+	if (rc != LRX_OK) return rc;
+	LRX_CUDA(cudaStreamSynchronize(st));
+	return LRX_OK;
+}
+
 lrx_status lrx_scene_device_status(lrx_scene *s, uint32_t *status, void *stream) {
 	if (!s || !status) {
 		set_error("lrx_scene_device_status: null argument");

@@ -154,6 +154,7 @@ constexpr uint32_t kQueueSlots = 4096;      // concurrent queue launches per dev
 constexpr uint32_t kMaxFetchRays = 0x7fffffffu;  // rays per fetch-kernel launch (claims stay below 2^32)
 constexpr uint32_t kDirectBatchRays = 131072;  // lrx_trace_batches: batches this large get launches of their own
 constexpr uint32_t kSideStreams = 4;           // ... on this many side streams per thread and device
+constexpr uint32_t kHostChunkRays = 1u << 20;  // lrx_trace_host_batches: rays per copy-in/trace/copy-out chunk
 struct QueueParams {
 	uint32_t n, total_tiles, slot;
 	uint32_t fetch;         // 1: warp-level ray fetch (k_trace_queue_fetch), 0: 64-ray tiles per block
@@ -177,6 +178,11 @@ lrx_status stream_pool(int dev, cudaMemPool_t *out);
 // Sets *flag to 1 in stream order, after a fence that orders every earlier
 // write of the stream's kernels before it (host-mapped flags allowed).
 lrx_status launch_set_flag(uint32_t *flag, cudaStream_t stream);
+
+// d_hits[i] = src[i] for the masked rays of d_rays[0, n); src is a device
+// view of the caller's (mapped host) hit buffer.
+lrx_status launch_restore_masked_hits(const void *d_rays, uint32_t n, const void *src, void *d_hits,
+		cudaStream_t stream);
 
 // One launch of the persistent queue kernel over p.n batches.
 lrx_status launch_trace_queue(const QueueParams &p, cudaStream_t stream);

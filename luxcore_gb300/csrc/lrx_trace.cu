@@ -879,6 +879,26 @@ lrx_status launch_set_flag(uint32_t *flag, cudaStream_t st) {
 	return LRX_OK;
 }
 
+// hits[i] = src[i] for every masked ray i (src: the caller's host buffer,
+// mapped); unmasked slots are left alone.
+__global__ void k_restore_masked_hits(const float4 *__restrict__ rays, uint32_t n, const uint32_t *src,
+		uint32_t *hits) {
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	const uint32_t flags = __float_as_uint(__ldcs(rays + 3 * (size_t)i + 2).y);
+	if (!(flags & LRX_RAY_FLAGS_MASKED)) return;
+#pragma unroll
+	for (int w = 0; w < 5; ++w) hits[5 * (size_t)i + w] = src[5 * (size_t)i + w];
+}
+
+lrx_status launch_restore_masked_hits(const void *d_rays, uint32_t n, const void *src, void *d_hits, cudaStream_t st) {
+	if (n == 0) return LRX_OK;
+	k_restore_masked_hits<<<(n + 255) / 256, 256, 0, st>>>(reinterpret_cast<const float4 *>(d_rays), n,
+			static_cast<const uint32_t *>(src), static_cast<uint32_t *>(d_hits));
+	LRX_CUDA(cudaGetLastError());
+	return LRX_OK;
+}
+
 lrx_status launch_trace_queue(const QueueParams &p, cudaStream_t st) {
 	if (p.total_tiles == 0) return LRX_OK;
 	static int resident = 0;  // 64-thread blocks resident per GB300 at this kernel's occupancy

@@ -48,7 +48,7 @@ EXPORTED = ["lrx_abi_version", "lrx_last_error", "lrx_scene_create", "lrx_scene_
             "lrx_server_add_scene",
             "lrx_server_submit", "lrx_server_wait", "lrx_server_get_stats", "lrx_server_reset_stats",
             "lrx_ply_load", "lrx_ply_free", "lrx_scene_key", "lrx_scene_save", "lrx_scene_load",
-            "lrx_scene_create_motion"]
+            "lrx_scene_create_motion", "lrx_trace_host_batches"]
 LRX_SERVE_BATCHED = 0
 LRX_SERVE_PLAIN = 1
 LRX_NOALLOC_MAX_RAYS = 131072
@@ -84,6 +84,11 @@ class TraceConfig(ctypes.Structure):
 class MotionDesc(ctypes.Structure):
     _fields_ = [("object", ctypes.c_uint32), ("count", ctypes.c_uint32), ("times", ctypes.c_void_p),
                 ("transforms", ctypes.c_void_p)]
+
+
+class HostBatch(ctypes.Structure):
+    _fields_ = [("scene", ctypes.c_void_p), ("h_rays", ctypes.c_void_p), ("h_hits", ctypes.c_void_p),
+                ("count", ctypes.c_uint32), ("mode", ctypes.c_uint32)]
 
 
 class PlyMesh(ctypes.Structure):
@@ -198,6 +203,26 @@ def batch_array(batches):
         arr[k].count = n
         arr[k].mode = m
     return arr
+
+
+def host_batch_array(batches):
+    """ctypes array of lrx_host_batch from (Scene, h_rays, h_hits, count, mode) tuples (host addresses)."""
+    arr = (HostBatch * max(1, len(batches)))()
+    for k, (s, r, h, n, m) in enumerate(batches):
+        arr[k].scene = s.handle.value if isinstance(s.handle, ctypes.c_void_p) else s.handle
+        arr[k].h_rays = r
+        arr[k].h_hits = h
+        arr[k].count = n
+        arr[k].mode = m
+    return arr
+
+
+def trace_host_batches(batches, stream: int = 0, arr=None):
+    """lrx_trace_host_batches: host batches whose copies and traces overlap;
+    returns when every hit is in host memory."""
+    if arr is None:
+        arr = host_batch_array(batches)
+    check(load().lrx_trace_host_batches(arr, len(batches), ctypes.c_void_p(stream)))
 
 
 def trace_batches(batches, stream: int = 0, d_tile_counters: int = 0, d_done_flags: int = 0, arr=None):

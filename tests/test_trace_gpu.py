@@ -268,6 +268,59 @@ def test_host_entry_point_matches_device(torch_cuda):
     assert np.array_equal(h.view(np.uint8), d.view(np.uint8))
 
 
+def test_host_batches_overlap_and_match_device_traces(torch_cuda):
+    """lrx_trace_host_batches over pinned and pageable host buffers, both
+    modes and two scenes, a batch of more than one chunk: the same hits as
+    device traces, masked slots untouched (pinned hit buffers are not copied
+    in; their masked slots are read back), empty batches skipped."""
+    torch = torch_cuda
+    flat, frays = W.config1(n_tris=20000, n_rays=70000, seed=63)
+    inst, irays, _ = W.config3(n_rays=50000, n_meshes=2, freq=8, n_inst=60, extent=2.0, scale=(0.1, 0.3))
+    frays["flags"][::9] = W.RAY_FLAGS_MASKED
+    sf, si = lrx.Scene(flat), lrx.Scene(inst)
+    jobs = [(sf, frays, lrx.LRX_TRACE_CLOSEST, True), (si, irays, lrx.LRX_TRACE_ANY, False),
+            (sf, frays[:0], lrx.LRX_TRACE_CLOSEST, False), (si, irays[:20000], lrx.LRX_TRACE_CLOSEST, True),
+            (sf, frays[:33333], lrx.LRX_TRACE_ANY, False),
+            (sf, np.tile(frays, 17)[:1_100_000], lrx.LRX_TRACE_CLOSEST, True)]  # more than one chunk
+    keep, items, want = [], [], []
+    for sc, r, mode, pinned in jobs:
+        want.append(gpu_trace(torch, sc, r, mode) if r.shape[0] else None)
+        hr = torch.from_numpy(np.ascontiguousarray(r).view(np.uint8).reshape(-1).copy())
+        hh = torch.empty(max(1, r.shape[0]) * 20, dtype=torch.uint8)
+        if pinned:
+            hr, hh = hr.pin_memory(), hh.pin_memory()
+        hh.view(torch.int32).fill_(np.int32(np.uint32(SENT).view(np.int32)).item())
+        keep += [hr, hh]
+        items.append((sc, hr.data_ptr(), hh.data_ptr(), r.shape[0], mode))
+    lrx.trace_host_batches(items)
+    for (sc, _r, h, n, _m), w, (_, _, _, _), hh in zip(items, want, jobs, keep[1::2]):
+        if n == 0:
+            continue
+        got = hh.numpy()[:n * 20].view(W.HIT_DTYPE)
+        assert np.array_equal(got.view(np.uint8), w.view(np.uint8))
+
+
+@pytest.mark.parametrize("mode", [lrx.LRX_TRACE_CLOSEST, lrx.LRX_TRACE_ANY])
+def test_host_entry_point_on_pinned_buffers(torch_cuda, mode):
+    """lrx_trace_host on pinned host buffers: the same hits as device
+    buffers, masked rays' slots untouched, and a buffer offset into a pinned
+    allocation works too."""
+    torch = torch_cuda
+    scene, rays = W.config1(n_tris=20000, n_rays=60000, seed=62)
+    rays["flags"][::5] = W.RAY_FLAGS_MASKED
+    s = lrx.Scene(scene)
+    d = gpu_trace(torch, s, rays, mode)
+    h_rays = torch.from_numpy(rays.view(np.uint8).reshape(-1).copy()).pin_memory()
+    h_hits = torch.empty(rays.shape[0] * 20 + 64, dtype=torch.uint8).pin_memory()
+    h_hits.view(torch.int32).fill_(np.int32(np.uint32(SENT).view(np.int32)).item())
+    off = 32  # hits start 32 bytes into the pinned allocation
+    s.trace_host_ptr(h_rays.data_ptr(), h_hits.data_ptr() + off, rays.shape[0], mode)
+    got = h_hits.numpy()[off:off + rays.shape[0] * 20].view(W.HIT_DTYPE)
+    assert np.array_equal(got.view(np.uint8), d.view(np.uint8))
+    assert (h_hits.numpy()[:off].view(np.uint32) == SENT).all()
+    assert (h_hits.numpy()[off + rays.shape[0] * 20:].view(np.uint32) == SENT).all()
+
+
 @KERNELS
 def test_deterministic_and_batch_independent(torch_cuda, kernel):
     scene, rays = W.config1(n_tris=30000, n_rays=100000, seed=71)
