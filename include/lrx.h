@@ -175,7 +175,9 @@ lrx_status lrx_trace(lrx_scene *scene, const void *d_rays, void *d_hits,
 
 /* Same as lrx_trace for rays and hits in HOST memory: copies the rays in,
  * traces, copies the hits out and synchronises `stream`.  Staging buffers
- * are allocated on first use and kept by the scene.
+ * are allocated on first use and kept by the scene.  Batches of more than
+ * 1,048,576 rays go through lrx_trace_host_batches (chunks whose copies
+ * overlap each other's traces).
  * Replaces: the serial IntersectionDevice::TraceRay loop
  * (include/luxrays/core/intersectiondevice.h:65-68) for batches. */
 lrx_status lrx_trace_host(lrx_scene *scene, const lrx_ray *h_rays, lrx_hit *h_hits,

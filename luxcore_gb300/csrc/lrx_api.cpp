@@ -1427,6 +1427,10 @@ lrx_status lrx_trace_host(lrx_scene *s, const lrx_ray *h_rays, lrx_hit *h_hits, 
 		set_error("lrx_trace_host: null ray or hit buffer");
 		return LRX_ERR_INVALID_ARGUMENT;
 	}
+	if (count > kHostChunkRays) {  // chunks whose copies overlap each other's traces
+		const lrx_host_batch b{s, h_rays, h_hits, count, mode};
+		return lrx_trace_host_batches(&b, 1, stream);
+	}
 	std::lock_guard<std::mutex> lk(s->mu);
 	DeviceGuard g(s->device);
 	lrx_status rc;
