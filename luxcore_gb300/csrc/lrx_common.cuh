@@ -109,9 +109,10 @@ __device__ __forceinline__ float3 rn_cross(float3 a, float3 b) {
 
 // Triangle::Intersect (include/luxrays/core/geometry/triangle.h:55-89) with
 // e1 = p1 - p0 and e2 = p2 - p0 precomputed (same FP32 subtraction).  The
-// reciprocal is the correctly rounded IEEE 1.f / divisor.  The t test is
-// written so a NaN t fails it; STRICT also fails t == maxt (the caller's
-// `t < rayHit->t`, bvhaccel.cpp:233, folded in for any-hit).
+// reciprocal is the correctly rounded IEEE 1.f / divisor.  The maxt test is
+// written so a NaN t fails it (the caller's `t < rayHit->t` would drop it);
+// STRICT also fails t == maxt (that caller test, bvhaccel.cpp:233, folded in
+// for any-hit).
 template <bool STRICT>
 __device__ __forceinline__ bool tri_intersect(float3 o, float3 d, float mint, float maxt,
 		float3 p0, float3 e1, float3 e2, float &t, float &b1, float &b2) {
@@ -128,7 +129,10 @@ __device__ __forceinline__ bool tri_intersect(float3 o, float3 d, float mint, fl
 	const float b0 = __fsub_rn(__fsub_rn(1.f, b1), b2);
 	if (b0 < 0.f) return false;
 	t = __fmul_rn(rn_dot(e2, s2), invDivisor);
-	return STRICT ? (t >= mint && t < maxt) : (t >= mint && t <= maxt);
+	// a NaN mint rejects nothing (as `t < ray.mint` in the reference); a NaN t
+	// fails the maxt side
+	if (t < mint) return false;
+	return STRICT ? t < maxt : t <= maxt;
 }
 
 // InvTransform * Point (transform.h:144-156): three rows plus the w divide,
