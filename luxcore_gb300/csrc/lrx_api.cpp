@@ -1196,6 +1196,16 @@ struct SideStreams {
 	int dev = -1;
 	cudaStream_t s[kSideStreams] = {};
 	cudaEvent_t fork = nullptr, join[kSideStreams] = {};
+	SideStreams() = default;
+	SideStreams(const SideStreams &) = delete;
+	SideStreams &operator=(const SideStreams &) = delete;
+	~SideStreams() {  // at thread exit; errors (a context already torn down) are ignored
+		for (uint32_t k = 0; k < kSideStreams; ++k) {
+			if (s[k]) cudaStreamDestroy(s[k]);
+			if (join[k]) cudaEventDestroy(join[k]);
+		}
+		if (fork) cudaEventDestroy(fork);
+	}
 };
 
 static lrx_status side_streams(int dev, SideStreams **out) {

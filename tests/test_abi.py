@@ -60,6 +60,9 @@ def test_null_arguments_are_rejected_without_a_device(lib):
     h = ctypes.c_void_p()
     assert lib.lrx_scene_create(None, 0, None, 0, None, None, None) == 1
     assert lib.lrx_trace(None, None, None, 10, 0, None) == 1
+    assert lib.lrx_trace_batches(None, 3, None) == 1
+    assert lib.lrx_trace_host_batches(None, 3, None) == 1
+    assert lib.lrx_scene_create_motion(None, 0, None, 0, None, 2, None, None, ctypes.byref(h)) == 1
     assert lib.lrx_scene_destroy(None) == 0
     assert b"null" in lib.lrx_last_error()
     del h
