@@ -853,17 +853,20 @@ __device__ __forceinline__ void drain_class(const QueueParams &p, uint32_t c, ui
 // that find a class drained move on while others finish its last rays.
 // FLAGS: the launch keeps completion flags (a separate build, so launches
 // without them carry none of that state).
-template <uint32_t CV, bool FLAGS>
-__global__ void __launch_bounds__(kTraceBlock, 7) k_trace_queue_fetch(const __grid_constant__ QueueParams p) {
+// TWO: the launch holds two-level batches (classes 1 and 3).  A launch of
+// flat batches only takes the build without those loops, at 64 registers
+// (8 blocks of 128 per SM) instead of 72.
+template <uint32_t CV, bool FLAGS, bool TWO>
+__global__ void __launch_bounds__(kTraceBlock, TWO ? 7 : 8) k_trace_queue_fetch(const __grid_constant__ QueueParams p) {
 	constexpr bool MM3 = (CV & kVarMinMax3) != 0;
 	uint32_t *slot = g_queue[p.slot];
 	const uint32_t lane = threadIdx.x & 31u;
 	TravState s;
 	TravStack stack;
 	drain_class<false, false, MM3, FLAGS>(p, 0, &slot[0], lane, s, stack);
-	drain_class<false, true, MM3, FLAGS>(p, 1, &slot[1], lane, s, stack);
+	if (TWO) drain_class<false, true, MM3, FLAGS>(p, 1, &slot[1], lane, s, stack);
 	drain_class<true, false, MM3, FLAGS>(p, 2, &slot[2], lane, s, stack);
-	drain_class<true, true, MM3, FLAGS>(p, 3, &slot[3], lane, s, stack);
+	if (TWO) drain_class<true, true, MM3, FLAGS>(p, 3, &slot[3], lane, s, stack);
 	__syncthreads();
 	release_slot(slot);
 }
@@ -910,26 +913,34 @@ lrx_status launch_trace_queue(const QueueParams &p, cudaStream_t st) {
 		resident = std::max(1, sms * std::max(1, per_sm));
 	}
 	if (p.fetch) {
-		static int fetch_resident[2] = {0, 0};  // 128-thread blocks resident per device, without / with flags
+		// 128-thread blocks resident per device, by [flags][two-level]
+		static int fetch_resident[2][2] = {{0, 0}, {0, 0}};
 		const int fl = p.done_flags ? 1 : 0;
-		if (fetch_resident[fl] == 0) {
+		const int two = (p.class_batch[1] != p.class_batch[2] || p.class_batch[3] != p.class_batch[4]) ? 1 : 0;
+		if (fetch_resident[fl][two] == 0) {
 			int dev = 0, sms = 0, per_sm = 0;
 			LRX_CUDA(cudaGetDevice(&dev));
 			LRX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-			if (fl)
-				LRX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_queue_fetch<0u, true>, kTraceBlock, 0));
-			else
-				LRX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_queue_fetch<0u, false>, kTraceBlock, 0));
-			fetch_resident[fl] = std::max(1, sms * std::max(1, per_sm));
+			const void *fn = fl ? (two ? (const void *)k_trace_queue_fetch<0u, true, true>
+									 : (const void *)k_trace_queue_fetch<0u, true, false>)
+							: (two ? (const void *)k_trace_queue_fetch<0u, false, true>
+								   : (const void *)k_trace_queue_fetch<0u, false, false>);
+			LRX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kTraceBlock, 0));
+			fetch_resident[fl][two] = std::max(1, sms * std::max(1, per_sm));
 		}
 		if (p.total_rays == 0 || p.refill < 1 || p.refill > 32) {
 			set_error("queue fetch launch: empty or bad refill");
 			return LRX_ERR_INVALID_ARGUMENT;
 		}
 		const uint32_t grid = (uint32_t)std::min<uint64_t>(((uint64_t)p.total_rays + kTraceBlock - 1) / kTraceBlock,
-				(uint64_t)fetch_resident[fl]);
-		if (fl) k_trace_queue_fetch<0u, true><<<grid, kTraceBlock, 0, st>>>(p);
-		else k_trace_queue_fetch<0u, false><<<grid, kTraceBlock, 0, st>>>(p);
+				(uint64_t)fetch_resident[fl][two]);
+		if (fl) {
+			if (two) k_trace_queue_fetch<0u, true, true><<<grid, kTraceBlock, 0, st>>>(p);
+			else k_trace_queue_fetch<0u, true, false><<<grid, kTraceBlock, 0, st>>>(p);
+		} else {
+			if (two) k_trace_queue_fetch<0u, false, true><<<grid, kTraceBlock, 0, st>>>(p);
+			else k_trace_queue_fetch<0u, false, false><<<grid, kTraceBlock, 0, st>>>(p);
+		}
 		LRX_CUDA(cudaGetLastError());
 		return LRX_OK;
 	}
