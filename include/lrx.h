@@ -244,9 +244,10 @@ lrx_status lrx_scene_set_trace_config(lrx_scene *scene, const lrx_trace_config *
 lrx_status lrx_scene_get_trace_config(const lrx_scene *scene, lrx_trace_config *config);
 
 /* Autotuner: traces the sample batch (device rays) under each candidate
- * launch configuration -- block size {32, 64, 128} x postpone {0, 8, 16} x
+ * launch configuration -- block size {32, 64, 128} x postpone {0, 8} x
  * variant {none, streaming ray access, ray sort, persistent (refill 8),
- * persistent + streaming} -- keeps the fastest for
+ * persistent + streaming, persistent + shared-memory stack top, persistent +
+ * L2-resident scene} -- keeps the fastest for
  * `mode` in the scene and returns it in `chosen` (nullable).  Synchronises
  * `stream`; do not trace the same scene from other threads meanwhile.
  * No reference counterpart (the reference fixes its launch shape). */

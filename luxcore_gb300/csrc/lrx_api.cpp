@@ -1141,10 +1141,13 @@ lrx_status lrx_scene_autotune(lrx_scene *s, const void *d_rays, uint32_t count, 
 	const int m = mode == LRX_TRACE_ANY ? 1 : 0;
 	lrx_trace_config best = s->tcfg[m];
 	float best_ms = INFINITY;
+	// launch shape, ray order, stack placement (local memory or a shared-memory
+	// top) and cache policy for the scene's node and triangle arrays
 	static const uint32_t kBlocks[] = {32, 64, 128};
-	static const uint32_t kPostpone[] = {0, 8, 16};
+	static const uint32_t kPostpone[] = {0, 8};
 	static const uint32_t kVariants[] = {0, LRX_VARIANT_STREAM_RAYS, LRX_VARIANT_SORT_RAYS, LRX_VARIANT_PERSISTENT,
-			LRX_VARIANT_PERSISTENT | LRX_VARIANT_STREAM_RAYS};
+			LRX_VARIANT_PERSISTENT | LRX_VARIANT_STREAM_RAYS, LRX_VARIANT_PERSISTENT | LRX_VARIANT_SMEM_STACK,
+			LRX_VARIANT_PERSISTENT | LRX_VARIANT_SCENE_L2_KEEP};
 	for (uint32_t bs : kBlocks) {
 		for (uint32_t pp : kPostpone) {
 			for (uint32_t var : kVariants) {
