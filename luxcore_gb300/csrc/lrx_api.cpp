@@ -1232,7 +1232,7 @@ static lrx_status side_streams(int dev, SideStreams **out) {
 
 // A batch traced by a launch of its own rather than in the queue launch:
 // one on a scene with motion instances, or -- when the call holds at most
-// kSideStreams batches of kDirectBatchRays rays or more -- one of those.
+// kMaxDirectBatches batches of kDirectBatchRays rays or more -- one of those.
 static bool direct_batch(const lrx_batch &b, bool big_direct) {
 	return b.count != 0 && ((big_direct && b.count >= kDirectBatchRays) || !b.scene->motions.empty());
 }
@@ -1275,7 +1275,7 @@ lrx_status lrx_trace_batches_ex(const lrx_batch *batches, uint32_t n_batches, vo
 	// fetch launch; otherwise 64-ray tiles per block.
 	uint32_t n_big = 0;
 	for (uint32_t k = 0; k < n_batches; ++k) n_big += batches[k].count >= kDirectBatchRays ? 1u : 0u;
-	const bool big_direct = n_big <= kSideStreams;
+	const bool big_direct = n_big <= kMaxDirectBatches;
 	uint32_t fetch = 0, refill = 16;
 	for (uint32_t k = 0; k < n_batches; ++k) {
 		if (direct_batch(batches[k], big_direct)) continue;
@@ -1364,7 +1364,7 @@ lrx_status lrx_trace_batches_ex(const lrx_batch *batches, uint32_t n_batches, vo
 		pend_tiles = pend_rays = pend_sorted = 0;
 		return rc;
 	};
-	// A few large batches (at most kSideStreams of at least kDirectBatchRays
+	// A few large batches (at most kMaxDirectBatches of at least kDirectBatchRays
 	// rays -- a wavefront's camera, bounce and shadow buffers), and batches on
 	// scenes with motion instances (the queue kernels carry no motion code),
 	// are traced by launches of their own -- the scene's plain path -- on side
@@ -1513,12 +1513,14 @@ lrx_status lrx_trace_host_batches(const lrx_host_batch *batches, uint32_t n_batc
 	LRX_CUDA(cudaEventRecord(side->fork, st));
 	for (uint32_t j = 0; j < kSideStreams; ++j) LRX_CUDA(cudaStreamWaitEvent(side->s[j], side->fork, 0));
 	// Batches are cut into chunks of at most kHostChunkRays rays; each chunk
-	// runs copy in -> trace -> copy out on a side stream (round robin), so one
-	// chunk's copies overlap the other chunks' traces.  Staging comes from the
-	// stream-ordered pool and goes back after the chunk's copy out.  Masked
-	// rays keep the caller's hit contents: when the hit buffer is mapped host
-	// memory, only the masked slots are read back from it after the trace;
-	// otherwise the whole chunk of hits is copied in first.
+	// runs copy in -> trace -> copy out on a side stream (round robin over
+	// kSideStreams, one per chunk for up to that many chunks), so one chunk's
+	// copies overlap the other chunks' traces and their launches' drains
+	// overlap each other.  Staging comes from the stream-ordered pool and goes
+	// back after the chunk's copy out.  Masked rays keep the caller's hit
+	// contents: when the hit buffer is mapped host memory, only the masked
+	// slots are read back from it after the trace; otherwise the chunk's hits
+	// are copied in first.
 	auto run = [&]() -> lrx_status {
 		uint32_t used = 0;
 		for (uint32_t k = 0; k < n_batches; ++k) {
