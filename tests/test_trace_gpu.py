@@ -455,6 +455,33 @@ def test_trace_batches_equals_per_batch_traces(torch_cuda, queue):
         assert bad.size == 0, (n, m, bad[:5], got[bad[:3]], ref[bad[:3]])
 
 
+def test_trace_batches_completion_flags_with_large_batches(torch_cuda):
+    """lrx_trace_batches_ex: large batches (own launches on side streams) and
+    queued ones all raise their completion flags and equal plain traces."""
+    torch = torch_cuda
+    flat_desc, _ = W.config1(n_tris=20000, n_rays=1, seed=321)
+    s = lrx.Scene(flat_desc)
+    sizes = [250_000, 3_000, 140_000, 0, 60_000]
+    items, want = [], []
+    for k, n in enumerate(sizes):
+        mode = lrx.LRX_TRACE_ANY if k % 2 else lrx.LRX_TRACE_CLOSEST
+        rays = W.random_rays(max(n, 1), 330 + k)[:n]
+        d_r = torch.from_numpy(rays.view(np.uint8).reshape(-1).copy()).cuda() if n else \
+            torch.empty(48, dtype=torch.uint8, device="cuda")
+        d_h = torch.empty(max(n, 1) * 20, dtype=torch.uint8, device="cuda")
+        items.append((s, d_r, d_h, n, mode))
+        want.append(gpu_trace(torch, s, rays, mode) if n else None)
+    tiles = torch.zeros(len(sizes), dtype=torch.int32, device="cuda")
+    flags = torch.zeros(len(sizes), dtype=torch.int32, device="cuda")
+    lrx.trace_batches([(sc, r.data_ptr(), h.data_ptr(), n, m) for sc, r, h, n, m in items],
+                      torch.cuda.current_stream().cuda_stream, tiles.data_ptr(), flags.data_ptr())
+    torch.cuda.synchronize()
+    assert flags.cpu().tolist() == [1 if n else 0 for n in sizes]
+    for (sc, r, h, n, m), w in zip(items, want):
+        if n:
+            assert np.array_equal(h.cpu().numpy()[:n * 20].view(np.uint32), w.view(np.uint32))
+
+
 def test_trace_batches_in_a_cuda_graph(torch_cuda):
     """lrx_trace_batches captured in a CUDA graph -- large batches on forked
     side streams, small ones in the queue launch -- replays to the plain
