@@ -439,10 +439,11 @@ def run_lrx(args):
                                    refill=c["refill"])
     builds = {}
     if args.build_sweep:
-        # the same sets on trees built with 0-3 treelet passes (default launch configs)
-        for passes in (0, 1, 2, 3):
+        # the same sets on trees built with 0-3 treelet passes, leaf size 2, and
+        # 4- and 6-wide nodes (default launch configs)
+        for passes, leaf, width in ((0, 3, 8), (1, 3, 8), (2, 3, 8), (3, 3, 8), (2, 2, 8), (2, 3, 4), (2, 3, 6)):
             with torch.cuda.stream(stream):
-                sc = lrx.Scene(scene_desc, stream=st, treelet_passes=passes)
+                sc = lrx.Scene(scene_desc, stream=st, treelet_passes=passes, leaf_max=leaf, node_width=width)
             inf = sc.info()
             row = {"build_ms": round(inf["build_ms"], 2), "wide_nodes": inf["node_count"], "depth": inf["max_depth"]}
             for name, dr, dh, n, mode in dev:
@@ -461,7 +462,7 @@ def run_lrx(args):
                 row[name] = {"Mrays": round(n * 5 / (e0.elapsed_time(e1) / 1e3) / 1e6, 1),
                              "nodes_per_ray": round(nn / n, 2), "tris_per_ray": round(nt / n, 2)}
             sc.close()
-            builds[f"treelet{passes}"] = row
+            builds[f"treelet{passes}-leaf{leaf}-width{width}"] = row
         log(f"[bench] {time.strftime('%H:%M:%S')} build sweep done")
 
     if args.sweep:

@@ -87,7 +87,8 @@ typedef struct lrx_build_opts {
 	uint32_t struct_size;    /* sizeof(lrx_build_opts) */
 	uint32_t leaf_max;       /* triangles per leaf, 1..3 (default 3) */
 	uint32_t treelet_passes; /* treelet SAH restructuring passes (default 2, 0 = plain LBVH) */
-	uint32_t reserved;
+	uint32_t node_width;     /* children per wide node, 4..8 (0 = 8); narrower nodes give deeper
+	                            trees in the same 80-byte node format */
 } lrx_build_opts;
 
 typedef struct lrx_scene lrx_scene;
@@ -253,6 +254,20 @@ lrx_status lrx_scene_get_trace_config(const lrx_scene *scene, lrx_trace_config *
  * No reference counterpart (the reference fixes its launch shape). */
 lrx_status lrx_scene_autotune(lrx_scene *scene, const void *d_sample_rays, uint32_t count, uint32_t mode,
 		void *stream, lrx_trace_config *chosen);
+
+/* Builds the scene under each candidate build -- node width {8, 4} x
+ * triangles per leaf {3, 2}, with opts' treelet passes (opts nullable: 2) --
+ * autotunes each candidate's launch configuration for `mode` on the sample
+ * rays (lrx_scene_autotune), and keeps the candidate whose tuned
+ * configuration traces the sample fastest; the others are destroyed.
+ * chosen_opts / chosen_config (nullable) receive the kept build options and
+ * launch configuration.  Synchronises `stream`.  Closest-hit results do not
+ * depend on the choice (ties go to the lowest index in every tree).
+ * No reference counterpart (the reference builds one fixed tree). */
+lrx_status lrx_scene_create_autotuned(const lrx_mesh_desc *meshes, uint32_t mesh_count,
+		const lrx_object_desc *objects, uint32_t object_count, const lrx_build_opts *opts,
+		const void *d_sample_rays, uint32_t sample_count, uint32_t mode, void *stream,
+		lrx_scene **out_scene, lrx_build_opts *chosen_opts, lrx_trace_config *chosen_config);
 
 /* One ray batch of a multi-batch call (device buffers, as for lrx_trace). */
 typedef struct lrx_batch {

@@ -225,6 +225,12 @@ int lrx::scene_device(const lrx_scene *scene) { return scene->device; }
 
 namespace {
 
+// Children per wide node of a scene's builds (0 in blobs written before the
+// option existed: the 8-wide default).
+static uint32_t node_width(const lrx_build_opts &o) {
+	return o.node_width ? o.node_width : 8u;
+}
+
 struct DeviceGuard {
 	int prev = -1;
 	explicit DeviceGuard(int dev) {
@@ -294,7 +300,8 @@ lrx_status build_blas(lrx_scene *s, const float *h_verts, uint32_t nv, const uin
 	if ((rc = launch_triangle_boxes(nt, d_v.as<float>(), d_i.as<uint32_t>(), d_lo.as<float4>(), d_hi.as<float4>(), st)) != LRX_OK)
 		return rc;
 	BvhResult r;
-	if ((rc = build_wide_bvh(nt, d_lo.as<float4>(), d_hi.as<float4>(), s->opts.leaf_max, s->opts.treelet_passes, st,
+	if ((rc = build_wide_bvh(nt, d_lo.as<float4>(), d_hi.as<float4>(), s->opts.leaf_max, node_width(s->opts),
+			     s->opts.treelet_passes, st,
 			     s->scratch, &r)) != LRX_OK)
 		return rc;
 	out.node_count = r.node_count;
@@ -414,7 +421,8 @@ lrx_status build_tlas(lrx_scene *s, const lrx_object_desc *objects, uint32_t n_o
 	LRX_CUDA(cudaMemcpyAsync(d_lo.ptr, blo.data(), 16ull * n, cudaMemcpyHostToDevice, st));
 	LRX_CUDA(cudaMemcpyAsync(d_hi.ptr, bhi.data(), 16ull * n, cudaMemcpyHostToDevice, st));
 	BvhResult r;
-	if ((rc = build_wide_bvh(n, d_lo.as<float4>(), d_hi.as<float4>(), 1, s->opts.treelet_passes, st, s->scratch, &r)) != LRX_OK)
+	if ((rc = build_wide_bvh(n, d_lo.as<float4>(), d_hi.as<float4>(), 1, node_width(s->opts), s->opts.treelet_passes, st,
+			     s->scratch, &r)) != LRX_OK)
 		return rc;
 	std::vector<uint32_t> order(n);
 	LRX_CUDA(cudaMemcpyAsync(order.data(), s->scratch.prim_order.ptr, 4ull * n, cudaMemcpyDeviceToHost, st));
@@ -508,9 +516,15 @@ lrx_status lrx_scene_create_motion(const lrx_mesh_desc *meshes, uint32_t mesh_co
 		s->opts.struct_size = sizeof(lrx_build_opts);
 		s->opts.leaf_max = 3;
 		s->opts.treelet_passes = 2;
+		s->opts.node_width = 8;
 		if (opts && opts->struct_size >= sizeof(lrx_build_opts)) {
 			if (opts->leaf_max) s->opts.leaf_max = std::min(3u, opts->leaf_max);
 			s->opts.treelet_passes = opts->treelet_passes;
+			if (opts->node_width) s->opts.node_width = opts->node_width;
+		}
+		if (s->opts.node_width < 4 || s->opts.node_width > 8) {
+			set_error("lrx_scene_create: node_width must be 0 or in [4, 8]");
+			return LRX_ERR_INVALID_ARGUMENT;
 		}
 		cudaStream_t st = (cudaStream_t)stream;
 		const auto t0 = std::chrono::steady_clock::now();
@@ -840,13 +854,15 @@ lrx_status lrx_scene_key(const lrx_mesh_desc *meshes, uint32_t mesh_count, const
 		if (o.flags & LRX_OBJECT_INSTANCE) h.words(o.transform, sizeof(o.transform));
 		if ((o.flags & LRX_OBJECT_INSTANCE) && (o.flags & LRX_OBJECT_HAS_INVERSE)) h.words(o.inverse, sizeof(o.inverse));
 	}
-	uint32_t leaf_max = 3, passes = 2;  // the lrx_scene_create defaults
+	uint32_t leaf_max = 3, passes = 2, width = 8;  // the lrx_scene_create defaults
 	if (opts && opts->struct_size >= sizeof(lrx_build_opts)) {
 		if (opts->leaf_max) leaf_max = std::min(3u, opts->leaf_max);
 		passes = opts->treelet_passes;
+		if (opts->node_width) width = opts->node_width;
 	}
 	h.value(leaf_max);
 	h.value(passes);
+	if (width != 8) h.value(width);  // keys of default-width scenes as before
 	*key = h.h;
 	return LRX_OK;
 }
@@ -1179,6 +1195,94 @@ lrx_status lrx_scene_autotune(lrx_scene *s, const void *d_rays, uint32_t count, 
 				: offsetof(lrx_trace_config, refill);
 		std::memcpy(chosen, &best, n);
 		chosen->struct_size = (uint32_t)n;
+	}
+	return LRX_OK;
+}
+
+lrx_status lrx_scene_create_autotuned(const lrx_mesh_desc *meshes, uint32_t mesh_count,
+		const lrx_object_desc *objects, uint32_t object_count, const lrx_build_opts *opts, const void *d_sample_rays,
+		uint32_t sample_count, uint32_t mode, void *stream, lrx_scene **out_scene, lrx_build_opts *chosen_opts,
+		lrx_trace_config *chosen_config) {
+	if (!out_scene || !d_sample_rays || sample_count == 0 || mode > LRX_TRACE_ANY) {
+		set_error("lrx_scene_create_autotuned: null scene or sample, empty sample or unknown mode");
+		return LRX_ERR_INVALID_ARGUMENT;
+	}
+	*out_scene = nullptr;
+	lrx_build_opts base{};
+	base.struct_size = sizeof(lrx_build_opts);
+	base.treelet_passes = 2;
+	if (opts && opts->struct_size >= sizeof(lrx_build_opts)) base.treelet_passes = opts->treelet_passes;
+	// candidate builds: node width x triangles per leaf
+	static const uint32_t kWidths[] = {8, 4};
+	static const uint32_t kLeaves[] = {3, 2};
+	cudaStream_t st = (cudaStream_t)stream;
+	lrx_scene *best = nullptr;
+	float best_ms = INFINITY;
+	lrx_build_opts best_opts = base;
+	lrx_trace_config best_cfg{};
+	lrx_status rc = LRX_OK;
+	void *hits = nullptr;
+	cudaEvent_t e0 = nullptr, e1 = nullptr;
+	for (uint32_t w : kWidths) {
+		for (uint32_t leaf : kLeaves) {
+			lrx_build_opts o = base;
+			o.node_width = w;
+			o.leaf_max = leaf;
+			lrx_scene *cand = nullptr;
+			if ((rc = lrx_scene_create(meshes, mesh_count, objects, object_count, &o, stream, &cand)) != LRX_OK) break;
+			DeviceGuard g(cand->device);
+			if (!hits) {
+				cudaMemPool_t pool;
+				if ((rc = stream_pool(cand->device, &pool)) == LRX_OK &&
+						cudaMallocFromPoolAsync(&hits, sizeof(lrx_hit) * (size_t)sample_count, pool, st) != cudaSuccess)
+					rc = cuda_fail(cudaGetLastError(), "cudaMallocFromPoolAsync");
+				if (rc == LRX_OK && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
+					rc = cuda_fail(cudaGetLastError(), "cudaEventCreate");
+			}
+			lrx_trace_config cfg{};
+			cfg.struct_size = sizeof(cfg);
+			if (rc == LRX_OK) rc = lrx_scene_autotune(cand, d_sample_rays, sample_count, mode, stream, &cfg);
+			float ms = INFINITY;
+			if (rc == LRX_OK) {  // the candidate at its tuned configuration
+				for (int r = 0; r < 2 && rc == LRX_OK; ++r)
+					rc = trace_common(cand, d_sample_rays, hits, sample_count, mode, nullptr, st);
+				cudaEventRecord(e0, st);
+				for (int r = 0; r < 5 && rc == LRX_OK; ++r)
+					rc = trace_common(cand, d_sample_rays, hits, sample_count, mode, nullptr, st);
+				cudaEventRecord(e1, st);
+				if (rc == LRX_OK && cudaEventSynchronize(e1) == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+			}
+			if (rc != LRX_OK) {
+				lrx_scene_destroy(cand);
+				break;
+			}
+			if (ms < best_ms) {
+				if (best) lrx_scene_destroy(best);
+				best = cand;
+				best_ms = ms;
+				best_opts = o;
+				best_cfg = cfg;
+			} else {
+				lrx_scene_destroy(cand);
+			}
+		}
+		if (rc != LRX_OK) break;
+	}
+	if (hits) cudaFreeAsync(hits, st);
+	if (e0) cudaEventDestroy(e0);
+	if (e1) cudaEventDestroy(e1);
+	if (rc != LRX_OK || !best) {
+		if (best) lrx_scene_destroy(best);
+		return rc != LRX_OK ? rc : LRX_ERR_BUILD;
+	}
+	cudaStreamSynchronize(st);
+	*out_scene = best;
+	if (chosen_opts) *chosen_opts = best_opts;
+	if (chosen_config) {  // as many bytes as the caller's struct holds
+		const size_t n = chosen_config->struct_size >= sizeof(lrx_trace_config) ? sizeof(lrx_trace_config)
+				: offsetof(lrx_trace_config, refill);
+		std::memcpy(chosen_config, &best_cfg, n);
+		chosen_config->struct_size = (uint32_t)n;
 	}
 	return LRX_OK;
 }

@@ -387,8 +387,8 @@ __global__ void __launch_bounds__(128) k_collapse(const uint2 *__restrict__ item
 		uint2 *__restrict__ out_items, uint32_t *n_out, const uint32_t *__restrict__ bchild,
 		const float4 *__restrict__ bn_lo, const float4 *__restrict__ bn_hi, const uint2 *__restrict__ bmeta,
 		const uint32_t *__restrict__ sorted, const float4 *__restrict__ plo, const float4 *__restrict__ phi,
-		uint32_t leaf_max, WideNode *__restrict__ wnodes, uint32_t *__restrict__ prim_order, uint32_t *counters,
-		uint32_t cap) {
+		uint32_t leaf_max, uint32_t width, WideNode *__restrict__ wnodes, uint32_t *__restrict__ prim_order,
+		uint32_t *counters, uint32_t cap) {
 	// cap = primitive count: bounds the node array, the leaf order and each queue
 	const uint32_t n_items = min(*n_items_ptr, cap);
 	for (uint32_t it = blockIdx.x * blockDim.x + threadIdx.x; it < n_items; it += gridDim.x * blockDim.x) {
@@ -407,8 +407,8 @@ __global__ void __launch_bounds__(128) k_collapse(const uint2 *__restrict__ item
 			load_ref_box(cref[1], sorted, plo, phi, bn_lo, bn_hi, cb[1]);
 			cnt = 2;
 		}
-		// Greedy: open the largest-area internal child until 8 slots are used.
-		while (cnt < 8) {
+		// Greedy: open the largest-area internal child until `width` (<= 8) slots are used.
+		while (cnt < (int)width) {
 			int best = -1;
 			float best_a = -1.f;
 			for (int k = 0; k < cnt; ++k) {
@@ -607,7 +607,11 @@ __global__ void k_init_counters(uint32_t *counters) {
 static inline uint32_t blocks_for(uint64_t n, uint32_t bs) { return (uint32_t)((n + bs - 1) / bs); }
 
 lrx_status build_wide_bvh(uint32_t n, const float4 *d_lo, const float4 *d_hi, uint32_t leaf_max,
-		uint32_t treelet_passes, cudaStream_t st, BuildScratch &S, BvhResult *out) {
+		uint32_t node_width, uint32_t treelet_passes, cudaStream_t st, BuildScratch &S, BvhResult *out) {
+	if (node_width < 2 || node_width > 8) {
+		set_error("node width must be in [2, 8]");
+		return LRX_ERR_INVALID_ARGUMENT;
+	}
 	*out = BvhResult();
 	if (n == 0) return LRX_OK;
 	if (leaf_max < 1) leaf_max = 1;
@@ -682,13 +686,13 @@ lrx_status build_wide_bvh(uint32_t n, const float4 *d_lo, const float4 *d_hi, ui
 		++depth;
 		if (depth > (uint32_t)kMaxTreeDepth) {
 			// a restructured tree may be deeper than the stack allows: build the plain LBVH instead
-			if (treelet_passes > 0) return build_wide_bvh(n, d_lo, d_hi, leaf_max, 0, st, S, out);
+			if (treelet_passes > 0) return build_wide_bvh(n, d_lo, d_hi, leaf_max, node_width, 0, st, S, out);
 			set_error("BVH deeper than the traversal stack allows");
 			return LRX_ERR_BUILD;
 		}
 		LRX_CUDA(cudaMemsetAsync(counters + cout, 0, sizeof(uint32_t), st));
 		k_collapse<<<std::min(blocks_for(n_in, 128), 152u * 16u), 128, 0, st>>>(qin, counters + cin, qout,
-				counters + cout, bchild, bn_lo, bn_hi, bmeta, sorted, d_lo, d_hi, leaf_max,
+				counters + cout, bchild, bn_lo, bn_hi, bmeta, sorted, d_lo, d_hi, leaf_max, node_width,
 				S.wide_nodes.as<WideNode>(), S.prim_order.as<uint32_t>(), counters, n);
 		LRX_CUDA(cudaGetLastError());
 		std::swap(qin, qout);

@@ -76,7 +76,7 @@ struct BvhResult {
 // child_base / tri_base are relative to 0, and scratch.prim_order holds the
 // n primitive indices in leaf order.  Synchronises `stream`.
 lrx_status build_wide_bvh(uint32_t n, const float4 *d_lo, const float4 *d_hi,
-		uint32_t leaf_max, uint32_t treelet_passes, cudaStream_t stream,
+		uint32_t leaf_max, uint32_t node_width, uint32_t treelet_passes, cudaStream_t stream,
 		BuildScratch &scratch, BvhResult *out);
 
 // Per-triangle padded boxes (Union(BBox(p0,p1),p2) expanded by

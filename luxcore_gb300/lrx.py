@@ -48,7 +48,7 @@ EXPORTED = ["lrx_abi_version", "lrx_last_error", "lrx_scene_create", "lrx_scene_
             "lrx_server_add_scene",
             "lrx_server_submit", "lrx_server_wait", "lrx_server_get_stats", "lrx_server_reset_stats",
             "lrx_ply_load", "lrx_ply_free", "lrx_scene_key", "lrx_scene_save", "lrx_scene_load",
-            "lrx_scene_create_motion", "lrx_trace_host_batches"]
+            "lrx_scene_create_motion", "lrx_trace_host_batches", "lrx_scene_create_autotuned"]
 LRX_SERVE_BATCHED = 0
 LRX_SERVE_PLAIN = 1
 LRX_NOALLOC_MAX_RAYS = 131072
@@ -72,7 +72,7 @@ class ObjectDesc(ctypes.Structure):
 
 class BuildOpts(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_uint32), ("leaf_max", ctypes.c_uint32),
-                ("treelet_passes", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+                ("treelet_passes", ctypes.c_uint32), ("node_width", ctypes.c_uint32)]
 
 
 class TraceConfig(ctypes.Structure):
@@ -387,12 +387,12 @@ def _mesh_descs(scene: W.SceneDesc, keep: list):
     return meshes
 
 
-def scene_key(scene: W.SceneDesc, leaf_max: int = 3, treelet_passes: int = 2) -> int:
+def scene_key(scene: W.SceneDesc, leaf_max: int = 3, treelet_passes: int = 2, node_width: int = 8) -> int:
     """lrx_scene_key: content key of a scene's inputs and build options."""
     keep = []
     meshes = _mesh_descs(scene, keep)
     objs = _object_array(scene)
-    opts = BuildOpts(ctypes.sizeof(BuildOpts), leaf_max, treelet_passes, 0)
+    opts = BuildOpts(ctypes.sizeof(BuildOpts), leaf_max, treelet_passes, node_width)
     k = ctypes.c_uint64()
     check(load().lrx_scene_key(meshes, len(scene.meshes), objs, len(scene.objects), ctypes.byref(opts),
                                ctypes.byref(k)))
@@ -403,7 +403,7 @@ class Scene:
     """A device-resident scene (lrx_scene): meshes + objects of a SceneDesc."""
 
     def __init__(self, scene: W.SceneDesc | None, stream: int = 0, leaf_max: int = 3, treelet_passes: int = 2,
-                 _handle=None):
+                 node_width: int = 8, _handle=None):
         L = load()
         if _handle is not None:  # from_blob
             self.handle = _handle
@@ -412,7 +412,7 @@ class Scene:
         self._keep = []
         meshes = _mesh_descs(scene, self._keep)
         objs = _object_array(scene)
-        opts = BuildOpts(ctypes.sizeof(BuildOpts), leaf_max, treelet_passes, 0)
+        opts = BuildOpts(ctypes.sizeof(BuildOpts), leaf_max, treelet_passes, node_width)
         h = ctypes.c_void_p()
         if scene.has_motion:
             motions, n_motion = _motion_array(scene, self._keep)
@@ -444,6 +444,31 @@ class Scene:
         buf = ctypes.create_string_buffer(n.value)
         check(L.lrx_scene_save(self.handle, buf, ctypes.byref(n), ctypes.c_void_p(stream)))
         return buf.raw[:n.value]
+
+    @classmethod
+    def autotuned(cls, scene: W.SceneDesc, d_rays: int, count: int, mode: int = LRX_TRACE_CLOSEST, stream: int = 0,
+                  treelet_passes: int = 2):
+        """lrx_scene_create_autotuned: the fastest of the candidate builds (node
+        width x leaf size) on the sample rays, each at its autotuned launch
+        configuration.  Returns (scene, build options, trace config) dicts."""
+        if scene.has_motion:
+            raise ValueError("autotuned builds take static scenes")
+        L = load()
+        keep = []
+        meshes = _mesh_descs(scene, keep)
+        objs = _object_array(scene)
+        opts = BuildOpts(ctypes.sizeof(BuildOpts), 0, treelet_passes, 0)
+        chosen = BuildOpts(ctypes.sizeof(BuildOpts), 0, 0, 0)
+        cfg = TraceConfig()
+        cfg.struct_size = ctypes.sizeof(TraceConfig)
+        h = ctypes.c_void_p()
+        check(L.lrx_scene_create_autotuned(meshes, len(scene.meshes), objs, len(scene.objects), ctypes.byref(opts),
+                                           ctypes.c_void_p(d_rays), count, mode, ctypes.c_void_p(stream),
+                                           ctypes.byref(h), ctypes.byref(chosen), ctypes.byref(cfg)))
+        sc = cls(scene, _handle=h)
+        return (sc, {"leaf_max": chosen.leaf_max, "treelet_passes": chosen.treelet_passes,
+                     "node_width": chosen.node_width},
+                {"block_size": cfg.block_size, "postpone": cfg.postpone, "variant": cfg.variant, "refill": cfg.refill})
 
     @classmethod
     def from_blob(cls, blob: bytes, stream: int = 0, desc: W.SceneDesc | None = None) -> "Scene":

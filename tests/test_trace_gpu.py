@@ -579,6 +579,43 @@ def test_treelet_restructured_builds_keep_parity(torch_cuda, passes):
         assert_parity(gpu_trace(torch, s, r), ref, o, r)
 
 
+@pytest.mark.parametrize("width", [4, 5, 6, 7])
+def test_narrower_nodes_keep_parity(torch_cuda, width):
+    """Trees of 4- to 7-wide nodes (the same node format, deeper trees) give
+    the oracle's hits, and closest hits equal the 8-wide tree's."""
+    scene, rays = W.config1(n_tris=30000, n_rays=1 << 15, seed=91)
+    oracle = po.OracleScene(scene)
+    ref, _ = oracle.intersect(rays)
+    s = lrx.Scene(scene, node_width=width)
+    s8 = lrx.Scene(scene)
+    if width == 4:  # (node counts need not fall monotonically with the width)
+        assert s.info()["node_count"] > s8.info()["node_count"]
+    for mode in (lrx.LRX_TRACE_CLOSEST, lrx.LRX_TRACE_ANY):
+        gpu = gpu_trace(torch_cuda, s, rays, mode)
+        if mode == lrx.LRX_TRACE_CLOSEST:
+            assert_parity(gpu, ref, oracle, rays, min_hit_rate=0.05)
+            assert np.array_equal(gpu.view(np.uint32), gpu_trace(torch_cuda, s8, rays, mode).view(np.uint32))
+        else:
+            a = check_anyhit(gpu, ref, oracle, rays)
+            assert a["ok"], a
+    with pytest.raises(lrx.LrxError):
+        lrx.Scene(scene, node_width=3)
+
+
+def test_autotuned_build_picks_a_candidate_and_keeps_results(torch_cuda):
+    """lrx_scene_create_autotuned keeps one of the candidate builds with its
+    tuned launch configuration; its closest hits equal the default build's."""
+    torch = torch_cuda
+    scene, rays = W.config1(n_tris=30000, n_rays=1 << 16, seed=92)
+    d_r = torch.from_numpy(rays.view(np.uint8).reshape(-1).copy()).cuda()
+    sc, opts, cfg = lrx.Scene.autotuned(scene, d_r.data_ptr(), rays.shape[0], lrx.LRX_TRACE_CLOSEST,
+                                        torch.cuda.current_stream().cuda_stream, treelet_passes=1)
+    assert opts["node_width"] in (4, 8) and opts["leaf_max"] in (2, 3) and opts["treelet_passes"] == 1
+    assert sc.trace_config(lrx.LRX_TRACE_CLOSEST) == cfg
+    want = gpu_trace(torch, lrx.Scene(scene), rays)
+    assert np.array_equal(gpu_trace(torch, sc, rays).view(np.uint32), want.view(np.uint32))
+
+
 @pytest.mark.parametrize("masked_frac", [0.0, 0.5, 0.97, 1.0])
 def test_compaction_skips_masked_rays(torch_cuda, masked_frac):
     """The compacting launch traces only unmasked rays: their hits equal the
