@@ -23,11 +23,12 @@ pytestmark = pytest.mark.gpu
 SENT = 0xDEADBEEF
 # launch configurations every parity test runs under:
 # (block size, postpone, variant bits[, refill])
-KERNELS = pytest.mark.parametrize("kernel", [(128, 0, 0), (64, 8, 0), (256, 24, 0), (64, 8, 0xF), (128, 8, 0x7),
-                                             (64, 8, 0x10), (32, 8, 0x1F), (64, 8, 0x30),
-                                             (64, 8, 0x40), (128, 0, 0x41, 1), (32, 8, 0x46, 32),
-                                             (64, 8, 0x50, 8), (64, 8, 0xC0, 8), (256, 8, 0x80), (64, 8, 0x90),
-                                             (64, 8, 0x140, 8)],
+KERNEL_CONFIGS = [(128, 0, 0), (64, 8, 0), (256, 24, 0), (64, 8, 0xF), (128, 8, 0x7),
+                  (64, 8, 0x10), (32, 8, 0x1F), (64, 8, 0x30),
+                  (64, 8, 0x40), (128, 0, 0x41, 1), (32, 8, 0x46, 32),
+                  (64, 8, 0x50, 8), (64, 8, 0xC0, 8), (256, 8, 0x80), (64, 8, 0x90),
+                  (64, 8, 0x140, 8)]
+KERNELS = pytest.mark.parametrize("kernel", KERNEL_CONFIGS,
                                   ids=["b128", "b64-p8", "b256-p24", "b64-p8-allvariants", "b128-p8-mm3-hints",
                                        "b64-p8-sorted", "b32-p8-sorted-all", "b64-p8-octsort",
                                        "b64-p8-persistent", "b128-persistent-refill1",
