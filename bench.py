@@ -510,6 +510,34 @@ def run_lrx(args):
     tot_alg = sum(alg_bytes.values())
     achieved = tot_alg / (elapsed_ms / args.steps / 1e3) / 1e9
     per_launch_frac = {name: round(alg_bytes[name] / (kern_ms[name] / 1e3) / 1e9 / peak, 4) for name, *_r in dev}
+    # the bounce kernel on a launch large enough to amortise its drain: 8 M
+    # distinct cosine-hemisphere rays from the same primary hit points (the
+    # step's own bounce set is 1 M rays per launch); outside the timed region
+    big_bounce = None
+    if not args.no_big_bounce:
+        nb = 8 << 20
+        b8 = W.bounce_rays(scene_desc, primary, ph, nb, W.BASE_SEED + 200)
+        d_b8 = up(b8)
+        d_h8 = torch.empty(nb * HIT_BYTES, dtype=torch.uint8, device=f"cuda:{local}")
+        cbuf.zero_()
+        torch.cuda.synchronize()
+        scene.trace_counted(d_b8.data_ptr(), d_h8.data_ptr(), nb, lrx.LRX_TRACE_CLOSEST, cbuf.data_ptr(), st)
+        stream.synchronize()
+        bn, bt, _bi, _br = cbuf.cpu().tolist()
+        for _ in range(2):
+            scene.trace(d_b8.data_ptr(), d_h8.data_ptr(), nb, lrx.LRX_TRACE_CLOSEST, st)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(5):
+            scene.trace(d_b8.data_ptr(), d_h8.data_ptr(), nb, lrx.LRX_TRACE_CLOSEST, st)
+        e1.record(stream)
+        e1.synchronize()
+        ms8 = e0.elapsed_time(e1) / 5
+        bpr = RAY_BYTES + HIT_BYTES + bn / nb * NODE_BYTES + bt / nb * TRI_BYTES
+        big_bounce = {"rays": nb, "Mrays": round(nb / (ms8 / 1e3) / 1e6, 1), "ms_per_launch": round(ms8, 4),
+                      "nodes_tris_per_ray": [round(bn / nb, 2), round(bt / nb, 2)],
+                      "frac": round(nb * bpr / (ms8 / 1e3) / 1e9 / peak, 4)}
+        del d_b8, d_h8
     tpr = load_traffic_per_ray()
     traffic = None
     if all(name in tpr for name, *_r in dev):  # DRAM bytes per trace launch, averaged over the sets
@@ -592,6 +620,7 @@ def run_lrx(args):
                          "frac": round(achieved / peak, 4), "traffic": traffic,
                          "peak_kind": peak_kind, "scope": "the timed step (algorithmic bytes / step time)",
                          "per_launch_frac": per_launch_frac,
+                         "bounce_8M_launch": big_bounce,
                          "bytes_per_ray": round(tot_alg / rays_per_step, 1)},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
@@ -1138,6 +1167,7 @@ def main():
                     help="CPU legs trace every Nth ray of each set")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (lrx_trace_host) leg")
+    ap.add_argument("--no-big-bounce", action="store_true", help="skip the 8 M-ray bounce launch")
     ap.add_argument("--sweep", action="store_true", help="also time other launch configurations")
     ap.add_argument("--treelet-passes", type=int, default=None, help="BVH treelet passes (default: the library's)")
     ap.add_argument("--build-sweep", action="store_true",
