@@ -1616,38 +1616,58 @@ lrx_status lrx_trace_host_batches(const lrx_host_batch *batches, uint32_t n_batc
 	if ((rc = stream_pool(dev, &pool)) != LRX_OK) return rc;
 	LRX_CUDA(cudaEventRecord(side->fork, st));
 	for (uint32_t j = 0; j < kSideStreams; ++j) LRX_CUDA(cudaStreamWaitEvent(side->s[j], side->fork, 0));
-	// Batches are cut into chunks of at most kHostChunkRays rays; each chunk
-	// runs copy in -> trace -> copy out on a side stream (round robin over
-	// kSideStreams, one per chunk for up to that many chunks), so one chunk's
-	// copies overlap the other chunks' traces and their launches' drains
-	// overlap each other.  Staging comes from the stream-ordered pool and goes
-	// back after the chunk's copy out.  Masked rays keep the caller's hit
-	// contents: when the hit buffer is mapped host memory, only the masked
-	// slots are read back from it after the trace; otherwise the chunk's hits
-	// are copied in first.
+	// Batches are cut into chunks of at most kHostChunkRays rays and run as a
+	// three-stage pipeline: every chunk's copy in on the first side stream,
+	// back to back, so the host-to-device copies never wait behind a trace or
+	// a copy out; its trace on one of the middle side streams (round robin, so
+	// the launches' drains overlap each other); its copy out on the last side
+	// stream.  Events order each chunk's stages.  Staging comes from the
+	// stream-ordered pool and is freed on the copy-out stream.  Masked rays
+	// keep the caller's hit contents: when the hit buffer is mapped host
+	// memory, only the masked slots are read back from it after the trace;
+	// otherwise the chunk's hits are copied in first.
+	static_assert(kSideStreams >= 3, "copy-in, trace and copy-out side streams");
 	auto run = [&]() -> lrx_status {
-		uint32_t used = 0;
+		cudaStream_t s_in = side->s[0], s_out = side->s[kSideStreams - 1];
+		uint32_t chunk = 0;
 		for (uint32_t k = 0; k < n_batches; ++k) {
 			const lrx_host_batch &b = batches[k];
 			void *mapped_hits = nullptr;
 			const bool mapped = b.count && mapped_host_range(b.h_hits, sizeof(lrx_hit) * (size_t)b.count, &mapped_hits);
-			for (uint32_t c0 = 0; c0 < b.count; c0 += kHostChunkRays) {
+			for (uint32_t c0 = 0; c0 < b.count; c0 += kHostChunkRays, ++chunk) {
 				const uint32_t n = std::min(kHostChunkRays, b.count - c0);
-				cudaStream_t ss = side->s[used++ % kSideStreams];
+				cudaStream_t s_tr = side->s[1 + chunk % (kSideStreams - 2)];
 				const size_t rb = sizeof(lrx_ray) * (size_t)n, hb = sizeof(lrx_hit) * (size_t)n;
 				const lrx_ray *hr = b.h_rays + c0;
 				lrx_hit *hh = b.h_hits + c0;
-				void *d_rays = nullptr, *d_hits = nullptr;
-				LRX_CUDA(cudaMallocFromPoolAsync(&d_rays, rb, pool, ss));
-				LRX_CUDA(cudaMallocFromPoolAsync(&d_hits, hb, pool, ss));
-				LRX_CUDA(cudaMemcpyAsync(d_rays, hr, rb, cudaMemcpyHostToDevice, ss));
-				if (!mapped) LRX_CUDA(cudaMemcpyAsync(d_hits, hh, hb, cudaMemcpyHostToDevice, ss));
-				lrx_status r = trace_common(b.scene, d_rays, d_hits, n, b.mode, nullptr, ss);
-				if (r == LRX_OK && mapped)
-					r = launch_restore_masked_hits(d_rays, n, static_cast<const lrx_hit *>(mapped_hits) + c0, d_hits, ss);
-				if (r == LRX_OK) LRX_CUDA(cudaMemcpyAsync(hh, d_hits, hb, cudaMemcpyDeviceToHost, ss));
-				cudaFreeAsync(d_rays, ss);
-				cudaFreeAsync(d_hits, ss);
+				cudaEvent_t in_done = nullptr, tr_done = nullptr;
+				LRX_CUDA(cudaEventCreateWithFlags(&in_done, cudaEventDisableTiming));
+				if (cudaEventCreateWithFlags(&tr_done, cudaEventDisableTiming) != cudaSuccess) {
+					cudaEventDestroy(in_done);
+					return cuda_fail(cudaGetLastError(), "cudaEventCreateWithFlags");
+				}
+				auto stages = [&]() -> lrx_status {
+					void *d_rays = nullptr, *d_hits = nullptr;
+					LRX_CUDA(cudaMallocFromPoolAsync(&d_rays, rb, pool, s_in));
+					LRX_CUDA(cudaMallocFromPoolAsync(&d_hits, hb, pool, s_in));
+					LRX_CUDA(cudaMemcpyAsync(d_rays, hr, rb, cudaMemcpyHostToDevice, s_in));
+					if (!mapped) LRX_CUDA(cudaMemcpyAsync(d_hits, hh, hb, cudaMemcpyHostToDevice, s_in));
+					LRX_CUDA(cudaEventRecord(in_done, s_in));
+					LRX_CUDA(cudaStreamWaitEvent(s_tr, in_done, 0));
+					lrx_status r = trace_common(b.scene, d_rays, d_hits, n, b.mode, nullptr, s_tr);
+					if (r == LRX_OK && mapped)
+						r = launch_restore_masked_hits(d_rays, n, static_cast<const lrx_hit *>(mapped_hits) + c0, d_hits,
+								s_tr);
+					LRX_CUDA(cudaEventRecord(tr_done, s_tr));
+					LRX_CUDA(cudaStreamWaitEvent(s_out, tr_done, 0));
+					if (r == LRX_OK) LRX_CUDA(cudaMemcpyAsync(hh, d_hits, hb, cudaMemcpyDeviceToHost, s_out));
+					cudaFreeAsync(d_rays, s_out);
+					cudaFreeAsync(d_hits, s_out);
+					return r;
+				};
+				const lrx_status r = stages();
+				cudaEventDestroy(in_done);  // released once the recorded work completes
+				cudaEventDestroy(tr_done);
 				if (r != LRX_OK) return r;
 			}
 		}

@@ -154,7 +154,7 @@ constexpr uint32_t kQueueSlots = 4096;      // concurrent queue launches per dev
 constexpr uint32_t kMaxFetchRays = 0x7fffffffu;  // rays per fetch-kernel launch (claims stay below 2^32)
 constexpr uint32_t kDirectBatchRays = 131072;  // lrx_trace_batches: batches this large get launches of their own
 constexpr uint32_t kMaxDirectBatches = 4;      // ... when a call holds at most this many of them
-constexpr uint32_t kSideStreams = 4;           // side streams per thread and device
+constexpr uint32_t kSideStreams = 6;           // side streams per thread and device
 constexpr uint32_t kHostChunkRays = 1u << 20;  // lrx_trace_host_batches: rays per copy-in/trace/copy-out chunk
 struct QueueParams {
 	uint32_t n, total_tiles, slot;
