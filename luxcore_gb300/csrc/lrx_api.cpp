@@ -1,6 +1,8 @@
 // C-ABI layer of liblrx.so: scene assembly on the device, instance
-// transforms, tracing entry points and error reporting.  Declarations and
-// the reference interfaces each entry point replaces are in include/lrx.h.
+// transforms, launch configuration, the autotuner and error reporting.  The
+// tracing entry points are in lrx_launch.cpp, built-scene blobs in
+// lrx_blob.cpp.  Declarations and the reference interfaces each entry point
+// replaces are in include/lrx.h.
 //
 // Compiled with -ffp-contract=off so the host-side FP32 arithmetic below
 // (Matrix4x4::Inverse, instance boxes) rounds exactly as the reference's.
@@ -19,6 +21,7 @@
 
 #include "lrx_common.cuh"
 #include "lrx_internal.h"
+#include "lrx_scene.h"
 
 namespace lrx {
 
@@ -172,75 +175,13 @@ static bool all_finite(const float *v, int n) {
 	return true;
 }
 
-struct Blas {
-	uint32_t mesh = kNull;        // instanced mesh, or kNull for the merged plain BLAS
-	uint32_t tri_count = 0;
-	uint32_t root = kNull;        // absolute node index
-	float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
-};
-
 }  // namespace lrx
 
 using namespace lrx;
 
-struct lrx_scene {
-	int device = 0;
-	bool two_level = false;
-	uint32_t root = kNull;
-	DevBuf nodes, tris, insts, status, stage_rays, stage_hits;
-	std::vector<Blas> blas;
-	std::vector<uint32_t> obj_blas;     // per object: BLAS index, kNull if empty
-	std::vector<uint32_t> obj_flags;
-	uint32_t mesh_count = 0;
-	uint32_t plain_blas = kNull;        // index of the merged plain BLAS
-	uint32_t tlas_node_offset = 0;
-	uint32_t tlas_capacity = 0;
-	uint32_t blas_node_total = 0;
-	lrx_build_opts opts{};
-	// default launch per mode (closest, any-hit): 64-thread blocks, triangles
-	// deferred below 8 lanes (best of a block-size x postpone sweep on the
-	// heightfield ray sets).  Closest-hit batches run on persistent warps that
-	// refill once 8 lanes are idle (+28 % on incoherent bounce rays there, -4 %
-	// on coherent primary rays); any-hit batches are reordered by octant +
-	// origin first (+20 % on shadow rays; the sort costs more than it saves on
-	// closest-hit rays, and persistent warps add nothing after it)
-	lrx_trace_config tcfg[2] = {{sizeof(lrx_trace_config), 64, 8, kVarPersistent, 1, 8},
-			{sizeof(lrx_trace_config), 64, 8, kVarSortRays, 2, 0}};
-	lrx_scene_info info{};
-	BuildScratch scratch;
-	std::mutex mu;
-	float bounds_lo[3] = {0, 0, 0}, bounds_hi[3] = {0, 0, 0};  // world box of the root
-	// motion-blurred instances: per object an index into motions (kNull: none)
-	struct Motion {
-		std::vector<MotionInterval> its;  // keyframes + 1 intervals (the device gets the first keyframes)
-		uint32_t offset16 = 0;            // device copy, in 16-byte units from the instance array's base
-		bool have_box = false;
-		float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};  // swept world box, padded
-	};
-	std::vector<uint32_t> obj_motion;
-	std::vector<Motion> motions;
-};
-
 int lrx::scene_device(const lrx_scene *scene) { return scene->device; }
 
 namespace {
-
-// Children per wide node of a scene's builds (0 in blobs written before the
-// option existed: the 8-wide default).
-static uint32_t node_width(const lrx_build_opts &o) {
-	return o.node_width ? o.node_width : 8u;
-}
-
-struct DeviceGuard {
-	int prev = -1;
-	explicit DeviceGuard(int dev) {
-		if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) cudaSetDevice(dev);
-		else prev = -1;
-	}
-	~DeviceGuard() {
-		if (prev >= 0) cudaSetDevice(prev);
-	}
-};
 
 lrx_status validate_meshes(const lrx_mesh_desc *meshes, uint32_t n) {
 	for (uint32_t i = 0; i < n; ++i) {
@@ -747,317 +688,15 @@ lrx_status lrx_scene_get_info(const lrx_scene *s, lrx_scene_info *info) {
 	return LRX_OK;
 }
 
-// ---------------------------------------------------------------------------
-// Scene keys and blobs (a cache of built scenes)
-// ---------------------------------------------------------------------------
-
-extern "C++" {
-namespace {
-
-// 64-bit mixing hash over bytes, 8 at a time (a cache key, not a checksum
-// against adversaries).
-struct Hash64 {
-	uint64_t h = 0x6a09e667f3bcc909ull;
-	void words(const void *p, size_t n) {
-		const unsigned char *b = static_cast<const unsigned char *>(p);
-		size_t i = 0;
-		for (; i + 8 <= n; i += 8) {
-			uint64_t w;
-			std::memcpy(&w, b + i, 8);
-			mix(w);
-		}
-		uint64_t tail = 0;
-		std::memcpy(&tail, b + i, n - i);
-		mix(tail ^ ((uint64_t)(n - i) << 56));
-	}
-	template <class T> void value(const T &v) { words(&v, sizeof(v)); }
-	void mix(uint64_t w) {
-		h ^= w + 0x9e3779b97f4a7c15ull + (h << 6) + (h >> 2);
-		h *= 0xff51afd7ed558ccdull;
-		h ^= h >> 33;
-	}
-};
-
-constexpr char kBlobMagic[8] = {'L', 'R', 'X', 'S', 'C', 'E', 'N', 'E'};
-constexpr uint32_t kBlobVersion = 2;
-
-struct BlobWriter {
-	unsigned char *p;  // null: only count
-	size_t n = 0;
-	void bytes(const void *src, size_t k) {
-		if (p) std::memcpy(p + n, src, k);
-		n += k;
-	}
-	template <class T> void value(const T &v) { bytes(&v, sizeof(v)); }
-	template <class T> void vec(const std::vector<T> &v) {
-		value((uint64_t)v.size());
-		if (!v.empty()) bytes(v.data(), sizeof(T) * v.size());
-	}
-};
-
-struct BlobReader {
-	const unsigned char *p;
-	size_t size, n = 0;
-	bool ok = true;
-	const unsigned char *take(size_t k) {
-		if (!ok || k > size - n) {
-			ok = false;
-			return nullptr;
-		}
-		const unsigned char *q = p + n;
-		n += k;
-		return q;
-	}
-	template <class T> T value() {
-		T v{};
-		const unsigned char *q = take(sizeof(T));
-		if (q) std::memcpy(&v, q, sizeof(T));
-		return v;
-	}
-	template <class T> bool vec(std::vector<T> &v, uint64_t max_items) {
-		const uint64_t k = value<uint64_t>();
-		if (!ok || k > max_items) return ok = false;
-		v.resize(k);
-		const unsigned char *q = take(sizeof(T) * k);
-		if (q && k) std::memcpy(v.data(), q, sizeof(T) * k);
-		return ok;
-	}
-};
-
-}  // namespace
-}  // extern "C++"
-
-lrx_status lrx_scene_key(const lrx_mesh_desc *meshes, uint32_t mesh_count, const lrx_object_desc *objects,
-		uint32_t object_count, const lrx_build_opts *opts, uint64_t *key) {
-	if (!key || (mesh_count && !meshes) || (object_count && !objects)) {
-		set_error("lrx_scene_key: null argument");
-		return LRX_ERR_INVALID_ARGUMENT;
-	}
-	Hash64 h;
-	h.value(mesh_count);
-	for (uint32_t i = 0; i < mesh_count; ++i) {
-		const lrx_mesh_desc &m = meshes[i];
-		if ((m.vertex_count && !m.vertices) || (m.triangle_count && !m.triangles)) {
-			set_error("lrx_scene_key: mesh " + std::to_string(i) + " has null arrays");
-			return LRX_ERR_INVALID_ARGUMENT;
-		}
-		h.value(m.vertex_count);
-		h.value(m.triangle_count);
-		h.words(m.vertices, sizeof(float) * 3 * (size_t)m.vertex_count);
-		h.words(m.triangles, sizeof(uint32_t) * 3 * (size_t)m.triangle_count);
-	}
-	h.value(objects ? object_count : mesh_count);
-	for (uint32_t i = 0; objects && i < object_count; ++i) {
-		const lrx_object_desc &o = objects[i];
-		h.value(o.mesh);
-		h.value(o.flags);
-		if (o.flags & LRX_OBJECT_INSTANCE) h.words(o.transform, sizeof(o.transform));
-		if ((o.flags & LRX_OBJECT_INSTANCE) && (o.flags & LRX_OBJECT_HAS_INVERSE)) h.words(o.inverse, sizeof(o.inverse));
-	}
-	uint32_t leaf_max = 3, passes = 2, width = 8;  // the lrx_scene_create defaults
-	if (opts && opts->struct_size >= sizeof(lrx_build_opts)) {
-		if (opts->leaf_max) leaf_max = std::min(3u, opts->leaf_max);
-		passes = opts->treelet_passes;
-		if (opts->node_width) width = opts->node_width;
-	}
-	h.value(leaf_max);
-	h.value(passes);
-	if (width != 8) h.value(width);  // keys of default-width scenes as before
-	*key = h.h;
-	return LRX_OK;
-}
-
-// Blob layout: magic, version, checksum of everything after it, the host
-// metadata, then the node, triangle and instance arrays (each a u64 byte
-// count and the bytes), copied straight between the blob and device memory.
-extern "C++" {
-static void write_meta(const lrx_scene *s, BlobWriter &w) {
-	w.value((uint32_t)(s->two_level ? 1u : 0u));
-	w.value(s->root);
-	w.vec(s->blas);
-	w.vec(s->obj_blas);
-	w.vec(s->obj_flags);
-	w.value(s->mesh_count);
-	w.value(s->plain_blas);
-	w.value(s->tlas_node_offset);
-	w.value(s->tlas_capacity);
-	w.value(s->blas_node_total);
-	w.value(s->opts);
-	w.value(s->tcfg[0]);
-	w.value(s->tcfg[1]);
-	w.value(s->info);
-	w.value(s->bounds_lo);
-	w.value(s->bounds_hi);
-	w.vec(s->obj_motion);
-	w.value((uint64_t)s->motions.size());
-	for (const lrx_scene::Motion &mo : s->motions) {
-		w.value(mo.offset16);
-		w.value((uint32_t)(mo.have_box ? 1u : 0u));
-		w.value(mo.lo);
-		w.value(mo.hi);
-		w.vec(mo.its);
-	}
-}
-}  // extern "C++"
-
-static size_t blob_size(const lrx_scene *s) {
-	BlobWriter w{nullptr};
-	write_meta(s, w);
-	return 20 + w.n + 3 * 8 + s->nodes.bytes + s->tris.bytes + s->insts.bytes;
-}
-
-lrx_status lrx_scene_save(const lrx_scene *s_, void *blob, size_t *bytes, void *stream) {
-	if (!s_ || !bytes) {
-		set_error("lrx_scene_save: null argument");
-		return LRX_ERR_INVALID_ARGUMENT;
-	}
-	lrx_scene *s = const_cast<lrx_scene *>(s_);
-	std::lock_guard<std::mutex> lk(s->mu);
-	const size_t need = blob_size(s);
-	if (!blob) {
-		*bytes = need;
-		return LRX_OK;
-	}
-	if (*bytes < need) {
-		set_error("lrx_scene_save: buffer too small (" + std::to_string(need) + " bytes needed)");
-		*bytes = need;
-		return LRX_ERR_INVALID_ARGUMENT;
-	}
-	DeviceGuard g(s->device);
-	cudaStream_t st = (cudaStream_t)stream;
-	unsigned char *out = static_cast<unsigned char *>(blob);
-	BlobWriter w{out};
-	w.bytes(kBlobMagic, 8);
-	w.value(kBlobVersion);
-	w.value((uint64_t)0);  // checksum, below
-	write_meta(s, w);
-	for (const DevBuf *d : {&s->nodes, &s->tris, &s->insts}) {
-		w.value((uint64_t)d->bytes);
-		if (d->bytes) LRX_CUDA(cudaMemcpyAsync(out + w.n, d->ptr, d->bytes, cudaMemcpyDeviceToHost, st));
-		w.n += d->bytes;
-	}
-	LRX_CUDA(cudaStreamSynchronize(st));
-	Hash64 h;
-	h.words(out + 20, w.n - 20);
-	std::memcpy(out + 12, &h.h, 8);
-	*bytes = w.n;
-	return LRX_OK;
-}
-
-// Creates a scene from a blob; verify = false skips the checksum (the
-// server's own cache of blobs it wrote).
-static lrx_status scene_from_blob(const void *blob, size_t bytes, cudaStream_t st, bool verify, lrx_scene **out_scene) {
-	*out_scene = nullptr;
-	const unsigned char *b = static_cast<const unsigned char *>(blob);
-	if (bytes < 20 || std::memcmp(b, kBlobMagic, 8) != 0) {
-		set_error("lrx_scene_load: not a scene blob");
-		return LRX_ERR_INVALID_ARGUMENT;
-	}
-	uint32_t version;
-	uint64_t sum;
-	std::memcpy(&version, b + 8, 4);
-	std::memcpy(&sum, b + 12, 8);
-	if (version != kBlobVersion) {
-		set_error("lrx_scene_load: blob version " + std::to_string(version) + " is not supported");
-		return LRX_ERR_NOT_SUPPORTED;
-	}
-	if (verify) {
-		Hash64 h;
-		h.words(b + 20, bytes - 20);
-		if (h.h != sum) {
-			set_error("lrx_scene_load: checksum mismatch (corrupt or truncated blob)");
-			return LRX_ERR_INVALID_ARGUMENT;
-		}
-	}
-	int dev = 0;
-	LRX_CUDA(cudaGetDevice(&dev));
-	try {
-		lrx_scene *s = new lrx_scene();
-		std::unique_ptr<lrx_scene> guard(s);
-		s->device = dev;
-		BlobReader r{b + 20, bytes - 20};
-		const uint64_t lim = bytes;  // no vector can hold more items than the blob has bytes
-		s->two_level = r.value<uint32_t>() != 0;
-		s->root = r.value<uint32_t>();
-		r.vec(s->blas, lim);
-		r.vec(s->obj_blas, lim);
-		r.vec(s->obj_flags, lim);
-		s->mesh_count = r.value<uint32_t>();
-		s->plain_blas = r.value<uint32_t>();
-		s->tlas_node_offset = r.value<uint32_t>();
-		s->tlas_capacity = r.value<uint32_t>();
-		s->blas_node_total = r.value<uint32_t>();
-		s->opts = r.value<lrx_build_opts>();
-		s->tcfg[0] = r.value<lrx_trace_config>();
-		s->tcfg[1] = r.value<lrx_trace_config>();
-		s->info = r.value<lrx_scene_info>();
-		for (int c = 0; c < 3; ++c) s->bounds_lo[c] = r.value<float>();
-		for (int c = 0; c < 3; ++c) s->bounds_hi[c] = r.value<float>();
-		r.vec(s->obj_motion, lim);
-		const uint64_t n_motion = r.value<uint64_t>();
-		if (n_motion > lim) r.ok = false;
-		for (uint64_t k = 0; r.ok && k < n_motion; ++k) {
-			lrx_scene::Motion mo;
-			mo.offset16 = r.value<uint32_t>();
-			mo.have_box = r.value<uint32_t>() != 0;
-			for (int c = 0; c < 3; ++c) mo.lo[c] = r.value<float>();
-			for (int c = 0; c < 3; ++c) mo.hi[c] = r.value<float>();
-			r.vec(mo.its, lim);
-			if (mo.its.size() < 2) r.ok = false;
-			s->motions.push_back(std::move(mo));
-		}
-		const unsigned char *arr[3];
-		uint64_t len[3];
-		for (int k = 0; k < 3; ++k) {
-			len[k] = r.value<uint64_t>();
-			arr[k] = r.take(len[k]);
-		}
-		if (!r.ok || r.n != r.size || len[0] % sizeof(WideNode) || len[1] % sizeof(TriRecord) ||
-				len[2] % 16 || s->obj_blas.size() != s->obj_flags.size() || s->obj_motion.size() != s->obj_flags.size() ||
-				(s->root != kNull && (uint64_t)s->root * sizeof(WideNode) >= len[0])) {
-			set_error("lrx_scene_load: malformed blob");
-			return LRX_ERR_INVALID_ARGUMENT;
-		}
-		lrx_status rc;
-		if ((rc = s->nodes.alloc(std::max<size_t>(len[0], sizeof(WideNode)))) != LRX_OK) return rc;
-		if ((rc = s->tris.alloc(std::max<size_t>(len[1], sizeof(TriRecord)))) != LRX_OK) return rc;
-		if (len[2] && (rc = s->insts.alloc(len[2])) != LRX_OK) return rc;
-		if ((rc = s->status.alloc(64)) != LRX_OK) return rc;
-		LRX_CUDA(cudaMemsetAsync(s->status.ptr, 0, 64, st));
-		DevBuf *dst[3] = {&s->nodes, &s->tris, &s->insts};
-		for (int k = 0; k < 3; ++k)
-			if (len[k]) LRX_CUDA(cudaMemcpyAsync(dst[k]->ptr, arr[k], len[k], cudaMemcpyHostToDevice, st));
-		LRX_CUDA(cudaStreamSynchronize(st));
-		s->info.device_bytes = s->nodes.bytes + s->tris.bytes + s->insts.bytes + s->status.bytes;
-		*out_scene = guard.release();
-		return LRX_OK;
-	} catch (const std::bad_alloc &) {
-		set_error("lrx_scene_load: host allocation failed");
-		return LRX_ERR_OUT_OF_MEMORY;
-	}
-}
-
-lrx_status lrx_scene_load(const void *blob, size_t bytes, void *stream, lrx_scene **out_scene) {
-	if (!blob || !out_scene) {
-		set_error("lrx_scene_load: null argument");
-		return LRX_ERR_INVALID_ARGUMENT;
-	}
-	return scene_from_blob(blob, bytes, (cudaStream_t)stream, true, out_scene);
-}
-
-extern "C++" lrx_status lrx::scene_load_trusted(const void *blob, size_t bytes, cudaStream_t stream,
-		lrx_scene **out_scene) {
-	return scene_from_blob(blob, bytes, stream, false, out_scene);
-}
 
 // A correct walk visits each node at most once per BLAS entry, so a ray never
 // needs more than (instances + 1) x nodes visits.
-static uint32_t scene_visit_limit(const lrx_scene *s) {
+extern "C++" uint32_t lrx::scene_visit_limit(const lrx_scene *s) {
 	const uint64_t lim = (uint64_t)(s->info.instance_count + 1) * (s->info.node_count + 1) + 64;
 	return (uint32_t)std::min<uint64_t>(lim, kMaxVisits);
 }
 
-static lrx_status trace_common(lrx_scene *s, const void *d_rays, void *d_hits, uint32_t count, uint32_t mode,
+extern "C++" lrx_status lrx::trace_common(lrx_scene *s, const void *d_rays, void *d_hits, uint32_t count, uint32_t mode,
 		uint64_t *d_counters, cudaStream_t st) {
 	if (!s) {
 		set_error("lrx_trace: null scene");
@@ -1287,401 +926,6 @@ lrx_status lrx_scene_create_autotuned(const lrx_mesh_desc *meshes, uint32_t mesh
 	return LRX_OK;
 }
 
-lrx_status lrx_trace(lrx_scene *s, const void *d_rays, void *d_hits, uint32_t count, uint32_t mode, void *stream) {
-	return trace_common(s, d_rays, d_hits, count, mode, nullptr, (cudaStream_t)stream);
-}
-
-lrx_status lrx_trace_batches(const lrx_batch *batches, uint32_t n_batches, void *stream) {
-	return lrx_trace_batches_ex(batches, n_batches, stream, nullptr, nullptr);
-}
-
-// Streams and events of the calling thread on one device for the batches
-// lrx_trace_batches launches on their own (created on first use, never
-// shared with another thread, so a graph capture on one thread cannot catch
-// another thread's work).
-struct SideStreams {
-	int dev = -1;
-	cudaStream_t s[kSideStreams] = {};
-	cudaEvent_t fork = nullptr, join[kSideStreams] = {};
-	SideStreams() = default;
-	SideStreams(const SideStreams &) = delete;
-	SideStreams &operator=(const SideStreams &) = delete;
-	~SideStreams() {  // at thread exit; errors (a context already torn down) are ignored
-		for (uint32_t k = 0; k < kSideStreams; ++k) {
-			if (s[k]) cudaStreamDestroy(s[k]);
-			if (join[k]) cudaEventDestroy(join[k]);
-		}
-		if (fork) cudaEventDestroy(fork);
-	}
-};
-
-static lrx_status side_streams(int dev, SideStreams **out) {
-	thread_local std::vector<std::unique_ptr<SideStreams>> per_dev;
-	for (auto &p : per_dev)
-		if (p->dev == dev) {
-			*out = p.get();
-			return LRX_OK;
-		}
-	std::unique_ptr<SideStreams> ss(new SideStreams());
-	ss->dev = dev;
-	for (uint32_t k = 0; k < kSideStreams; ++k) {
-		LRX_CUDA(cudaStreamCreateWithFlags(&ss->s[k], cudaStreamNonBlocking));
-		LRX_CUDA(cudaEventCreateWithFlags(&ss->join[k], cudaEventDisableTiming));
-	}
-	LRX_CUDA(cudaEventCreateWithFlags(&ss->fork, cudaEventDisableTiming));
-	*out = ss.get();
-	per_dev.push_back(std::move(ss));
-	return LRX_OK;
-}
-
-// A batch traced by a launch of its own rather than in the queue launch:
-// one on a scene with motion instances, or -- when the call holds at most
-// kMaxDirectBatches batches of kDirectBatchRays rays or more -- one of those.
-static bool direct_batch(const lrx_batch &b, bool big_direct) {
-	return b.count != 0 && ((big_direct && b.count >= kDirectBatchRays) || !b.scene->motions.empty());
-}
-
-lrx_status lrx_trace_batches_ex(const lrx_batch *batches, uint32_t n_batches, void *stream,
-		uint32_t *d_tile_counters, uint32_t *d_done_flags) {
-	if (n_batches && !batches) {
-		set_error("lrx_trace_batches: null batch array");
-		return LRX_ERR_INVALID_ARGUMENT;
-	}
-	if ((d_tile_counters == nullptr) != (d_done_flags == nullptr)) {
-		set_error("lrx_trace_batches_ex: give both the tile counters and the done flags, or neither");
-		return LRX_ERR_INVALID_ARGUMENT;
-	}
-	int dev = 0;
-	for (uint32_t k = 0; k < n_batches; ++k) {
-		const lrx_batch &b = batches[k];
-		if (!b.scene || b.mode > LRX_TRACE_ANY) {
-			set_error("lrx_trace_batches: batch " + std::to_string(k) + ": null scene or unknown mode");
-			return LRX_ERR_INVALID_ARGUMENT;
-		}
-		if (b.count && (!b.d_rays || !b.d_hits || ((uintptr_t)b.d_rays & 15u) || ((uintptr_t)b.d_hits & 3u))) {
-			set_error("lrx_trace_batches: batch " + std::to_string(k) + ": null or misaligned ray/hit buffer");
-			return LRX_ERR_INVALID_ARGUMENT;
-		}
-		if (k == 0) dev = b.scene->device;
-		if (b.scene->device != dev) {
-			set_error("lrx_trace_batches: all scenes of one call must live on one device");
-			return LRX_ERR_INVALID_ARGUMENT;
-		}
-	}
-	if (n_batches == 0) return LRX_OK;
-	DeviceGuard g(dev);
-	thread_local std::unique_ptr<QueueParams> params;
-	if (!params) params.reset(new QueueParams());
-	QueueParams &p = *params;
-	cudaStream_t st = (cudaStream_t)stream;
-	// Warp-level ray fetch when any batch's scene asks for persistent warps in
-	// its mode (refill from the first such config) and every batch fits one
-	// fetch launch; otherwise 64-ray tiles per block.
-	uint32_t n_big = 0;
-	for (uint32_t k = 0; k < n_batches; ++k) n_big += batches[k].count >= kDirectBatchRays ? 1u : 0u;
-	const bool big_direct = n_big <= kMaxDirectBatches;
-	uint32_t fetch = 0, refill = 16;
-	for (uint32_t k = 0; k < n_batches; ++k) {
-		if (direct_batch(batches[k], big_direct)) continue;
-		if (batches[k].count > kMaxFetchRays) {
-			fetch = 0;
-			break;
-		}
-		const lrx_trace_config &cfg = batches[k].scene->tcfg[batches[k].mode == LRX_TRACE_ANY ? 1 : 0];
-		if (!fetch && (cfg.variant & kVarPersistent)) {
-			fetch = 1;
-			if (cfg.refill) refill = std::min(32u, cfg.refill);
-		}
-	}
-	p.fetch = fetch;
-	p.refill = refill;
-	p.tiles_done = d_tile_counters;
-	p.done_flags = d_done_flags;
-	if (d_tile_counters) LRX_CUDA(cudaMemsetAsync(d_tile_counters, 0, sizeof(uint32_t) * n_batches, st));
-	// The batches of one launch are gathered first, then laid out by ray class
-	// (closest/any x flat/two-level) so each class is one contiguous range.
-	struct Entry {
-		uint32_t k, cls;
-		bool sort;  // scene config sorts rays and the batch has >= kSortMinRays
-	};
-	std::vector<Entry> pending;
-	uint64_t pend_tiles = 0, pend_rays = 0, pend_sorted = 0;
-	std::vector<SortBatch> sorted;
-	auto flush = [&]() -> lrx_status {
-		if (pending.empty()) return LRX_OK;
-		std::stable_sort(pending.begin(), pending.end(), [](const Entry &a, const Entry &b) { return a.cls < b.cls; });
-		p.n = 0;
-		p.total_tiles = 0;
-		p.total_rays = 0;
-		p.order = nullptr;
-		sorted.clear();
-		uint32_t sorted_rays = 0;
-		for (uint32_t c = 0; c <= 4; ++c) p.class_batch[c] = (uint32_t)pending.size();
-		for (const Entry &e : pending) {
-			const lrx_batch &b = batches[e.k];
-			lrx_scene *s = b.scene;
-			const lrx_trace_config &cfg = s->tcfg[b.mode == LRX_TRACE_ANY ? 1 : 0];
-			if (p.class_batch[e.cls] == pending.size()) p.class_batch[e.cls] = p.n;
-			QueueBatch &q = p.b[p.n++];
-			q.nodes = s->nodes.as<WideNode>();
-			q.tris = s->tris.as<TriRecord>();
-			q.insts = s->insts.as<InstRecord>();
-			q.rays = b.d_rays;
-			q.hits = b.d_hits;
-			q.status = s->status.as<uint32_t>();
-			q.root = s->root;
-			q.count = b.count;
-			q.tile_begin = p.total_tiles;
-			q.ray_begin = p.total_rays;
-			// runtime-selectable variants only (cache hints); sorting is done before the launch
-			const uint32_t var = cfg.variant & (LRX_VARIANT_SCENE_L2_KEEP | LRX_VARIANT_STREAM_RAYS);
-			q.flags = (b.mode == LRX_TRACE_ANY ? 1u : 0u) | (s->two_level ? 2u : 0u) |
-					((cfg.postpone & 0xffu) << 8) | (var << 16);
-			q.visit_limit = scene_visit_limit(s);
-			q.user_index = e.k;
-			q.order_begin = kNull;
-			if (e.sort) {
-				SortBatch sb;
-				sb.rays = b.d_rays;
-				sb.count = b.count;
-				sb.offset = sorted_rays;
-				for (int c = 0; c < 3; ++c) {
-					sb.lo[c] = s->bounds_lo[c];
-					sb.hi[c] = s->bounds_hi[c];
-				}
-				sb.octant_only = (cfg.variant & kVarSortOctantOnly) != 0;
-				sorted.push_back(sb);
-				q.order_begin = sorted_rays;
-				sorted_rays += b.count;
-			}
-			p.total_tiles += (b.count + kTileRays - 1) / kTileRays;
-			p.total_rays += fetch ? b.count : 0u;
-		}
-		// a class with no batches starts where the next non-empty one does
-		for (int c = 3; c >= 0; --c) p.class_batch[c] = std::min(p.class_batch[c], p.class_batch[c + 1]);
-		p.slot = next_queue_slot();
-		void *scratch = nullptr;
-		lrx_status rc = sort_queue_batches(sorted, sorted_rays, st, &p.order, &scratch);
-		if (rc == LRX_OK) rc = launch_trace_queue(p, st);
-		if (scratch) cudaFreeAsync(scratch, st);  // ordered after the launch that reads it
-		pending.clear();
-		pend_tiles = pend_rays = pend_sorted = 0;
-		return rc;
-	};
-	// A few large batches (at most kMaxDirectBatches of at least kDirectBatchRays
-	// rays -- a wavefront's camera, bounce and shadow buffers), and batches on
-	// scenes with motion instances (the queue kernels carry no motion code),
-	// are traced by launches of their own -- the scene's plain path -- on side
-	// streams forked from `stream` and joined back into it, so their launches
-	// run beside each other and beside the queue launch of the other batches:
-	// one launch's drain (its last, longest rays) overlaps the others' work.
-	// Many large batches stay in the queue launch, which drains once for all
-	// of them.  A direct batch's completion flag follows its launch on its
-	// side stream.
-	SideStreams *side = nullptr;
-	auto trace_all = [&]() -> lrx_status {
-		uint32_t n_direct = 0;
-		for (uint32_t k = 0; k < n_batches; ++k) {
-			const lrx_batch &b = batches[k];
-			if (!direct_batch(b, big_direct)) continue;
-			if (!side) {
-				lrx_status rc = side_streams(dev, &side);
-				if (rc != LRX_OK) return rc;
-				LRX_CUDA(cudaEventRecord(side->fork, st));
-				for (uint32_t j = 0; j < kSideStreams; ++j) LRX_CUDA(cudaStreamWaitEvent(side->s[j], side->fork, 0));
-			}
-			cudaStream_t ss = side->s[n_direct++ % kSideStreams];
-			lrx_status rc = trace_common(b.scene, b.d_rays, b.d_hits, b.count, b.mode, nullptr, ss);
-			if (rc == LRX_OK && d_done_flags) rc = launch_set_flag(d_done_flags + k, ss);
-			if (rc != LRX_OK) return rc;
-		}
-		for (uint32_t k = 0; k < n_batches; ++k) {
-			const lrx_batch &b = batches[k];
-			if (b.count == 0 || direct_batch(b, big_direct)) continue;
-			lrx_scene *s = b.scene;
-			const uint32_t tiles = (b.count + kTileRays - 1) / kTileRays;
-			const lrx_trace_config &cfg = s->tcfg[b.mode == LRX_TRACE_ANY ? 1 : 0];
-			const bool sort = (cfg.variant & kVarSortRays) && b.count >= kSortMinRays && s->root != kNull;
-			if (pending.size() == kMaxQueueBatches || pend_tiles + tiles > 0xffffffffull ||
-					(fetch && pend_rays + b.count > kMaxFetchRays) || (sort && pend_sorted + b.count > kMaxFetchRays)) {
-				lrx_status rc = flush();
-				if (rc != LRX_OK) return rc;
-			}
-			pending.push_back({k, (b.mode == LRX_TRACE_ANY ? 2u : 0u) | (s->two_level ? 1u : 0u), sort});
-			pend_tiles += tiles;
-			pend_rays += b.count;
-			pend_sorted += sort ? b.count : 0u;
-		}
-		return flush();
-	};
-	const lrx_status rc = trace_all();
-	if (side) {  // join every side stream back, also after an error (a capture must not stay forked)
-		for (uint32_t j = 0; j < kSideStreams; ++j) {
-			cudaEventRecord(side->join[j], side->s[j]);
-			cudaStreamWaitEvent(st, side->join[j], 0);
-		}
-	}
-	return rc;
-}
-
-lrx_status lrx_trace_counted(lrx_scene *s, const void *d_rays, void *d_hits, uint32_t count, uint32_t mode,
-		uint64_t *d_counters, void *stream) {
-	if (!d_counters) {
-		set_error("lrx_trace_counted: null counters");
-		return LRX_ERR_INVALID_ARGUMENT;
-	}
-	return trace_common(s, d_rays, d_hits, count, mode, d_counters, (cudaStream_t)stream);
-}
-
-lrx_status lrx_trace_host(lrx_scene *s, const lrx_ray *h_rays, lrx_hit *h_hits, uint32_t count, uint32_t mode,
-		void *stream) {
-	if (!s) {
-		set_error("lrx_trace_host: null scene");
-		return LRX_ERR_INVALID_ARGUMENT;
-	}
-	if (count == 0) return LRX_OK;
-	if (!h_rays || !h_hits) {
-		set_error("lrx_trace_host: null ray or hit buffer");
-		return LRX_ERR_INVALID_ARGUMENT;
-	}
-	if (count > kHostChunkRays) {  // chunks whose copies overlap each other's traces
-		const lrx_host_batch b{s, h_rays, h_hits, count, mode};
-		return lrx_trace_host_batches(&b, 1, stream);
-	}
-	std::lock_guard<std::mutex> lk(s->mu);
-	DeviceGuard g(s->device);
-	lrx_status rc;
-	if ((rc = s->stage_rays.alloc(sizeof(lrx_ray) * (size_t)count)) != LRX_OK) return rc;
-	if ((rc = s->stage_hits.alloc(sizeof(lrx_hit) * (size_t)count)) != LRX_OK) return rc;
-	cudaStream_t st = (cudaStream_t)stream;
-	LRX_CUDA(cudaMemcpyAsync(s->stage_rays.ptr, h_rays, sizeof(lrx_ray) * (size_t)count, cudaMemcpyHostToDevice, st));
-	// masked rays keep the caller's hit contents: stage them first
-	LRX_CUDA(cudaMemcpyAsync(s->stage_hits.ptr, h_hits, sizeof(lrx_hit) * (size_t)count, cudaMemcpyHostToDevice, st));
-	if ((rc = trace_common(s, s->stage_rays.ptr, s->stage_hits.ptr, count, mode, nullptr, st)) != LRX_OK) return rc;
-	LRX_CUDA(cudaMemcpyAsync(h_hits, s->stage_hits.ptr, sizeof(lrx_hit) * (size_t)count, cudaMemcpyDeviceToHost, st));
-	LRX_CUDA(cudaStreamSynchronize(st));
-	return LRX_OK;
-}
-
-// Device view of host memory the device can reach directly -- pinned and
-// mapped (cudaHostAlloc, cudaHostRegister) under unified addressing -- for
-// the `bytes` bytes at h: both ends must resolve, to device addresses
-// `bytes - 1` apart.  Pageable memory (cudaMemoryTypeUnregistered) and device
-// memory give false.
-static bool mapped_host_range(const void *h, size_t bytes, void **d) {
-	cudaPointerAttributes a0, a1;
-	if (cudaPointerGetAttributes(&a0, h) != cudaSuccess) {
-		cudaGetLastError();
-		return false;
-	}
-	const void *last = static_cast<const char *>(h) + (bytes - 1);
-	if (cudaPointerGetAttributes(&a1, last) != cudaSuccess) {
-		cudaGetLastError();
-		return false;
-	}
-	if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer || !a1.devicePointer)
-		return false;
-	if (static_cast<const char *>(a1.devicePointer) - static_cast<const char *>(a0.devicePointer) !=
-			(std::ptrdiff_t)(bytes - 1))
-		return false;
-	*d = a0.devicePointer;
-	return true;
-}
-
-lrx_status lrx_trace_host_batches(const lrx_host_batch *batches, uint32_t n_batches, void *stream) {
-	if (n_batches && !batches) {
-		set_error("lrx_trace_host_batches: null batch array");
-		return LRX_ERR_INVALID_ARGUMENT;
-	}
-	int dev = -1;
-	for (uint32_t k = 0; k < n_batches; ++k) {
-		const lrx_host_batch &b = batches[k];
-		if (!b.scene || b.mode > LRX_TRACE_ANY || (b.count && (!b.h_rays || !b.h_hits))) {
-			set_error("lrx_trace_host_batches: batch " + std::to_string(k) + ": null scene or buffer, or unknown mode");
-			return LRX_ERR_INVALID_ARGUMENT;
-		}
-		if (dev < 0) dev = b.scene->device;
-		if (b.scene->device != dev) {
-			set_error("lrx_trace_host_batches: all scenes of one call must live on one device");
-			return LRX_ERR_INVALID_ARGUMENT;
-		}
-	}
-	if (dev < 0) return LRX_OK;
-	DeviceGuard g(dev);
-	cudaStream_t st = (cudaStream_t)stream;
-	SideStreams *side = nullptr;
-	lrx_status rc = side_streams(dev, &side);
-	if (rc != LRX_OK) return rc;
-	cudaMemPool_t pool;
-	if ((rc = stream_pool(dev, &pool)) != LRX_OK) return rc;
-	LRX_CUDA(cudaEventRecord(side->fork, st));
-	for (uint32_t j = 0; j < kSideStreams; ++j) LRX_CUDA(cudaStreamWaitEvent(side->s[j], side->fork, 0));
-	// Batches are cut into chunks of at most kHostChunkRays rays and run as a
-	// three-stage pipeline: every chunk's copy in on the first side stream,
-	// back to back, so the host-to-device copies never wait behind a trace or
-	// a copy out; its trace on one of the middle side streams (round robin, so
-	// the launches' drains overlap each other); its copy out on the last side
-	// stream.  Events order each chunk's stages.  Staging comes from the
-	// stream-ordered pool and is freed on the copy-out stream.  Masked rays
-	// keep the caller's hit contents: when the hit buffer is mapped host
-	// memory, only the masked slots are read back from it after the trace;
-	// otherwise the chunk's hits are copied in first.
-	static_assert(kSideStreams >= 3, "copy-in, trace and copy-out side streams");
-	auto run = [&]() -> lrx_status {
-		cudaStream_t s_in = side->s[0], s_out = side->s[kSideStreams - 1];
-		uint32_t chunk = 0;
-		for (uint32_t k = 0; k < n_batches; ++k) {
-			const lrx_host_batch &b = batches[k];
-			void *mapped_hits = nullptr;
-			const bool mapped = b.count && mapped_host_range(b.h_hits, sizeof(lrx_hit) * (size_t)b.count, &mapped_hits);
-			for (uint32_t c0 = 0; c0 < b.count; c0 += kHostChunkRays, ++chunk) {
-				const uint32_t n = std::min(kHostChunkRays, b.count - c0);
-				cudaStream_t s_tr = side->s[1 + chunk % (kSideStreams - 2)];
-				const size_t rb = sizeof(lrx_ray) * (size_t)n, hb = sizeof(lrx_hit) * (size_t)n;
-				const lrx_ray *hr = b.h_rays + c0;
-				lrx_hit *hh = b.h_hits + c0;
-				cudaEvent_t in_done = nullptr, tr_done = nullptr;
-				LRX_CUDA(cudaEventCreateWithFlags(&in_done, cudaEventDisableTiming));
-				if (cudaEventCreateWithFlags(&tr_done, cudaEventDisableTiming) != cudaSuccess) {
-					cudaEventDestroy(in_done);
-					return cuda_fail(cudaGetLastError(), "cudaEventCreateWithFlags");
-				}
-				auto stages = [&]() -> lrx_status {
-					void *d_rays = nullptr, *d_hits = nullptr;
-					LRX_CUDA(cudaMallocFromPoolAsync(&d_rays, rb, pool, s_in));
-					LRX_CUDA(cudaMallocFromPoolAsync(&d_hits, hb, pool, s_in));
-					LRX_CUDA(cudaMemcpyAsync(d_rays, hr, rb, cudaMemcpyHostToDevice, s_in));
-					if (!mapped) LRX_CUDA(cudaMemcpyAsync(d_hits, hh, hb, cudaMemcpyHostToDevice, s_in));
-					LRX_CUDA(cudaEventRecord(in_done, s_in));
-					LRX_CUDA(cudaStreamWaitEvent(s_tr, in_done, 0));
-					lrx_status r = trace_common(b.scene, d_rays, d_hits, n, b.mode, nullptr, s_tr);
-					if (r == LRX_OK && mapped)
-						r = launch_restore_masked_hits(d_rays, n, static_cast<const lrx_hit *>(mapped_hits) + c0, d_hits,
-								s_tr);
-					LRX_CUDA(cudaEventRecord(tr_done, s_tr));
-					LRX_CUDA(cudaStreamWaitEvent(s_out, tr_done, 0));
-					if (r == LRX_OK) LRX_CUDA(cudaMemcpyAsync(hh, d_hits, hb, cudaMemcpyDeviceToHost, s_out));
-					cudaFreeAsync(d_rays, s_out);
-					cudaFreeAsync(d_hits, s_out);
-					return r;
-				};
-				const lrx_status r = stages();
-				cudaEventDestroy(in_done);  // released once the recorded work completes
-				cudaEventDestroy(tr_done);
-				if (r != LRX_OK) return r;
-			}
-		}
-		return LRX_OK;
-	};
-	rc = run();
-	for (uint32_t j = 0; j < kSideStreams; ++j) {
-		cudaEventRecord(side->join[j], side->s[j]);
-		cudaStreamWaitEvent(st, side->join[j], 0);
-	}
-	if (rc != LRX_OK) return rc;
-	LRX_CUDA(cudaStreamSynchronize(st));
-	return LRX_OK;
-}
 
 lrx_status lrx_scene_device_status(lrx_scene *s, uint32_t *status, void *stream) {
 	if (!s || !status) {

@@ -1,0 +1,91 @@
+// The scene record behind the opaque lrx_scene handle, shared by the C-ABI
+// translation units: scene assembly (lrx_api.cpp), built-scene blobs
+// (lrx_blob.cpp) and the tracing entry points (lrx_launch.cpp).  Not part of
+// the public ABI.
+#pragma once
+
+#include <cstdint>
+#include <mutex>
+#include <vector>
+
+#include "lrx_common.cuh"
+#include "lrx_internal.h"
+
+namespace lrx {
+
+struct Blas {
+	uint32_t mesh = kNull;        // instanced mesh, or kNull for the merged plain BLAS
+	uint32_t tri_count = 0;
+	uint32_t root = kNull;        // absolute node index
+	float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+};
+
+// Children per wide node of a scene's builds (0 in blobs written before the
+// option existed: the 8-wide default).
+inline uint32_t node_width(const lrx_build_opts &o) {
+	return o.node_width ? o.node_width : 8u;
+}
+
+// Makes `dev` current for the guard's lifetime.
+struct DeviceGuard {
+	int prev = -1;
+	explicit DeviceGuard(int dev) {
+		if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) cudaSetDevice(dev);
+		else prev = -1;
+	}
+	~DeviceGuard() {
+		if (prev >= 0) cudaSetDevice(prev);
+	}
+};
+
+}  // namespace lrx
+
+struct lrx_scene {
+	int device = 0;
+	bool two_level = false;
+	uint32_t root = lrx::kNull;
+	lrx::DevBuf nodes, tris, insts, status, stage_rays, stage_hits;
+	std::vector<lrx::Blas> blas;
+	std::vector<uint32_t> obj_blas;     // per object: BLAS index, kNull if empty
+	std::vector<uint32_t> obj_flags;
+	uint32_t mesh_count = 0;
+	uint32_t plain_blas = lrx::kNull;  // index of the merged plain BLAS
+	uint32_t tlas_node_offset = 0;
+	uint32_t tlas_capacity = 0;
+	uint32_t blas_node_total = 0;
+	lrx_build_opts opts{};
+	// default launch per mode (closest, any-hit): 64-thread blocks, triangles
+	// deferred below 8 lanes (best of a block-size x postpone sweep on the
+	// heightfield ray sets).  Closest-hit batches run on persistent warps that
+	// refill once 8 lanes are idle (+28 % on incoherent bounce rays there, -4 %
+	// on coherent primary rays); any-hit batches are reordered by octant +
+	// origin first (+20 % on shadow rays; the sort costs more than it saves on
+	// closest-hit rays, and persistent warps add nothing after it)
+	lrx_trace_config tcfg[2] = {{sizeof(lrx_trace_config), 64, 8, lrx::kVarPersistent, 1, 8},
+			{sizeof(lrx_trace_config), 64, 8, lrx::kVarSortRays, 2, 0}};
+	lrx_scene_info info{};
+	lrx::BuildScratch scratch;
+	std::mutex mu;
+	float bounds_lo[3] = {0, 0, 0}, bounds_hi[3] = {0, 0, 0};  // world box of the root
+	// motion-blurred instances: per object an index into motions (kNull: none)
+	struct Motion {
+		std::vector<lrx::MotionInterval> its;  // keyframes + 1 intervals (the device gets the first keyframes)
+		uint32_t offset16 = 0;            // device copy, in 16-byte units from the instance array's base
+		bool have_box = false;
+		float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};  // swept world box, padded
+	};
+	std::vector<uint32_t> obj_motion;
+	std::vector<Motion> motions;
+};
+
+namespace lrx {
+
+// The node-visit cap of one ray in scene s (a correct walk never reaches it).
+uint32_t scene_visit_limit(const lrx_scene *s);
+
+// One trace launch of `count` rays with the scene's configuration for `mode`,
+// validating every argument (the body of lrx_trace and lrx_trace_counted).
+lrx_status trace_common(lrx_scene *s, const void *d_rays, void *d_hits, uint32_t count, uint32_t mode,
+		uint64_t *d_counters, cudaStream_t st);
+
+}  // namespace lrx
