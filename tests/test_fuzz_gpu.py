@@ -90,3 +90,86 @@ def test_random_scenes_match_the_oracle(torch_cuda, seed):
     anyh = gpu_trace(torch_cuda, s, rays, lrx.LRX_TRACE_ANY)
     a = check_anyhit(anyh[live], ref, oracle, rays[live])
     assert a["ok"], (seed, kernel, a)
+
+
+def random_motion_scene(rng, rigid):
+    """random_scene's meshes under plain objects, static instances and
+    motion-blurred instances.  Translation-only systems share one 3x3 part
+    across their keyframes (the reference's lerp path); `rigid` systems turn
+    about a random axis and scale between keyframes (its Slerp path)."""
+    scale = float(10.0 ** rng.uniform(-1, 2))
+    meshes = [random_mesh(rng, scale) for _ in range(int(rng.integers(1, 4)))]
+    objects = [(i, None) for i in range(len(meshes)) if rng.random() < 0.5]
+    t0 = float(rng.uniform(-1.0, 1.0))
+    t1 = t0 + float(rng.uniform(0.1, 2.0))
+    for _ in range(int(rng.integers(2, 14))):
+        q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+        lw = np.eye(4)
+        lw[:3, :3] = q * rng.uniform(0.2, 2.0)
+        lw[:3, 3] = rng.random(3) * scale
+        mi = int(rng.integers(0, len(meshes)))
+        if rng.random() < 0.25 and any(isinstance(m, W.Motion) for _, m in objects):
+            objects.append((mi, lw.astype(np.float32)))
+            continue
+        nk = int(rng.integers(1, 5))
+        times = np.sort(rng.uniform(t0, t1, nk)) if nk > 1 else np.array([rng.uniform(t0, t1)])
+        times = np.unique(times.astype(np.float32))
+        move = rng.normal(size=3) * scale * rng.uniform(0.0, 0.2)
+        wl0 = np.linalg.inv(lw).astype(np.float32)
+        axis = rng.normal(size=3)
+        axis /= np.linalg.norm(axis)
+        keys = []
+        for k, t in enumerate(times):
+            f = (float(t) - t0) / (t1 - t0)
+            if rigid:
+                a = rng.uniform(0.0, 0.5 * np.pi) * f
+                x, y, z = axis
+                c, s = np.cos(a), np.sin(a)
+                r = np.array([[c + x * x * (1 - c), x * y * (1 - c) - z * s, x * z * (1 - c) + y * s],
+                              [y * x * (1 - c) + z * s, c + y * y * (1 - c), y * z * (1 - c) - x * s],
+                              [z * x * (1 - c) - y * s, z * y * (1 - c) + x * s, c + z * z * (1 - c)]])
+                m = lw.copy()
+                m[:3, :3] = r @ lw[:3, :3] * (1.0 + 0.5 * f)
+                m[:3, 3] = lw[:3, 3] + move * f
+                keys.append(np.linalg.inv(m).astype(np.float32))
+            else:
+                w = wl0.copy()
+                w[:3, 3] = (wl0[:3, 3].astype(np.float64) - move * f).astype(np.float32)
+                keys.append(w)
+        objects.append((mi, W.Motion(times, np.stack(keys))))
+    return W.SceneDesc(meshes, objects), scale, (t0, t1)
+
+
+@pytest.mark.parametrize("seed", range(24))
+def test_random_motion_scenes_match_the_oracle(torch_cuda, seed):
+    """Translation-only systems meet the full parity bar (ties aside);
+    rotating ones the motion tolerance of test_motion_gpu (CUDA's sinf
+    against the C library's sin in Slerp).  Ray times run past both ends of
+    the keyframes."""
+    from test_motion_gpu import tolerant_compare
+    rng = np.random.default_rng(5000 + seed)
+    rigid = seed % 2 == 1
+    scene, scale, (t0, t1) = random_motion_scene(rng, rigid)
+    kernel = KERNEL_CONFIGS[int(rng.integers(0, len(KERNEL_CONFIGS)))]
+    s = lrx.Scene(scene, leaf_max=int(rng.integers(1, 4)), treelet_passes=int(rng.integers(0, 3)),
+                  node_width=int(rng.choice([4, 6, 8])))
+    refill = kernel[3] if len(kernel) > 3 else 0
+    s.set_trace_config(*kernel[:3], refill=refill)
+    assert s.info()["two_level"] == 1
+    oracle = po.OracleScene(scene)
+    rays = random_rays(rng, scene, scale, 20000)
+    span = t1 - t0
+    rays["time"] = rng.uniform(t0 - 0.2 * span, t1 + 0.2 * span, rays.shape[0]).astype(np.float32)
+    live = (rays["flags"] & W.RAY_FLAGS_MASKED) == 0
+    ref, _ = oracle.intersect(rays[live])
+    gpu = gpu_trace(torch_cuda, s, rays)
+    if rigid:
+        st = tolerant_compare(gpu[live], ref, oracle, rays[live], min_bitexact=0.5)
+        assert st["ok"], repr((seed, kernel, st))
+    else:
+        st = compare(gpu[live], ref, oracle, rays[live])
+        assert st["bad_disagreements"] == 0 and st["values_ok"] and st["ties_valid"], repr((seed, kernel, st))
+        assert st["agree"] >= 0.95, repr((seed, kernel, st))
+        anyh = gpu_trace(torch_cuda, s, rays, lrx.LRX_TRACE_ANY)
+        a = check_anyhit(anyh[live], ref, oracle, rays[live])
+        assert a["ok"], (seed, kernel, a)
