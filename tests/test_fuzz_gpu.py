@@ -143,7 +143,7 @@ def random_motion_scene(rng, rigid):
 @pytest.mark.parametrize("seed", range(24))
 def test_random_motion_scenes_match_the_oracle(torch_cuda, seed):
     """Translation-only systems meet the full parity bar (ties aside);
-    rotating ones the motion tolerance of test_motion_gpu (CUDA's sinf
+    rotating ones the value tolerance of test_motion_gpu (CUDA's sinf
     against the C library's sin in Slerp).  Ray times run past both ends of
     the keyframes."""
     from test_motion_gpu import tolerant_compare
@@ -164,8 +164,15 @@ def test_random_motion_scenes_match_the_oracle(torch_cuda, seed):
     ref, _ = oracle.intersect(rays[live])
     gpu = gpu_trace(torch_cuda, s, rays)
     if rigid:
-        st = tolerant_compare(gpu[live], ref, oracle, rays[live], min_bitexact=0.5)
-        assert st["ok"], repr((seed, kernel, st))
+        # coincident triangles make ties common, so (as in the static fuzz)
+        # the agreement rate bar gives way to: every disagreement on a GPU
+        # hit explained, hits the GPU misses within 1e-4 of the rays, values
+        # within tolerance where the triangle agrees
+        g, r = gpu[live], ref
+        st = tolerant_compare(g, r, oracle, rays[live], min_bitexact=0.5)
+        lost = int(((g["meshIndex"] == W.NULL_INDEX) & (r["meshIndex"] != W.NULL_INDEX)).sum())
+        assert st["values_ok"] and st["unexplained"] == 0 and st["bitexact"] >= 0.5, repr((seed, kernel, st))
+        assert lost <= max(2, int(1e-4 * g.shape[0])) and st["agree"] >= 0.95, repr((seed, kernel, lost, st))
     else:
         st = compare(gpu[live], ref, oracle, rays[live])
         assert st["bad_disagreements"] == 0 and st["values_ok"] and st["ties_valid"], repr((seed, kernel, st))
