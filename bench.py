@@ -242,7 +242,22 @@ def cpu_measure(scene, sets, threads: int, accel: str = "bvh"):
         _, s = o.intersect(rays, n_threads=threads)
         secs += s
         total += rays.shape[0]
-    return total, secs
+    return total, secs, o
+
+
+def reference_layout_bytes(o, sets, stride: int = 16):
+    """B_ref: the bytes per ray that the reference's own layout fetches for the
+    same rays -- one 32-B BVHArrayNode per node visit and, per leaf visit,
+    three 12-B vertices plus the 12-B index triple -- with the ray read and
+    the 20-B RayHit write, counted by the oracle's BVHAccel walk
+    (bvhaccel.cpp:170-260; `o` an OracleScene) over every `stride`-th ray of
+    each set."""
+    out = {}
+    for name, rays in sets:
+        nodes, leaves = o.visit_stats(np.ascontiguousarray(rays[::stride]))
+        out[name] = {"nodes_per_ray": round(nodes, 2), "leaves_per_ray": round(leaves, 2),
+                     "bytes_per_ray": round(RAY_BYTES + HIT_BYTES + 32 * nodes + 48 * leaves, 1)}
+    return out
 
 
 def run_reference(args):
@@ -590,10 +605,18 @@ def run_lrx(args):
             threads = os.cpu_count() or 1
             frac = args.ref_fraction
             sample = [primary[::frac], bounce[::frac], shadow[::frac]]
-            n_s, secs = cpu_measure(scene_desc, sample, threads)
+            n_s, secs, oracle_scene = cpu_measure(scene_desc, sample, threads)
             cpu = {"value": round(n_s / secs / 1e6, 3), "unit": UNIT, "cores": threads, "kind": "port",
                    "sample": f"every {frac}th ray of each of the 3 sets ({n_s} rays), oracle BVHAccel::Intersect "
                              f"restatement, classic-builder BVH, {threads} threads"}
+            # the reference layout's bytes per ray on the same rays, beside this
+            # build's (roofline.bytes_per_ray): a worse tree cannot raise the
+            # roofline fraction unnoticed
+            bref = reference_layout_bytes(oracle_scene, [(nm, r) for nm, r, _m in sets])
+            step_bref = sum(bref[nm]["bytes_per_ray"] * r.shape[0] for nm, r, _m in sets) / rays_per_step
+            cpu["b_ref"] = {"per_set": bref, "step_bytes_per_ray": round(step_bref, 1),
+                            "sample": "every 16th ray of each set, oracle BVHAccel walk (classic builder, 4-ary)",
+                            "formula": "48 + 20 + 32 x node visits + (3 x 12 + 12) x leaf visits"}
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(elapsed_ms / args.steps, 4), "higher_is_better": True,
@@ -736,7 +759,7 @@ def run_instanced(args, motion: bool = False):
         threads = os.cpu_count() or 1
         frac = args.ref_fraction * 64
         sample = [closest[::frac], anyr[::frac]]
-        n_s, secs = cpu_measure(scene_desc, sample, threads, accel="mbvh")
+        n_s, secs, _o = cpu_measure(scene_desc, sample, threads, accel="mbvh")
         cpu = {"value": round(n_s / secs / 1e6, 3), "unit": UNIT, "cores": threads, "kind": "port",
                "sample": f"every {frac}th ray of both sets ({n_s} rays), oracle MBVHAccel::Intersect restatement "
                          f"(closest hit for both), {threads} threads"}
