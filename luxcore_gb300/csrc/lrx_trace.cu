@@ -902,38 +902,54 @@ lrx_status launch_restore_masked_hits(const void *d_rays, uint32_t n, const void
 	return LRX_OK;
 }
 
+// Blocks of one kernel and block size resident on a device at once, per
+// device, computed on first use.  Threads that race on a first use compute
+// the same value; the relaxed atomics keep the cache free of data races.
+constexpr int kMaxCachedDevices = 64;
+struct ResidentCache {
+	std::atomic<int> blocks[kMaxCachedDevices];
+};
+
+static lrx_status resident_blocks(ResidentCache &c, const void *fn, int block, size_t smem, int *out) {
+	int dev = 0;
+	LRX_CUDA(cudaGetDevice(&dev));
+	const bool cached = dev >= 0 && dev < kMaxCachedDevices;
+	if (cached) {
+		const int v = c.blocks[dev].load(std::memory_order_relaxed);
+		if (v > 0) {
+			*out = v;
+			return LRX_OK;
+		}
+	}
+	int sms = 0, per_sm = 0;
+	LRX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+	LRX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, block, smem));
+	const int v = std::max(1, sms * std::max(1, per_sm));
+	if (cached) c.blocks[dev].store(v, std::memory_order_relaxed);
+	*out = v;
+	return LRX_OK;
+}
+
 lrx_status launch_trace_queue(const QueueParams &p, cudaStream_t st) {
 	if (p.total_tiles == 0) return LRX_OK;
-	static int resident = 0;  // 64-thread blocks resident per GB300 at this kernel's occupancy
-	if (resident == 0) {
-		int dev = 0, sms = 0, per_sm = 0;
-		LRX_CUDA(cudaGetDevice(&dev));
-		LRX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-		LRX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_trace_queue<0u>, kTileRays, 0));
-		resident = std::max(1, sms * std::max(1, per_sm));
-	}
 	if (p.fetch) {
 		// 128-thread blocks resident per device, by [flags][two-level]
-		static int fetch_resident[2][2] = {{0, 0}, {0, 0}};
+		static ResidentCache fetch_cache[2][2];
 		const int fl = p.done_flags ? 1 : 0;
 		const int two = (p.class_batch[1] != p.class_batch[2] || p.class_batch[3] != p.class_batch[4]) ? 1 : 0;
-		if (fetch_resident[fl][two] == 0) {
-			int dev = 0, sms = 0, per_sm = 0;
-			LRX_CUDA(cudaGetDevice(&dev));
-			LRX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-			const void *fn = fl ? (two ? (const void *)k_trace_queue_fetch<0u, true, true>
-									 : (const void *)k_trace_queue_fetch<0u, true, false>)
-							: (two ? (const void *)k_trace_queue_fetch<0u, false, true>
-								   : (const void *)k_trace_queue_fetch<0u, false, false>);
-			LRX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kTraceBlock, 0));
-			fetch_resident[fl][two] = std::max(1, sms * std::max(1, per_sm));
-		}
+		const void *fn = fl ? (two ? (const void *)k_trace_queue_fetch<0u, true, true>
+								 : (const void *)k_trace_queue_fetch<0u, true, false>)
+						: (two ? (const void *)k_trace_queue_fetch<0u, false, true>
+							   : (const void *)k_trace_queue_fetch<0u, false, false>);
+		int resident = 0;
+		lrx_status rc = resident_blocks(fetch_cache[fl][two], fn, kTraceBlock, 0, &resident);
+		if (rc != LRX_OK) return rc;
 		if (p.total_rays == 0 || p.refill < 1 || p.refill > 32) {
 			set_error("queue fetch launch: empty or bad refill");
 			return LRX_ERR_INVALID_ARGUMENT;
 		}
 		const uint32_t grid = (uint32_t)std::min<uint64_t>(((uint64_t)p.total_rays + kTraceBlock - 1) / kTraceBlock,
-				(uint64_t)fetch_resident[fl][two]);
+				(uint64_t)resident);
 		if (fl) {
 			if (two) k_trace_queue_fetch<0u, true, true><<<grid, kTraceBlock, 0, st>>>(p);
 			else k_trace_queue_fetch<0u, true, false><<<grid, kTraceBlock, 0, st>>>(p);
@@ -944,6 +960,10 @@ lrx_status launch_trace_queue(const QueueParams &p, cudaStream_t st) {
 		LRX_CUDA(cudaGetLastError());
 		return LRX_OK;
 	}
+	static ResidentCache tile_cache;  // 64-thread blocks of the tile kernel
+	int resident = 0;
+	lrx_status rc = resident_blocks(tile_cache, (const void *)k_trace_queue<0u>, kTileRays, 0, &resident);
+	if (rc != LRX_OK) return rc;
 	const uint32_t grid = std::min<uint32_t>(p.total_tiles, (uint32_t)resident);
 	k_trace_queue<0u><<<grid, kTileRays, 0, st>>>(p);
 	LRX_CUDA(cudaGetLastError());
@@ -955,19 +975,12 @@ lrx_status launch_trace_queue(const QueueParams &p, cudaStream_t st) {
 template <bool ANY, bool TWO_LEVEL, uint32_t CV>
 static lrx_status launch_fetch(const TraceArgs &a, uint32_t bs, cudaStream_t st) {
 	const size_t smem_bytes = (CV & kVarSmemStack) ? sizeof(uint2) * kSmemStack * bs : 0;
-	static int resident[kTraceBlock / 32] = {0};  // blocks per SM for bs = 32, 64, 96, 128
-	static int sms = 0;
-	int &per_sm = resident[bs / 32 - 1];
-	if (per_sm == 0 || sms == 0) {
-		int dev = 0, n = 0, r = 0;
-		LRX_CUDA(cudaGetDevice(&dev));
-		LRX_CUDA(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev));
-		LRX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, k_trace_fetch<ANY, TWO_LEVEL, CV>, (int)bs,
-				smem_bytes));
-		sms = n;
-		per_sm = std::max(1, r);
-	}
-	const uint32_t grid = (uint32_t)std::min<uint64_t>(((uint64_t)a.count + bs - 1) / bs, (uint64_t)sms * per_sm);
+	static ResidentCache cache[kTraceBlock / 32];  // by block size 32, 64, 96, 128
+	int resident = 0;
+	const lrx_status rc = resident_blocks(cache[bs / 32 - 1], (const void *)k_trace_fetch<ANY, TWO_LEVEL, CV>, (int)bs,
+			smem_bytes, &resident);
+	if (rc != LRX_OK) return rc;
+	const uint32_t grid = (uint32_t)std::min<uint64_t>(((uint64_t)a.count + bs - 1) / bs, (uint64_t)resident);
 	const uint32_t refill = a.refill == 0 ? 16u : std::min(32u, a.refill);
 	k_trace_fetch<ANY, TWO_LEVEL, CV><<<grid, bs, smem_bytes, st>>>(a, next_queue_slot(), refill);
 	LRX_CUDA(cudaGetLastError());
