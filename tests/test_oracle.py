@@ -168,3 +168,18 @@ def test_morton_expand_matches_bit_loop():
         v = int(v)
         slow = sum(((v >> b) & 1) << (3 * b) for b in range(21))
         assert expand(v) == slow
+
+
+def test_reference_layout_bytes_per_ray():
+    """bench.py's B_ref: the reference layout's bytes per ray from the
+    oracle's BVHAccel walk counts (32 B per node visit, 48 B per leaf visit,
+    68 B of ray and hit)."""
+    import bench
+    desc = W.SceneDesc([W.heightfield_mesh(65, 7)])
+    o = po.OracleScene(desc, po.ACCEL_BVH)
+    rays = W.pinhole_rays(32, 32)
+    got = bench.reference_layout_bytes(o, [("primary", rays)], stride=1)["primary"]
+    nodes, leaves = o.visit_stats(rays)
+    assert leaves > 0 and nodes >= leaves
+    assert got["bytes_per_ray"] == round(48 + 20 + 32 * nodes + 48 * leaves, 1)
+    assert got["nodes_per_ray"] == round(nodes, 2) and got["leaves_per_ray"] == round(leaves, 2)
