@@ -382,20 +382,35 @@ lrx_status lrx_trace_host_batches(const lrx_host_batch *batches, uint32_t n_batc
 				auto stages = [&]() -> lrx_status {
 					void *d_rays = nullptr, *d_hits = nullptr;
 					LRX_CUDA(cudaMallocFromPoolAsync(&d_rays, rb, pool, s_in));
-					LRX_CUDA(cudaMallocFromPoolAsync(&d_hits, hb, pool, s_in));
-					LRX_CUDA(cudaMemcpyAsync(d_rays, hr, rb, cudaMemcpyHostToDevice, s_in));
-					if (!mapped) LRX_CUDA(cudaMemcpyAsync(d_hits, hh, hb, cudaMemcpyHostToDevice, s_in));
-					LRX_CUDA(cudaEventRecord(in_done, s_in));
-					LRX_CUDA(cudaStreamWaitEvent(s_tr, in_done, 0));
-					lrx_status r = trace_common(b.scene, d_rays, d_hits, n, b.mode, nullptr, s_tr);
-					if (r == LRX_OK && mapped)
-						r = launch_restore_masked_hits(d_rays, n, static_cast<const lrx_hit *>(mapped_hits) + c0, d_hits,
-								s_tr);
-					LRX_CUDA(cudaEventRecord(tr_done, s_tr));
-					LRX_CUDA(cudaStreamWaitEvent(s_out, tr_done, 0));
-					if (r == LRX_OK) LRX_CUDA(cudaMemcpyAsync(hh, d_hits, hb, cudaMemcpyDeviceToHost, s_out));
-					cudaFreeAsync(d_rays, s_out);
-					cudaFreeAsync(d_hits, s_out);
+					const cudaError_t ea = cudaMallocFromPoolAsync(&d_hits, hb, pool, s_in);
+					if (ea != cudaSuccess) {
+						cudaFreeAsync(d_rays, s_in);
+						return cuda_fail(ea, "cudaMallocFromPoolAsync");
+					}
+					bool ordered = false;  // the copy-out stream waits for the chunk's trace
+					const lrx_status r = [&]() -> lrx_status {
+						LRX_CUDA(cudaMemcpyAsync(d_rays, hr, rb, cudaMemcpyHostToDevice, s_in));
+						if (!mapped) LRX_CUDA(cudaMemcpyAsync(d_hits, hh, hb, cudaMemcpyHostToDevice, s_in));
+						LRX_CUDA(cudaEventRecord(in_done, s_in));
+						LRX_CUDA(cudaStreamWaitEvent(s_tr, in_done, 0));
+						lrx_status t = trace_common(b.scene, d_rays, d_hits, n, b.mode, nullptr, s_tr);
+						if (t == LRX_OK && mapped)
+							t = launch_restore_masked_hits(d_rays, n, static_cast<const lrx_hit *>(mapped_hits) + c0,
+									d_hits, s_tr);
+						LRX_CUDA(cudaEventRecord(tr_done, s_tr));
+						LRX_CUDA(cudaStreamWaitEvent(s_out, tr_done, 0));
+						ordered = true;
+						if (t == LRX_OK) LRX_CUDA(cudaMemcpyAsync(hh, d_hits, hb, cudaMemcpyDeviceToHost, s_out));
+						return t;
+					}();
+					if (!ordered) {
+						// a stage failed before the copy-out stream was ordered after
+						// the chunk's work: wait for that work before the buffers go
+						cudaStreamSynchronize(s_tr);
+						cudaStreamSynchronize(s_in);
+					}
+					cudaFreeAsync(d_rays, ordered ? s_out : s_in);
+					cudaFreeAsync(d_hits, ordered ? s_out : s_in);
 					return r;
 				};
 				const lrx_status r = stages();
