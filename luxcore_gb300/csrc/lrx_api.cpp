@@ -405,6 +405,11 @@ lrx_status lrx_scene_create_motion(const lrx_mesh_desc *meshes, uint32_t mesh_co
 			return LRX_ERR_INVALID_ARGUMENT;
 		}
 		*out_scene = nullptr;
+		if (opts && opts->struct_size >= sizeof(lrx_build_opts) && opts->node_width &&
+				(opts->node_width < 4 || opts->node_width > 8)) {
+			set_error("lrx_scene_create: node_width must be 0 or in [4, 8]");
+			return LRX_ERR_INVALID_ARGUMENT;
+		}
 		int dev = 0;
 		LRX_CUDA(cudaGetDevice(&dev));
 		cudaDeviceProp prop;

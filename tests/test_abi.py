@@ -68,6 +68,15 @@ def test_null_arguments_are_rejected_without_a_device(lib):
     del h
 
 
+def test_bad_node_width_is_rejected_without_a_device(lib):
+    # build options are checked before any CUDA call too
+    h = ctypes.c_void_p()
+    for w in (1, 3, 9, 64):
+        opts = lrx.BuildOpts(ctypes.sizeof(lrx.BuildOpts), 3, 2, w)
+        assert lib.lrx_scene_create(None, 0, None, 0, ctypes.byref(opts), None, ctypes.byref(h)) == 1
+        assert b"node_width" in lib.lrx_last_error()
+
+
 def test_package_has_no_cpu_fallback():
     # the product path must not import the oracle
     for dirpath, _, files in os.walk(os.path.join(ROOT, "luxcore_gb300")):
