@@ -170,24 +170,14 @@ def load_peaks():
     return 6800.0, "fallback"
 
 
-def load_traffic_per_ray():
-    """DRAM bytes per ray of each ray set's traversal launch, from the
-    committed ncu summary (profiles/trace_heightfield_ncu.md, lines
-    `dram_bytes_per_ray_<set>: <bytes>`)."""
-    p = os.path.join(ROOT, "profiles", "trace_heightfield_ncu.md")
-    out = {}
-    if not os.path.exists(p):
-        return out
-    with open(p) as f:
-        for ln in f:
-            ln = ln.strip().strip("`")
-            if ln.startswith("dram_bytes_per_ray_"):
-                key, _, val = ln.partition(":")
-                try:
-                    out[key[len("dram_bytes_per_ray_"):]] = float(val.split()[0])
-                except (ValueError, IndexError):
-                    pass
-    return out
+# DRAM bytes per ray of each ray set's traversal launch, from one ncu
+# capture of this workload (dram__bytes_read.sum + dram__bytes_write.sum over
+# the rays of the launch; the capture's command and table are in
+# profiles/trace_heightfield_ncu.md).  A constant of that capture, not a
+# figure of this run: the line says so in roofline.traffic_source.
+TRAFFIC_PER_RAY = {"primary": 153.4, "bounce": 296.7, "shadow": 197.3}
+TRAFFIC_SOURCE = ("ncu capture of the traversal launches of one step (profiles/trace_heightfield_ncu.md), "
+                  "not this run; DRAM bytes per launch averaged over the three sets")
 
 
 def count_kernel_launches(stream_handle, fn):
@@ -232,17 +222,44 @@ def count_kernel_launches(stream_handle, fn):
 # CPU arm (the reference's CPU accelerator, restated)
 # ---------------------------------------------------------------------------
 
-def cpu_measure(scene, sets, threads: int, accel: str = "bvh"):
+def cpu_measure(scene, sets, threads: int, accel: str = "bvh", keep_hits: bool = False):
     """Times the oracle's BVHAccel::Intersect (or MBVHAccel::Intersect for
-    instanced scenes) over the given ray sets."""
+    instanced scenes) over the given ray sets; with keep_hits, also returns
+    the oracle's hits per set (for the parity check of the GPU's)."""
     from oracle import pyoracle as po
     o = po.OracleScene(scene, po.ACCEL_MBVH if accel == "mbvh" else po.ACCEL_BVH)
-    total, secs = 0, 0.0
+    total, secs, hits = 0, 0.0, []
     for rays in sets:
-        _, s = o.intersect(rays, n_threads=threads)
+        h, s = o.intersect(rays, n_threads=threads)
         secs += s
         total += rays.shape[0]
+        if keep_hits:
+            hits.append(h)
+    if keep_hits:
+        return total, secs, o, hits
     return total, secs, o
+
+
+def parity_block(oracle_scene, sets, gpu_hits, ref_hits, stride: int):
+    """The GPU hits of the timed step against the oracle's on the CPU
+    sample (every `stride`-th ray of each set): closest-hit sets by
+    oracle.parity.compare, any-hit sets by oracle.parity.check_anyhit."""
+    from oracle.parity import check_anyhit, compare
+    out, ok = {}, True
+    for (name, rays, mode), g, r in zip(sets, gpu_hits, ref_hits):
+        g = np.ascontiguousarray(g[::stride])
+        rs = np.ascontiguousarray(rays[::stride])
+        if mode == 0:
+            c = compare(g, r, oracle_scene, rs)
+            out[name] = {k: c[k] for k in ("n", "agree", "ties", "bad_disagreements", "bitexact_t", "values_ok",
+                                           "ties_valid", "ok")}
+        else:
+            c = check_anyhit(g, r, oracle_scene, rs)
+            out[name] = {"n": c["n"], "hitmiss_agree": c["hitmiss_agree"], "valid": c["valid"], "ok": c["ok"]}
+        ok = ok and out[name]["ok"]
+    out["ok"] = bool(ok)
+    out["sample"] = f"every {stride}th ray of each set, GPU hits of the last timed step"
+    return out
 
 
 def reference_layout_bytes(o, sets, stride: int = 16):
@@ -412,6 +429,8 @@ def run_lrx(args):
     log(f"[bench] {time.strftime('%H:%M:%S')} timed region done")
     if scene.device_status(st) != 0:
         raise RuntimeError("device status word set during the timed steps")
+    # the last timed step's hits, for the parity check on the CPU sample
+    step_hits = [dh.cpu().numpy().view(W.HIT_DTYPE).copy() for _nm, _dr, dh, _n, _m in dev] if rank == 0 else None
     d.barrier()
     elapsed_ms = start.elapsed_time(end)
     elapsed_ms = d.max(elapsed_ms)
@@ -553,10 +572,8 @@ def run_lrx(args):
                       "nodes_tris_per_ray": [round(bn / nb, 2), round(bt / nb, 2)],
                       "frac": round(nb * bpr / (ms8 / 1e3) / 1e9 / peak, 4)}
         del d_b8, d_h8
-    tpr = load_traffic_per_ray()
-    traffic = None
-    if all(name in tpr for name, *_r in dev):  # DRAM bytes per trace launch, averaged over the sets
-        traffic = round(sum(tpr[name] * n for name, _dr, _dh, n, _m in dev) / len(dev))
+    # DRAM bytes per trace launch, averaged over the sets
+    traffic = round(sum(TRAFFIC_PER_RAY[name] * n for name, _dr, _dh, n, _m in dev) / len(dev))
 
     # end to end: host rays in pinned memory -> lrx_trace_host -> host hits
     e2e_value = None
@@ -601,14 +618,16 @@ def run_lrx(args):
     line = None
     if rank == 0:
         cpu = None
+        parity = None
         if not args.no_cpu_baseline:
             threads = os.cpu_count() or 1
             frac = args.ref_fraction
             sample = [primary[::frac], bounce[::frac], shadow[::frac]]
-            n_s, secs, oracle_scene = cpu_measure(scene_desc, sample, threads)
+            n_s, secs, oracle_scene, ref_hits = cpu_measure(scene_desc, sample, threads, keep_hits=True)
             cpu = {"value": round(n_s / secs / 1e6, 3), "unit": UNIT, "cores": threads, "kind": "port",
                    "sample": f"every {frac}th ray of each of the 3 sets ({n_s} rays), oracle BVHAccel::Intersect "
                              f"restatement, classic-builder BVH, {threads} threads"}
+            parity = parity_block(oracle_scene, sets, step_hits, ref_hits, frac)
             # the reference layout's bytes per ray on the same rays, beside this
             # build's (roofline.bytes_per_ray): a worse tree cannot raise the
             # roofline fraction unnoticed
@@ -640,12 +659,13 @@ def run_lrx(args):
                 "treelet_passes": args.treelet_passes,
             },
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                         "frac": round(achieved / peak, 4), "traffic": traffic,
+                         "frac": round(achieved / peak, 4), "traffic": traffic, "traffic_source": TRAFFIC_SOURCE,
                          "peak_kind": peak_kind, "scope": "the timed step (algorithmic bytes / step time)",
                          "per_launch_frac": per_launch_frac,
                          "bounce_8M_launch": big_bounce,
                          "bytes_per_ray": round(tot_alg / rays_per_step, 1)},
             "cpu_baseline": cpu,
+            "parity": parity,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
                     "api": ("lrx_trace_host_batches over the 3 sets (pinned host buffers)" if args.step_form == "batched"

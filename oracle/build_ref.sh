@@ -4,12 +4,15 @@
 # oracle/_ref/.
 # Test infrastructure only: the result pins the oracle (tests/golden/).
 # Usage: oracle/build_ref.sh [path to the LuxCore source tree]
+# The tree is the argument, else $LUXCORE_REFERENCE_TREE, else the copy this
+# project was developed beside.  Exits 3 (nothing built) when it is absent,
+# as on a machine that has only this repository.
 set -e
-REF="${1:-/root/reference}"
+REF="${1:-${LUXCORE_REFERENCE_TREE:-/root/reference}}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 if [ ! -f "$REF/include/luxrays/accelerators/bvh.cl" ]; then
 	echo "reference tree not found at $REF" >&2
-	exit 1
+	exit 3
 fi
 mkdir -p "$HERE/_ref"
 # bvh.cl (BVHKernel) and mbvh.cl (MBVHKernel with transforms and motion systems)
