@@ -24,7 +24,7 @@
 extern "C" {
 #endif
 
-#define LRX_ABI_VERSION 2u
+#define LRX_ABI_VERSION 3u
 #define LRX_NULL_INDEX 0xffffffffu      /* luxrays_types.cl:21 */
 #define LRX_RAY_FLAGS_MASKED 0x1u       /* ray_types.cl:22 */
 
@@ -221,6 +221,17 @@ typedef struct lrx_trace_config {
 	uint32_t refill;          /* with LRX_VARIANT_PERSISTENT: idle lanes of a warp that trigger
 	                             its next ray claim, 1-32 (0 = 16).  Added in ABI 2: a caller
 	                             passing the 20-byte ABI 1 struct gets 0 */
+	/* Failure bounds (added in ABI 3; a caller passing an older, shorter
+	 * struct gets 0 for both).  A ray that reaches either is abandoned: its
+	 * hit is not written and the scene's status word records why
+	 * (lrx_scene_device_status). */
+	uint32_t max_visits;      /* node visits per ray.  0 = the scene's own bound, which no
+	                             valid tree reaches: the node count of its top-level tree
+	                             (the whole BVH of a flat scene), plus the node count of the
+	                             largest instanced BVH at each instance entry */
+	uint32_t deadline_us;     /* launch deadline in microseconds, from the launch's first
+	                             block: rays not yet started when it has passed are abandoned.
+	                             0 = 10 s plus 0.1 us per ray of the launch */
 } lrx_trace_config;
 #define LRX_VARIANT_MINMAX3 0x1u       /* 3-input min/max in the slab tests */
 #define LRX_VARIANT_SCENE_L2_KEEP 0x2u /* node/triangle loads marked evict-last in L2 */
@@ -378,20 +389,26 @@ lrx_status lrx_server_reset_stats(lrx_server *server);
  * Another is an application that owns all device memory through its own
  * fixed pool or budget and allows no allocation outside it.
  *
- * Instead of allocating, the rays and hits are staged through one array that
- * the library reserves statically on every GPU that loads it: room for
- * LRX_NOALLOC_MAX_RAYS rays and hits (8.5 MiB), held until the process exits.
- * A batch larger than that is rejected with LRX_ERR_INVALID_ARGUMENT.
- * Results are the same as lrx_trace_host's for the same scene and rays.
+ * Instead of allocating, the rays, the hits and the launch's scratch (the ray
+ * sort's keys, indices and temporary storage for any-hit batches of 32,768
+ * rays or more, or the index list of a compacting configuration) live in one
+ * array that the library reserves statically on every GPU that loads it:
+ * room for LRX_NOALLOC_MAX_RAYS rays and hits plus 4 MiB of scratch
+ * (12.5 MiB), held until the process exits.  A batch larger than
+ * LRX_NOALLOC_MAX_RAYS is rejected with LRX_ERR_INVALID_ARGUMENT.  The scene's
+ * launch configuration for the mode applies unchanged, so results are the
+ * same as lrx_trace_host's for the same scene and rays.
  *
  * The first call on a device looks up the array's device address (one
  * cudaGetSymbolAddress, with that device current); make that first call
  * before any stream capture.  Every call on a device shares the array and it
- * keeps the last call's contents; nothing in it needs to start at zero,
- * because each call copies its rays and the caller's hit buffer in before
- * the kernel runs.  Calls whose GPU work overlapped would race on the array,
- * so the library serialises these calls per device and each one
- * synchronises `stream` before it returns. */
+ * keeps the last call's contents; nothing in it needs to start at zero:
+ * each call copies its rays and the caller's hit buffer in before the kernel
+ * runs, the sort writes its keys and indices before reading them, and the
+ * sort's temporary storage is initialised by the sort itself.  Calls whose
+ * GPU work overlapped would race on the array, so the library serialises
+ * these calls per device, and each one synchronises `stream` before it
+ * returns, on success and on failure alike. */
 lrx_status lrx_trace_host_noalloc(lrx_scene *scene, const lrx_ray *h_rays, lrx_hit *h_hits,
 		uint32_t count, uint32_t mode, void *stream);
 
@@ -402,7 +419,10 @@ lrx_status lrx_trace_counted(lrx_scene *scene, const void *d_rays, void *d_hits,
 		uint32_t count, uint32_t mode, uint64_t *d_counters, void *stream);
 
 /* Synchronises `stream` and returns (then clears) the scene's device status
- * word: 0 = no fault; bit 0 = traversal stack limit; bit 1 = visit limit. */
+ * word: 0 = no fault; bit 0 = traversal stack limit; bit 1 = visit limit;
+ * bit 2 = launch deadline.  Each bit means some rays of some launch since the
+ * last call were abandoned, their hits not written; the call then returns
+ * LRX_ERR_DEVICE. */
 lrx_status lrx_scene_device_status(lrx_scene *scene, uint32_t *status, void *stream);
 
 /* ---- Scene ingestion and the BVH blob cache ---------------------------- */

@@ -694,15 +694,33 @@ lrx_status lrx_scene_get_info(const lrx_scene *s, lrx_scene_info *info) {
 }
 
 
-// A correct walk visits each node at most once per BLAS entry, so a ray never
-// needs more than (instances + 1) x nodes visits.
+// A correct walk expands each node of a tree at most once per entry into
+// that tree.  A ray's visit count rises by one per expansion and each
+// instance entry takes B (the largest BLAS's node count + 64) off it,
+// stopping at zero.  Right after the last point where it stood at zero (or
+// the start), the count has since grown by at most one BLAS walk (< B) plus
+// TLAS expansions, while every later entry takes off more than its walk
+// adds; so a valid walk never passes T + B, T the node count of the
+// top-level tree (the whole BVH of a flat scene, where B = 0) + 64.
 extern "C++" uint32_t lrx::scene_visit_limit(const lrx_scene *s) {
-	const uint64_t lim = (uint64_t)(s->info.instance_count + 1) * (s->info.node_count + 1) + 64;
-	return (uint32_t)std::min<uint64_t>(lim, kMaxVisits);
+	const uint64_t top = s->two_level ? s->info.node_count - s->blas_node_total : s->info.node_count;
+	return (uint32_t)std::min<uint64_t>(top + 64 + scene_blas_visits(s), 0x7fffffffull);
+}
+
+extern "C++" uint32_t lrx::scene_blas_visits(const lrx_scene *s) {
+	if (!s->two_level) return 0;
+	std::vector<uint32_t> roots;  // BLAS node ranges are contiguous, in root order
+	for (const Blas &b : s->blas)
+		if (b.root != kNull) roots.push_back(b.root);
+	std::sort(roots.begin(), roots.end());
+	roots.push_back(s->blas_node_total);
+	uint64_t widest = 0;
+	for (size_t k = 0; k + 1 < roots.size(); ++k) widest = std::max<uint64_t>(widest, roots[k + 1] - roots[k]);
+	return (uint32_t)std::min<uint64_t>(widest + 64, 1ull << 30);
 }
 
 extern "C++" lrx_status lrx::trace_common(lrx_scene *s, const void *d_rays, void *d_hits, uint32_t count, uint32_t mode,
-		uint64_t *d_counters, cudaStream_t st) {
+		uint64_t *d_counters, cudaStream_t st, const FixedScratch *fixed) {
 	if (!s) {
 		set_error("lrx_trace: null scene");
 		return LRX_ERR_INVALID_ARGUMENT;
@@ -734,16 +752,18 @@ extern "C++" lrx_status lrx::trace_common(lrx_scene *s, const void *d_rays, void
 	a.any_hit = mode == LRX_TRACE_ANY;
 	a.status = s->status.as<uint32_t>();
 	a.counters = reinterpret_cast<unsigned long long *>(d_counters);
-	a.visit_limit = scene_visit_limit(s);
 	const lrx_trace_config &cfg = s->tcfg[mode == LRX_TRACE_ANY ? 1 : 0];
+	a.visit_limit = cfg.max_visits ? cfg.max_visits : scene_visit_limit(s);
+	a.blas_visits = cfg.max_visits ? 0u : scene_blas_visits(s);
+	a.deadline_ticks = deadline_ticks(cfg.deadline_us, count);
 	a.block_size = cfg.block_size;
 	a.postpone = cfg.postpone;
 	a.variant = cfg.variant;
 	a.refill = cfg.refill;
 	if ((a.variant & kVarSortRays) && count >= kSortMinRays && s->root != kNull)
-		return launch_trace_sorted(a, s->bounds_lo, s->bounds_hi, st);
-	if ((a.variant & kVarCompact) && (a.variant & kVarPersistent) && !d_counters && count < 0x80000000u)
-		return launch_trace_compacted(a, st);
+		return launch_trace_sorted(a, s->bounds_lo, s->bounds_hi, st, fixed);
+	if ((a.variant & kVarCompact) && (a.variant & kVarPersistent) && !d_counters && count <= kMaxFetchRays)
+		return launch_trace_compacted(a, st, fixed);
 	return launch_trace(a, st);
 }
 
@@ -813,7 +833,7 @@ lrx_status lrx_scene_autotune(lrx_scene *s, const void *d_rays, uint32_t count, 
 			for (uint32_t var : kVariants) {
 				if ((var & LRX_VARIANT_SORT_RAYS) && count < kSortMinRays) continue;
 				s->tcfg[m] = lrx_trace_config{sizeof(lrx_trace_config), bs, pp, var, 1u << m,
-							(var & LRX_VARIANT_PERSISTENT) ? 8u : 0u};
+							(var & LRX_VARIANT_PERSISTENT) ? 8u : 0u, best.max_visits, best.deadline_us};
 				if ((rc = trace_common(s, d_rays, hits, count, mode, nullptr, st)) != LRX_OK) break;
 				cudaEventRecord(e0, st);
 				for (int r = 0; r < 3 && rc == LRX_OK; ++r) rc = trace_common(s, d_rays, hits, count, mode, nullptr, st);
@@ -835,8 +855,8 @@ lrx_status lrx_scene_autotune(lrx_scene *s, const void *d_rays, uint32_t count, 
 	cudaEventDestroy(e1);
 	if (rc != LRX_OK) return rc;
 	if (chosen) {  // as many bytes as the caller's struct holds (ABI 1 struct: no refill field)
-		const size_t n = chosen->struct_size >= sizeof(lrx_trace_config) ? sizeof(lrx_trace_config)
-				: offsetof(lrx_trace_config, refill);
+		const size_t n = std::max<size_t>(offsetof(lrx_trace_config, refill),
+				std::min<size_t>(chosen->struct_size, sizeof(lrx_trace_config)));
 		std::memcpy(chosen, &best, n);
 		chosen->struct_size = (uint32_t)n;
 	}

@@ -47,7 +47,7 @@ struct Hash64 {
 };
 
 constexpr char kBlobMagic[8] = {'L', 'R', 'X', 'S', 'C', 'E', 'N', 'E'};
-constexpr uint32_t kBlobVersion = 2;
+constexpr uint32_t kBlobVersion = 3;  // 3: the trace configs carry the failure bounds
 
 struct BlobWriter {
 	unsigned char *p;  // null: only count

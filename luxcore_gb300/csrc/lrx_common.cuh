@@ -25,7 +25,7 @@ constexpr uint32_t kInternalMetaBase = 0x38u;  // meta byte of internal slot s: 
 // Status word bits (lrx_scene_device_status)
 constexpr uint32_t kStatusStackOverflow = 1u;
 constexpr uint32_t kStatusVisitLimit = 2u;
-constexpr uint32_t kMaxVisits = 1u << 24;
+constexpr uint32_t kStatusDeadline = 4u;
 
 // Node words:
 //   w[0] = (px, py, pz, ex | ey << 8 | ez << 16 | imask << 24)

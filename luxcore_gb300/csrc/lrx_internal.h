@@ -2,6 +2,7 @@
 // traversal launchers.  Not part of the public ABI.
 #pragma once
 
+#include <algorithm>
 #include <cstdint>
 #include <mutex>
 #include <string>
@@ -110,7 +111,21 @@ struct TraceArgs {
 	uint32_t block_size = 0;       // threads per block (0 = kTraceBlock)
 	uint32_t postpone = 0;         // min lanes testing triangles before deferring (0 = never)
 	uint32_t variant = 0;          // lrx_trace_config.variant bits
-	uint32_t visit_limit = 1u << 24;  // node visits after which a ray is abandoned (status bit 1)
+	// Node-visit budget of a ray: visit_limit at its start, plus blas_visits
+	// at every instance entry; a ray that exhausts it is abandoned (status
+	// bit 1, hit not written).  The scene's own bound -- its top-level tree's
+	// node count, plus the largest BLAS's at each entry -- is never reached
+	// by a valid tree, since a walk expands each node of a tree at most once
+	// per entry into that tree.
+	uint32_t visit_limit = 1u << 24;
+	uint32_t blas_visits = 0;
+	// Launch deadline in %globaltimer ticks of 1,024 ns (0 = none), from the
+	// start of each persistent warp or of each block of the one-ray-per-thread
+	// kernel: once it has passed, rays not yet started are abandoned (status
+	// bit 2, hits not written).  launch_id picks the persistent kernels'
+	// counter slot (next_launch_id).
+	uint32_t deadline_ticks = 0;
+	uint32_t launch_id = 0;
 	const uint32_t *order = nullptr;  // thread i traces ray order[i] (sorted launches)
 	uint32_t refill = 0;           // persistent fetch: idle lanes that trigger a warp's claim (0 = 16)
 	const uint32_t *count_dev = nullptr;  // persistent fetch: rays to claim, read on the device (<= count)
@@ -128,9 +143,16 @@ constexpr uint32_t kSortMinRays = 32768;   // smaller batches are traced in call
 
 lrx_status launch_trace(const TraceArgs &a, cudaStream_t stream);
 
-// Counter slot for the next persistent launch (round robin over kQueueSlots;
-// a slot is reused only kQueueSlots launches later).
-uint32_t next_queue_slot();
+// Launch deadline in timer ticks for a launch of `rays` rays under a config
+// deadline of `deadline_us` microseconds (0: 10 s plus 0.1 us per ray).
+inline uint32_t deadline_ticks(uint32_t deadline_us, uint64_t rays) {
+	const uint64_t us = deadline_us ? deadline_us : 10000000ull + rays / 10u;
+	return (uint32_t)std::min<uint64_t>((us * 1000u + 1023u) / 1024u, 0x7fffffffull);
+}
+
+// Id of the next launch: its persistent counter slot is id % kQueueSlots
+// (a slot is reused only kQueueSlots launches later).
+uint32_t next_launch_id();
 
 // One batch of a multi-batch queue launch (kernel parameter space).
 struct QueueBatch {
@@ -143,7 +165,8 @@ struct QueueBatch {
 	uint32_t root, count;
 	uint32_t tile_begin;   // first 64-ray tile of this batch in the launch (tile kernel)
 	uint32_t ray_begin;    // first ray of this batch in the launch's ray index space (fetch kernel)
-	uint32_t flags;        // bit 0 any-hit, bit 1 two-level, bits 8-15 postpone, bits 16-23 variant
+	uint32_t flags;        // bit 0 any-hit, bit 1 two-level, bits 8-15 postpone, bits 16-23 variant,
+	                       // bits 24-28 f: each instance entry adds 2^f node visits to the budget (f = 0: none)
 	uint32_t visit_limit;
 	uint32_t user_index;   // the caller's index of this batch (completion flags)
 	uint32_t order_begin;  // sorted batch: its permutation at QueueParams::order + order_begin; else kNull
@@ -151,13 +174,16 @@ struct QueueBatch {
 constexpr uint32_t kTileRays = 64;
 constexpr uint32_t kMaxQueueBatches = 384;  // keeps the parameter block under 32 KB
 constexpr uint32_t kQueueSlots = 4096;      // concurrent queue launches per device
-constexpr uint32_t kMaxFetchRays = 0x7fffffffu;  // rays per fetch-kernel launch (claims stay below 2^32)
+// Rays per fetch-kernel launch: claims overshoot the count by at most one
+// claim per resident warp (< 2^20 rays), so they stay below 2^31 and bit 31 of
+// a broadcast claim base is free to carry the deadline flag.
+constexpr uint32_t kMaxFetchRays = 0x7f000000u;
 constexpr uint32_t kDirectBatchRays = 131072;  // lrx_trace_batches: batches this large get launches of their own
 constexpr uint32_t kMaxDirectBatches = 4;      // ... when a call holds at most this many of them
 constexpr uint32_t kSideStreams = 6;           // side streams per thread and device
 constexpr uint32_t kHostChunkRays = 1u << 20;  // lrx_trace_host_batches: rays per copy-in/trace/copy-out chunk
 struct QueueParams {
-	uint32_t n, total_tiles, slot;
+	uint32_t n, total_tiles, slot;  // slot = launch_id % kQueueSlots
 	uint32_t fetch;         // 1: warp-level ray fetch (k_trace_queue_fetch), 0: 64-ray tiles per block
 	uint32_t total_rays;    // fetch kernel: rays in the launch (<= kMaxFetchRays)
 	uint32_t refill;        // fetch kernel: idle lanes that trigger a warp's claim, 1-32
@@ -167,7 +193,8 @@ struct QueueParams {
 	// batches are ordered by ray class (0 closest flat, 1 closest two-level, 2 any flat,
 	// 3 any two-level); class c is batches [class_batch[c], class_batch[c + 1])
 	uint32_t class_batch[5];
-	uint32_t pad2;
+	uint32_t deadline_ticks;  // as TraceArgs::deadline_ticks, for the whole launch
+	uint32_t launch_id;
 	QueueBatch b[kMaxQueueBatches];
 };
 static_assert(sizeof(QueueParams) <= 32000, "kernel parameter limit");
@@ -188,15 +215,31 @@ lrx_status launch_restore_masked_hits(const void *d_rays, uint32_t n, const void
 // One launch of the persistent queue kernel over p.n batches.
 lrx_status launch_trace_queue(const QueueParams &p, cudaStream_t stream);
 
+// A device region the caller already owns, lent to one sorted or compacted
+// launch for its scratch in place of the stream-ordered pool (the
+// no-allocation entry point passes its static array).  The launch fails with
+// LRX_ERR_NOT_SUPPORTED if the region is too small; nothing is allocated.
+struct FixedScratch {
+	void *base = nullptr;   // 256-byte aligned
+	size_t bytes = 0;
+};
+// Scratch bytes a sorted launch of n rays needs besides the sort's own
+// temporary storage: keys and indices, double-buffered.
+inline size_t sorted_scratch_arrays(uint32_t n) {
+	return 4 * (((sizeof(uint32_t) * (size_t)n + 255) / 256) * 256);
+}
+
 // Sorts the rays (octant, origin Morton code in [lo, hi]) and traces them in
-// that order; scratch from a stream-ordered pool.  Hits land in caller order.
-lrx_status launch_trace_sorted(const TraceArgs &a, const float lo[3], const float hi[3], cudaStream_t stream);
+// that order; scratch from a stream-ordered pool, or from `fixed` when given.
+// Hits land in caller order.
+lrx_status launch_trace_sorted(const TraceArgs &a, const float lo[3], const float hi[3], cudaStream_t stream,
+		const FixedScratch *fixed = nullptr);
 
 // Compacts the indices of the rays without RAY_FLAGS_MASKED (stable) into
-// pool scratch and traces them with the persistent kernel, which reads the
-// compacted count on the device.  Masked rays are neither read by the
-// traversal nor written.
-lrx_status launch_trace_compacted(const TraceArgs &a, cudaStream_t stream);
+// pool scratch (or `fixed` when given) and traces them with the persistent
+// kernel, which reads the compacted count on the device.  Masked rays are
+// neither read by the traversal nor written.
+lrx_status launch_trace_compacted(const TraceArgs &a, cudaStream_t stream, const FixedScratch *fixed = nullptr);
 
 // One batch of a queue launch to reorder: its rays, count, the scene box and
 // the offset of its permutation in the launch's concatenated order array.

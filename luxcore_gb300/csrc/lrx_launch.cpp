@@ -140,6 +140,7 @@ lrx_status lrx_trace_batches_ex(const lrx_batch *batches, uint32_t n_batches, vo
 	std::vector<Entry> pending;
 	uint64_t pend_tiles = 0, pend_rays = 0, pend_sorted = 0;
 	std::vector<SortBatch> sorted;
+	uint32_t launch_deadline_us = 0;  // the smallest deadline the launch's batches' configs set (0: none set)
 	auto flush = [&]() -> lrx_status {
 		if (pending.empty()) return LRX_OK;
 		std::stable_sort(pending.begin(), pending.end(), [](const Entry &a, const Entry &b) { return a.cls < b.cls; });
@@ -168,9 +169,16 @@ lrx_status lrx_trace_batches_ex(const lrx_batch *batches, uint32_t n_batches, vo
 			q.ray_begin = p.total_rays;
 			// runtime-selectable variants only (cache hints); sorting is done before the launch
 			const uint32_t var = cfg.variant & (LRX_VARIANT_SCENE_L2_KEEP | LRX_VARIANT_STREAM_RAYS);
+			// the visit budget's per-instance-entry part, as a power of two (bits 24-28)
+			uint32_t f = 0;
+			if (!cfg.max_visits)
+				while (f < 31u && (1u << f) < scene_blas_visits(s)) ++f;
+			if (f && !s->two_level) f = 0;
 			q.flags = (b.mode == LRX_TRACE_ANY ? 1u : 0u) | (s->two_level ? 2u : 0u) |
-					((cfg.postpone & 0xffu) << 8) | (var << 16);
-			q.visit_limit = scene_visit_limit(s);
+					((cfg.postpone & 0xffu) << 8) | (var << 16) | (f << 24);
+			q.visit_limit = cfg.max_visits ? cfg.max_visits : scene_visit_limit(s);
+			if (cfg.deadline_us) launch_deadline_us = launch_deadline_us ? std::min(launch_deadline_us, cfg.deadline_us)
+					: cfg.deadline_us;
 			q.user_index = e.k;
 			q.order_begin = kNull;
 			if (e.sort) {
@@ -192,7 +200,10 @@ lrx_status lrx_trace_batches_ex(const lrx_batch *batches, uint32_t n_batches, vo
 		}
 		// a class with no batches starts where the next non-empty one does
 		for (int c = 3; c >= 0; --c) p.class_batch[c] = std::min(p.class_batch[c], p.class_batch[c + 1]);
-		p.slot = next_queue_slot();
+		p.launch_id = next_launch_id();
+		p.slot = p.launch_id % kQueueSlots;
+		p.deadline_ticks = deadline_ticks(launch_deadline_us, fetch ? p.total_rays : (uint64_t)p.total_tiles * kTileRays);
+		launch_deadline_us = 0;
 		void *scratch = nullptr;
 		lrx_status rc = sort_queue_batches(sorted, sorted_rays, st, &p.order, &scratch);
 		if (rc == LRX_OK) rc = launch_trace_queue(p, st);

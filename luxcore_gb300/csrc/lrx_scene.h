@@ -80,12 +80,16 @@ struct lrx_scene {
 
 namespace lrx {
 
-// The node-visit cap of one ray in scene s (a correct walk never reaches it).
+// The node-visit budget of one ray in scene s at its start, and what each
+// instance entry adds to it (a correct walk never spends it).
 uint32_t scene_visit_limit(const lrx_scene *s);
+uint32_t scene_blas_visits(const lrx_scene *s);
 
 // One trace launch of `count` rays with the scene's configuration for `mode`,
 // validating every argument (the body of lrx_trace and lrx_trace_counted).
+// `fixed`, when given, is the scratch of sorted and compacted launches
+// instead of the stream-ordered pool.
 lrx_status trace_common(lrx_scene *s, const void *d_rays, void *d_hits, uint32_t count, uint32_t mode,
-		uint64_t *d_counters, cudaStream_t st);
+		uint64_t *d_counters, cudaStream_t st, const FixedScratch *fixed = nullptr);
 
 }  // namespace lrx

@@ -8,9 +8,11 @@
 // Scratch (keys, indices, sort temp) comes from a library-owned stream-ordered
 // memory pool: allocation and release are ordered on the caller's stream, so
 // concurrent calls on one scene do not share scratch and nothing synchronises
-// the device.
+// the device.  A caller may lend a region of its own instead (FixedScratch),
+// and then nothing is allocated.
 #include <cstdint>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include <cub/device/device_radix_sort.cuh>
@@ -164,45 +166,51 @@ struct RayUnmasked {
 	}
 };
 
-lrx_status launch_trace_compacted(const TraceArgs &a_in, cudaStream_t st) {
+lrx_status launch_trace_compacted(const TraceArgs &a_in, cudaStream_t st, const FixedScratch *fixed) {
 	TraceArgs a = a_in;
 	const uint32_t n = a.count;
-	int dev = 0;
-	LRX_CUDA(cudaGetDevice(&dev));
-	cudaMemPool_t pool;
-	lrx_status rc = stream_pool(dev, &pool);
-	if (rc != LRX_OK) return rc;
 	const RayUnmasked pred{static_cast<const uint32_t *>(a.rays)};
 	thrust::counting_iterator<uint32_t> first(0u);
 	size_t temp_bytes = 0;
 	LRX_CUDA(cub::DeviceSelect::If(nullptr, temp_bytes, first, static_cast<uint32_t *>(nullptr),
 			static_cast<uint32_t *>(nullptr), (int)n, pred, st));
 	const size_t idx_bytes = ((sizeof(uint32_t) * (size_t)n + 255) / 256) * 256;
+	const size_t total = idx_bytes + 256 + temp_bytes;
 	void *base = nullptr;
-	LRX_CUDA(cudaMallocFromPoolAsync(&base, idx_bytes + 256 + temp_bytes, pool, st));
+	if (fixed) {
+		if (total > fixed->bytes) {
+			set_error("ray compaction: " + std::to_string(total) + " scratch bytes needed, " +
+					std::to_string(fixed->bytes) + " lent");
+			return LRX_ERR_NOT_SUPPORTED;
+		}
+		base = fixed->base;
+	} else {
+		int dev = 0;
+		LRX_CUDA(cudaGetDevice(&dev));
+		cudaMemPool_t pool;
+		lrx_status prc = stream_pool(dev, &pool);
+		if (prc != LRX_OK) return prc;
+		LRX_CUDA(cudaMallocFromPoolAsync(&base, total, pool, st));
+	}
 	unsigned char *p = static_cast<unsigned char *>(base);
 	uint32_t *idx = reinterpret_cast<uint32_t *>(p);
 	uint32_t *n_sel = reinterpret_cast<uint32_t *>(p + idx_bytes);
+	lrx_status rc = LRX_OK;
 	cudaError_t e = cub::DeviceSelect::If(p + idx_bytes + 256, temp_bytes, first, idx, n_sel, (int)n, pred, st);
 	if (e == cudaSuccess) {
 		a.order = idx;
 		a.count_dev = n_sel;
 		rc = launch_trace(a, st);
 	}
-	cudaFreeAsync(base, st);  // ordered after the trace on the same stream
+	if (!fixed) cudaFreeAsync(base, st);  // ordered after the trace on the same stream
 	if (e != cudaSuccess) return cuda_fail(e, "ray compaction");
 	return rc;
 }
 
-lrx_status launch_trace_sorted(const TraceArgs &a_in, const float lo[3], const float hi[3], cudaStream_t st) {
+lrx_status launch_trace_sorted(const TraceArgs &a_in, const float lo[3], const float hi[3], cudaStream_t st,
+		const FixedScratch *fixed) {
 	TraceArgs a = a_in;
 	const uint32_t n = a.count;
-	int dev = 0;
-	LRX_CUDA(cudaGetDevice(&dev));
-	if (dev < 0 || dev >= kMaxDevices) return launch_trace(a, st);
-	cudaMemPool_t pool;
-	lrx_status rc = stream_pool(dev, &pool);
-	if (rc != LRX_OK) return rc;
 
 	// octant-only keys sort in one pass and keep caller order inside an octant
 	const int begin_bit = (a.variant & kVarSortOctantOnly) ? 27 : 0;
@@ -211,15 +219,31 @@ lrx_status launch_trace_sorted(const TraceArgs &a_in, const float lo[3], const f
 		cub::DoubleBuffer<uint32_t> dk(nullptr, nullptr), dv(nullptr, nullptr);
 		LRX_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, temp_bytes, dk, dv, (int)n, begin_bit, 30, st));
 	}
-	const size_t arr = ((sizeof(uint32_t) * (size_t)n + 255) / 256) * 256;
+	const size_t arr = sorted_scratch_arrays(n) / 4;
 	const size_t total = 4 * arr + temp_bytes;
 	void *base = nullptr;
-	LRX_CUDA(cudaMallocFromPoolAsync(&base, total, pool, st));
+	if (fixed) {
+		if (total > fixed->bytes) {
+			set_error("ray sort: " + std::to_string(total) + " scratch bytes needed, " +
+					std::to_string(fixed->bytes) + " lent");
+			return LRX_ERR_NOT_SUPPORTED;
+		}
+		base = fixed->base;
+	} else {
+		int dev = 0;
+		LRX_CUDA(cudaGetDevice(&dev));
+		if (dev < 0 || dev >= kMaxDevices) return launch_trace(a, st);
+		cudaMemPool_t pool;
+		lrx_status prc = stream_pool(dev, &pool);
+		if (prc != LRX_OK) return prc;
+		LRX_CUDA(cudaMallocFromPoolAsync(&base, total, pool, st));
+	}
 	unsigned char *p = static_cast<unsigned char *>(base);
 	uint32_t *k0 = reinterpret_cast<uint32_t *>(p), *k1 = reinterpret_cast<uint32_t *>(p + arr);
 	uint32_t *v0 = reinterpret_cast<uint32_t *>(p + 2 * arr), *v1 = reinterpret_cast<uint32_t *>(p + 3 * arr);
 	void *temp = p + 4 * arr;
 
+	lrx_status rc = LRX_OK;
 	float3 l = make_float3(lo[0], lo[1], lo[2]);
 	float3 s = key_scale(lo, hi);
 	k_ray_keys<<<(n + 255) / 256, 256, 0, st>>>(reinterpret_cast<const float4 *>(a.rays), n, l, s, k0, v0);
@@ -232,7 +256,7 @@ lrx_status launch_trace_sorted(const TraceArgs &a_in, const float lo[3], const f
 			rc = launch_trace(a, st);
 		}
 	}
-	cudaFreeAsync(base, st);  // ordered after the trace on the same stream
+	if (!fixed) cudaFreeAsync(base, st);  // ordered after the trace on the same stream
 	if (e != cudaSuccess) return cuda_fail(e, "ray sort");
 	return rc;
 }

@@ -229,6 +229,96 @@ __device__ __forceinline__ uint2 stack_get(const TravStack &st, StackTop t, int 
 enum : int { kRayMasked = 0, kRayAnswered = 1, kRayTraverse = 2 };
 
 // ---------------------------------------------------------------------------
+// Launch deadline, counted in %globaltimer ticks of 1,024 ns (~1 us) from the
+// launch's start: the first time any of its blocks or warps looked, kept in
+// the launch's counter slot (zeroed again after the launch, so every
+// execution, graph replays included, starts afresh).  It is checked only
+// where rays are about to start, never inside a ray's walk -- a started ray
+// is bounded by its visit budget:
+// - persistent kernels: the claiming lane reads the timer on the claim that
+//   crosses each kDeadlineCheckRays boundary of the claim counter; once the
+//   deadline has passed it sets bit 31 of the counter, so every later claim
+//   of the launch sees it in its atomic's return value and starts no ray;
+// - one-ray-per-thread kernels: thread 0 of each block checks once, at the
+//   block's start (or per tile in the tile queue kernel); a late block starts
+//   none of its rays.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kDeadlineCheckRays = 2048;
+constexpr uint32_t kClaimLate = 0x80000000u;  // claims stay below 2^31 (kMaxFetchRays)
+
+__device__ __forceinline__ uint32_t now_ticks() {
+	uint64_t t;
+	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+	return (uint32_t)(t >> 10);
+}
+
+// Per-launch counter slots of 256 bytes: words 0-3 claim counters (one per
+// ray class of a queue launch; single-batch kernels use word 0), word 4 the
+// count of blocks that have stopped claiming, word 32 -- a cache line of its
+// own, away from the claim atomics -- the launch's start (its first reader's
+// time in timer ticks | 1, so that 0 means not yet).
+constexpr int kSlotWords = 64, kSlotFinished = 4, kSlotStart = 32;
+__device__ uint32_t g_queue[kQueueSlots][kSlotWords];
+
+// The launch's start.  Only the installer (one caller per launch) writes it;
+// any other caller that finds it not yet written takes its own time, which is
+// later and so only more lenient.  (Slot words are zero when a launch begins
+// and are zeroed again after it; no compare-and-swap, so the first wave of
+// blocks does not queue on one address.)
+__device__ __forceinline__ uint32_t slot_start(uint32_t *slot, bool installer) {
+	const uint32_t v = *reinterpret_cast<volatile uint32_t *>(&slot[kSlotStart]);
+	if (v != 0u) return v;
+	const uint32_t mine = now_ticks() | 1u;
+	if (installer) *reinterpret_cast<volatile uint32_t *>(&slot[kSlotStart]) = mine;
+	return mine;
+}
+
+// Slot protocol shared by the persistent kernels: a launch owns a slot, all
+// zero at entry; every block adds itself to the finished count once it has
+// stopped claiming work, and the last one zeroes the slot for its next user.
+__device__ __forceinline__ void release_slot(uint32_t *slot) {
+	if (threadIdx.x == 0) {
+		__threadfence();
+		if (atomicAdd(&slot[kSlotFinished], 1u) == gridDim.x - 1) {  // every block has stopped claiming work
+#pragma unroll
+			for (int w = 0; w < kSlotWords; ++w) slot[w] = 0u;
+			__threadfence();
+		}
+	}
+}
+
+// The start a block counts the deadline from, and (one-ray-per-thread
+// kernels) whether the block found the deadline passed; one copy per block.
+__shared__ uint32_t s_launch_start, s_block_late;
+
+// Block start (all threads of the block) of a persistent kernel: all of its
+// blocks are resident from the launch's start, so each counts from its own
+// start, with no memory access; expiry spreads through the claim counter.
+__device__ __forceinline__ void note_block_start() {
+	if (threadIdx.x == 0) s_launch_start = now_ticks();
+	__syncthreads();
+}
+
+// True once `deadline_ticks` (non-zero, below 2^31) has passed since
+// `start`.  The difference is signed: a reading a tick behind `start` (timer
+// skew between SMs) is not past, and the timer's 2^32 wrap does not matter.
+__device__ __forceinline__ bool past_deadline(uint32_t start, uint32_t deadline_ticks) {
+	return deadline_ticks != 0u && (int32_t)(now_ticks() - start) > (int32_t)deadline_ticks;
+}
+
+// The claiming lane's deadline test (persistent kernels): `base` is the
+// claim's atomicAdd result on `counter`.  Returns base, with kClaimLate set
+// when the claim must start no ray.
+__device__ __forceinline__ uint32_t claim_deadline(uint32_t base, uint32_t nidle, uint32_t *counter, uint32_t start,
+		uint32_t deadline_ticks) {
+	if (!(base & kClaimLate) && (base & (kDeadlineCheckRays - 1u)) < nidle && past_deadline(start, deadline_ticks)) {
+		atomicOr(counter, kClaimLate);  // every later claim of the launch sees it
+		base |= kClaimLate;
+	}
+	return base;
+}
+
+// ---------------------------------------------------------------------------
 // Motion instances: the transform at a ray's time, from the host-decomposed
 // intervals -- MotionSystem::Sample and InterpolatedTransform::Sample
 // (src/luxrays/core/geometry/motionsystem.cpp:56-160, 333-337; the GPU
@@ -374,9 +464,11 @@ __device__ __forceinline__ int ray_begin(const TraceArgs &a, uint32_t i, bool st
 // One trip of the traversal loop: expand one node (or take a popped group),
 // test the triangles it yields (or enter one instance), pop when the node
 // group is spent.  Returns true when the ray is finished: stack empty, any
-// hit found, or abandoned (stack overflow / visit limit, recorded in the
-// status word).  Every trip either expands a node -- at most visit_limit of
-// them -- or consumes a stack entry or an instance bit, so a ray finishes in
+// hit found, or abandoned -- stack overflow or visit budget spent, recorded
+// in the status word, and s.sp set to -1 so the caller writes no hit.
+// Every trip either expands a node -- spending the visit budget, which only
+// instance entries raise, each by a bounded amount once per instance leaf
+// bit -- or consumes a stack entry or an instance bit, so a ray finishes in
 // a bounded number of trips.
 template <bool ANY, bool TWO_LEVEL, bool COUNT, bool MM3, bool SMEM = false, bool MOTION = false>
 __device__ __forceinline__ bool ray_step(const TraceArgs &a, TravState &s, TravStack &stack, bool keep, uint64_t pol,
@@ -385,6 +477,7 @@ __device__ __forceinline__ bool ray_step(const TraceArgs &a, TravState &s, TravS
 	{                                                        \
 		if (s.sp >= kStackSize) {                            \
 			atomicOr(a.status, kStatusStackOverflow);        \
+			s.sp = -1;                                       \
 			return true;                                     \
 		}                                                    \
 		stack_put<SMEM>(stack, top, s.sp++, (V));            \
@@ -397,6 +490,7 @@ __device__ __forceinline__ bool ray_step(const TraceArgs &a, TravState &s, TravS
 		if (s.ng.y > 0x00ffffffu) LRX_PUSH(s.ng);
 		if (++s.visits > a.visit_limit) {
 			atomicOr(a.status, kStatusVisitLimit);
+			s.sp = -1;
 			return true;
 		}
 		if (COUNT) ++c.nodes;
@@ -418,6 +512,7 @@ __device__ __forceinline__ bool ray_step(const TraceArgs &a, TravState &s, TravS
 			const uint4 info = __ldg(reinterpret_cast<const uint4 *>(&ir->info));
 			if (COUNT) ++c.insts;
 			s.inst_obj = info.y;
+			s.visits -= min(a.blas_visits, s.visits);  // credit for the BLAS's walk
 			if (info.z & kInstIdentity) {
 				make_active(s.ray, s.wo, s.wd);
 			} else if (MOTION && (info.z & kInstMotion)) {
@@ -503,7 +598,8 @@ __device__ __forceinline__ void ray_write(const TraceArgs &a, uint32_t i, const 
 }
 
 // Traces ray `tid` of the batch `a` (through a.order when set) and writes its
-// hit.  Shared by the one-batch kernel and the multi-batch queue kernel.
+// hit, unless the ray is abandoned.  Shared by the one-batch kernel and the
+// multi-batch tile queue kernel (which test the deadline before calling).
 template <bool ANY, bool TWO_LEVEL, bool COUNT, uint32_t CV>
 __device__ __forceinline__ void trace_ray(const TraceArgs &a, uint32_t tid, bool active, Counts &cnt,
 		StackTop top = StackTop{nullptr, 0}) {
@@ -519,9 +615,11 @@ __device__ __forceinline__ void trace_ray(const TraceArgs &a, uint32_t tid, bool
 	TravStack stack;
 	const int k = ray_begin(a, i, stream, s);
 	if (k == kRayMasked) return;
-	if (k == kRayTraverse)
+	if (k == kRayTraverse) {
 		while (!ray_step<ANY, TWO_LEVEL, COUNT, MM3, SMEM, MOTION>(a, s, stack, keep, pol, cnt, top)) {
 		}
+		if (s.sp < 0) return;  // abandoned
+	}
 	ray_write(a, i, s, stream);
 	if (COUNT) cnt.rays += 1;
 }
@@ -533,6 +631,20 @@ __global__ void __launch_bounds__((CV & kVarOccupancy) ? 64 : (TWO_LEVEL ? 896 :
 k_trace(TraceArgs a) {
 	extern __shared__ uint2 s_stack_top[];  // kSmemStack entries per thread with SMEM_STACK, else empty
 	const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+	// this thread's ray is on its way into L1 while thread 0 looks up the
+	// launch's start: the block waits for the two at once
+	if (tid < a.count) {
+		const char *rp = static_cast<const char *>(a.rays) + 48 * (size_t)(a.order ? a.order[tid] : tid);
+		asm volatile("prefetch.global.L1 [%0];" ::"l"(rp));
+		asm volatile("prefetch.global.L1 [%0];" ::"l"(rp + 47));
+	}
+	if (threadIdx.x == 0) {
+		const uint32_t start = slot_start(g_queue[a.launch_id % kQueueSlots], blockIdx.x == 0);
+		s_block_late = past_deadline(start, a.deadline_ticks) ? 1u : 0u;
+		if (s_block_late) atomicOr(a.status, kStatusDeadline);
+	}
+	__syncthreads();
+	if (s_block_late) return;  // started after the deadline: none of the block's rays
 	if (!COUNT && tid >= a.count) return;
 	Counts cnt{0, 0, 0, 0};
 	trace_ray<ANY, TWO_LEVEL, COUNT, CV>(a, tid, tid < a.count, cnt, StackTop{s_stack_top + threadIdx.x, blockDim.x});
@@ -551,31 +663,18 @@ k_trace(TraceArgs a) {
 			for (int k = 0; k < 4; ++k) atomicAdd(&a.counters[k], v[k]);
 		}
 	}
+	// the launch start is cleared after the launch (k_clear_launch_start)
 }
 
-// Per-launch counter slots: words 0-3 claim counters (one per ray class of
-// a queue launch; single-batch kernels use word 0), word 4 the count of
-// blocks that have stopped claiming.
-constexpr int kSlotWords = 8, kSlotFinished = 4;
-__device__ uint32_t g_queue[kQueueSlots][kSlotWords];
-
-// Slot protocol shared by the persistent kernels: a launch owns a slot, all
-// zero at entry; every block adds itself to the finished count once it has
-// stopped claiming work, and the last one zeroes the slot for its next user.
-__device__ __forceinline__ void release_slot(uint32_t *slot) {
-	if (threadIdx.x == 0) {
-		__threadfence();
-		if (atomicAdd(&slot[kSlotFinished], 1u) == gridDim.x - 1) {  // every block has stopped claiming work
-#pragma unroll
-			for (int w = 0; w < kSlotWords; ++w) slot[w] = 0u;
-			__threadfence();
-		}
-	}
+// Zeroes the launch start of a one-ray-per-thread launch after it, on its
+// stream, so its counter slot is all zero again for the slot's next user.
+__global__ void k_clear_launch_start(uint32_t slot_index) {
+	g_queue[slot_index][kSlotStart] = 0u;
 }
 
-uint32_t next_queue_slot() {
+uint32_t next_launch_id() {
 	static std::atomic<uint32_t> next{0};
-	return next.fetch_add(1u) % kQueueSlots;
+	return next.fetch_add(1u);
 }
 
 // ---------------------------------------------------------------------------
@@ -593,19 +692,24 @@ uint32_t next_queue_slot() {
 // claims run out.  Every ballot/shuffle is executed by all 32 lanes: the
 // block is a whole number of warps, no lane leaves the loop alone (the exit
 // test is warp-uniform), and `refill` is in [1, 32].
+// Deadline: the claiming lane reads the timer; once the launch's deadline
+// has passed, the warp still claims rays (so the counter runs out as
+// before) but starts none of them -- their hits are not written and the
+// status word records it -- while rays already started finish their walks.
 // ---------------------------------------------------------------------------
 
 // Two-level builds carry the world ray and instance state on top of the
 // flat ones: 72 registers (7 blocks of 128 per SM) keep them from spilling,
 // which is faster than 64 with spills (instanced closest hit +5.6 %).
 template <bool ANY, bool TWO_LEVEL, uint32_t CV>
-__global__ void __launch_bounds__(kTraceBlock, TWO_LEVEL ? 7 : 8) k_trace_fetch(TraceArgs a, uint32_t slot_index, uint32_t refill) {
+__global__ void __launch_bounds__(kTraceBlock, TWO_LEVEL ? 7 : 8) k_trace_fetch(TraceArgs a, uint32_t refill) {
 	constexpr bool MM3 = (CV & kVarMinMax3) != 0;
 	constexpr bool SMEM = (CV & kVarSmemStack) != 0;
 	constexpr bool MOTION = (CV & kVarMotion) != 0;
 	extern __shared__ uint2 s_stack_top[];  // kSmemStack entries per thread with SMEM_STACK, else empty
 	const StackTop top{s_stack_top + threadIdx.x, blockDim.x};
-	uint32_t *slot = g_queue[slot_index];
+	uint32_t *slot = g_queue[a.launch_id % kQueueSlots];
+	note_block_start();
 	const bool keep = (a.variant & kVarSceneEvictLast) != 0;
 	const bool stream = (a.variant & kVarStreamRays) != 0;
 	const uint64_t pol = keep ? evict_last_policy() : 0ull;
@@ -622,10 +726,15 @@ __global__ void __launch_bounds__(kTraceBlock, TWO_LEVEL ? 7 : 8) k_trace_fetch(
 		if (!drained && nidle >= refill) {
 			const uint32_t leader = __ffs(idle) - 1;
 			uint32_t base = 0;
-			if (lane == leader) base = atomicAdd(&slot[0], nidle);
+			if (lane == leader) {
+				base = claim_deadline(atomicAdd(&slot[0], nidle), nidle, &slot[0], s_launch_start, a.deadline_ticks);
+				if ((base & kClaimLate) && (base & ~kClaimLate) < count) atomicOr(a.status, kStatusDeadline);
+			}
 			base = __shfl_sync(0xffffffffu, base, leader);
+			const bool late = (base & kClaimLate) != 0u;
+			base &= ~kClaimLate;
 			drained = base + nidle >= count;
-			if (rid == kNull) {
+			if (rid == kNull && !late) {
 				const uint32_t idx = base + __popc(idle & ((1u << lane) - 1u));
 				if (idx < count) {
 					const uint32_t i = a.order ? a.order[idx] : idx;
@@ -640,7 +749,7 @@ __global__ void __launch_bounds__(kTraceBlock, TWO_LEVEL ? 7 : 8) k_trace_fetch(
 			continue;  // every lane idle: the next trip claims 32 rays
 		}
 		if (rid != kNull && ray_step<ANY, TWO_LEVEL, false, MM3, SMEM, MOTION>(a, s, stack, keep, pol, cnt, top)) {
-			ray_write(a, rid, s, stream);
+			if (s.sp >= 0) ray_write(a, rid, s, stream);  // an abandoned ray writes nothing
 			rid = kNull;
 		}
 	}
@@ -673,6 +782,10 @@ __device__ __forceinline__ TraceArgs batch_args(const QueueParams &p, const Queu
 	a.postpone = (qb.flags >> 8) & 0xffu;
 	a.variant = (qb.flags >> 16) & 0xffu;
 	a.visit_limit = qb.visit_limit;
+	const uint32_t f = (qb.flags >> 24) & 31u;
+	a.blas_visits = f ? 1u << f : 0u;
+	a.deadline_ticks = p.deadline_ticks;
+	a.launch_id = p.launch_id;
 	return a;
 }
 
@@ -680,11 +793,16 @@ template <uint32_t CV>
 __global__ void __launch_bounds__(kTileRays, 12) k_trace_queue(const __grid_constant__ QueueParams p) {
 	__shared__ uint32_t s_tile;
 	uint32_t *slot = g_queue[p.slot];
+	note_block_start();
 	Counts cnt{0, 0, 0, 0};
 	for (;;) {
-		if (threadIdx.x == 0) s_tile = atomicAdd(&slot[0], 1u);
+		if (threadIdx.x == 0) {
+			s_tile = atomicAdd(&slot[0], 1u);
+			s_block_late = past_deadline(s_launch_start, p.deadline_ticks) ? 1u : 0u;
+		}
 		__syncthreads();
 		const uint32_t tile = s_tile;
+		const bool late = s_block_late != 0u;
 		__syncthreads();
 		if (tile >= p.total_tiles) break;
 		uint32_t lo = 0, hi = p.n;  // last batch whose first tile is <= tile
@@ -696,7 +814,8 @@ __global__ void __launch_bounds__(kTileRays, 12) k_trace_queue(const __grid_cons
 		const QueueBatch &qb = p.b[lo];
 		const TraceArgs a = batch_args(p, qb);
 		const uint32_t tid = (tile - qb.tile_begin) * kTileRays + threadIdx.x;
-		const bool active = tid < a.count;
+		const bool active = tid < a.count && !late;  // past the deadline: the tile's rays are not started
+		if (late && threadIdx.x == 0) atomicOr(a.status, kStatusDeadline);
 		if (a.any_hit) {
 			if (a.two_level) trace_ray<true, true, false, CV>(a, tid, active, cnt);
 			else trace_ray<true, false, false, CV>(a, tid, active, cnt);
@@ -762,7 +881,10 @@ __device__ __forceinline__ uint32_t batch_of_ray(const QueueParams &p, uint32_t 
 // a trip whose finishing lanes span batches adds per batch group
 // (__match_any_sync).  The add that brings a batch to its count raises the
 // batch's flag.  Termination as k_trace_fetch: each trip steps a busy lane or
-// claims rays, and the counter only grows.
+// claims rays, and the counter only grows.  Past the launch's deadline a
+// warp's claims start no rays; each claimed ray then counts as finished
+// (so every batch's flag is still raised) with its hit not written and its
+// scene's status word recording the deadline.
 template <bool ANY, bool TWO_LEVEL, bool MM3, bool FLAGS>
 __device__ __forceinline__ void drain_class(const QueueParams &p, uint32_t c, uint32_t *counter, uint32_t lane,
 		TravState &s, TravStack &stack) {
@@ -782,23 +904,34 @@ __device__ __forceinline__ void drain_class(const QueueParams &p, uint32_t c, ui
 		if (!drained && nidle >= p.refill) {
 			const uint32_t leader = __ffs(idle) - 1;
 			uint32_t base = 0;
-			if (lane == leader) base = atomicAdd(counter, nidle);
+			if (lane == leader) {
+				base = atomicAdd(counter, nidle);
+				if (!(base & kClaimLate) && (base & (kDeadlineCheckRays - 1u)) < nidle)
+					base = claim_deadline(base, nidle, counter, slot_start(counter - c, base == 0u), p.deadline_ticks);
+			}
 			base = __shfl_sync(0xffffffffu, base, leader);
+			const bool late = (base & kClaimLate) != 0u;
+			base &= ~kClaimLate;
 			drained = base + nidle >= nrays;
 			if (rid == kNull) {
 				const uint32_t g = base + __popc(idle & ((1u << lane) - 1u));
 				if (g < nrays) {
 					bi = batch_of_ray(p, r0 + g, cb, ce);
-					const TraceArgs a = batch_args(p, p.b[bi]);
-					const uint32_t local = r0 + g - p.b[bi].ray_begin;
-					const uint32_t i = a.order ? a.order[local] : local;  // the ray (sorted batches: permuted)
-					const bool stream = (a.variant & kVarStreamRays) != 0;
-					const int k = ray_begin(a, i, stream, s);
-					if (k == kRayTraverse) {
-						rid = i;
-					} else {
-						if (k == kRayAnswered) ray_write(a, i, s, stream);
+					if (late) {
+						atomicOr(p.b[bi].status, kStatusDeadline);
 						fin = true;
+					} else {
+						const TraceArgs a = batch_args(p, p.b[bi]);
+						const uint32_t local = r0 + g - p.b[bi].ray_begin;
+						const uint32_t i = a.order ? a.order[local] : local;  // the ray (sorted batches: permuted)
+						const bool stream = (a.variant & kVarStreamRays) != 0;
+						const int k = ray_begin(a, i, stream, s);
+						if (k == kRayTraverse) {
+							rid = i;
+						} else {
+							if (k == kRayAnswered) ray_write(a, i, s, stream);
+							fin = true;
+						}
 					}
 				}
 			}
@@ -808,7 +941,7 @@ __device__ __forceinline__ void drain_class(const QueueParams &p, uint32_t c, ui
 			const bool keep = (a.variant & kVarSceneEvictLast) != 0;
 			const uint64_t pol = keep ? evict_last_policy() : 0ull;
 			if (ray_step<ANY, TWO_LEVEL, false, MM3>(a, s, stack, keep, pol, cnt)) {
-				ray_write(a, rid, s, (a.variant & kVarStreamRays) != 0);
+				if (s.sp >= 0) ray_write(a, rid, s, (a.variant & kVarStreamRays) != 0);  // abandoned: no hit
 				rid = kNull;
 				fin = true;
 			}
@@ -982,13 +1115,15 @@ static lrx_status launch_fetch(const TraceArgs &a, uint32_t bs, cudaStream_t st)
 	if (rc != LRX_OK) return rc;
 	const uint32_t grid = (uint32_t)std::min<uint64_t>(((uint64_t)a.count + bs - 1) / bs, (uint64_t)resident);
 	const uint32_t refill = a.refill == 0 ? 16u : std::min(32u, a.refill);
-	k_trace_fetch<ANY, TWO_LEVEL, CV><<<grid, bs, smem_bytes, st>>>(a, next_queue_slot(), refill);
+	k_trace_fetch<ANY, TWO_LEVEL, CV><<<grid, bs, smem_bytes, st>>>(a, refill);
 	LRX_CUDA(cudaGetLastError());
 	return LRX_OK;
 }
 
-lrx_status launch_trace(const TraceArgs &a, cudaStream_t st) {
-	if (a.count == 0) return LRX_OK;
+lrx_status launch_trace(const TraceArgs &a_in, cudaStream_t st) {
+	if (a_in.count == 0) return LRX_OK;
+	TraceArgs a = a_in;
+	a.launch_id = next_launch_id();  // its counter slot (persistent) or launch-start word
 	uint32_t bs = a.block_size ? a.block_size : kTraceBlock;
 	if (bs < 32 || bs > 512 || (bs & 31)) {
 		set_error("trace block size must be a multiple of 32 in [32, 512]");
@@ -999,7 +1134,7 @@ lrx_status launch_trace(const TraceArgs &a, cudaStream_t st) {
 	if (a.motion && a.two_level) {
 		// motion scenes: builds of their own (no MINMAX3 / SMEM_STACK / occupancy
 		// forms), so the static builds carry no motion code
-		if ((a.variant & kVarPersistent) && !cnt && a.count < 0x80000000u) {
+		if ((a.variant & kVarPersistent) && !cnt && a.count <= kMaxFetchRays) {
 			const uint32_t fbs = std::min(bs, kTraceBlock);
 			return a.any_hit ? launch_fetch<true, true, kVarMotion>(a, fbs, st)
 					: launch_fetch<false, true, kVarMotion>(a, fbs, st);
@@ -1012,9 +1147,11 @@ lrx_status launch_trace(const TraceArgs &a, cudaStream_t st) {
 			else k_trace<false, true, false, kVarMotion><<<grid, bs, 0, st>>>(a);
 		}
 		LRX_CUDA(cudaGetLastError());
+		k_clear_launch_start<<<1, 1, 0, st>>>(a.launch_id % kQueueSlots);
+		LRX_CUDA(cudaGetLastError());
 		return LRX_OK;
 	}
-	if ((a.variant & kVarPersistent) && !cnt && a.count < 0x80000000u) {
+	if ((a.variant & kVarPersistent) && !cnt && a.count <= kMaxFetchRays) {
 		// persistent warps with ray fetch; block size capped at kTraceBlock
 		const uint32_t fbs = std::min(bs, kTraceBlock);
 		const bool mm3 = (a.variant & kVarMinMax3) != 0;
@@ -1050,6 +1187,8 @@ lrx_status launch_trace(const TraceArgs &a, cudaStream_t st) {
 	}
 #undef LRX_LAUNCH_V
 #undef LRX_LAUNCH
+	LRX_CUDA(cudaGetLastError());
+	k_clear_launch_start<<<1, 1, 0, st>>>(a.launch_id % kQueueSlots);
 	LRX_CUDA(cudaGetLastError());
 	return LRX_OK;
 }

@@ -78,7 +78,7 @@ class BuildOpts(ctypes.Structure):
 class TraceConfig(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_uint32), ("block_size", ctypes.c_uint32),
                 ("postpone", ctypes.c_uint32), ("variant", ctypes.c_uint32), ("modes", ctypes.c_uint32),
-                ("refill", ctypes.c_uint32)]
+                ("refill", ctypes.c_uint32), ("max_visits", ctypes.c_uint32), ("deadline_us", ctypes.c_uint32)]
 
 
 class MotionDesc(ctypes.Structure):
@@ -484,19 +484,27 @@ class Scene:
         return inf.as_dict()
 
     def set_trace_config(self, block_size: int = 64, postpone: int = 8, variant: int = 0, modes: int = 0,
-                         refill: int = 0):
+                         refill: int = 0, max_visits: int = 0, deadline_us: int = 0):
         """modes: 1 = closest-hit launches, 2 = any-hit launches, 0 = both.
         refill: with LRX_VARIANT_PERSISTENT, idle lanes that trigger a warp's
-        next ray claim (0 = the library default)."""
-        c = TraceConfig(ctypes.sizeof(TraceConfig), block_size, postpone, variant, modes, refill)
+        next ray claim (0 = the library default).  max_visits / deadline_us:
+        the failure bounds (0 = the scene's own visit bound / the default
+        launch deadline)."""
+        c = TraceConfig(ctypes.sizeof(TraceConfig), block_size, postpone, variant, modes, refill, max_visits,
+                        deadline_us)
         check(load().lrx_scene_set_trace_config(self.handle, ctypes.byref(c)))
 
-    def trace_config(self, mode: int = LRX_TRACE_CLOSEST) -> dict:
+    def trace_config(self, mode: int = LRX_TRACE_CLOSEST, bounds: bool = False) -> dict:
+        """The launch configuration of `mode`; with bounds, also its failure
+        bounds (max_visits, deadline_us)."""
         c = TraceConfig()
         c.struct_size = ctypes.sizeof(TraceConfig)
         c.modes = 2 if mode == LRX_TRACE_ANY else 1
         check(load().lrx_scene_get_trace_config(self.handle, ctypes.byref(c)))
-        return {"block_size": c.block_size, "postpone": c.postpone, "variant": c.variant, "refill": c.refill}
+        out = {"block_size": c.block_size, "postpone": c.postpone, "variant": c.variant, "refill": c.refill}
+        if bounds:
+            out.update(max_visits=c.max_visits, deadline_us=c.deadline_us)
+        return out
 
     def autotune(self, d_rays: int, count: int, mode: int = LRX_TRACE_CLOSEST, stream: int = 0) -> dict:
         """Picks this scene's fastest launch configuration for `mode` on a

@@ -34,7 +34,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_abi_version_and_error_string(lib):
-    assert lib.lrx_abi_version() == 2
+    assert lib.lrx_abi_version() == 3
     assert isinstance(lib.lrx_last_error(), bytes)
 
 
@@ -44,7 +44,7 @@ def test_struct_layouts():
     assert ctypes.sizeof(lrx.MeshDesc) == 24
     assert ctypes.sizeof(lrx.ObjectDesc) == 136
     assert ctypes.sizeof(lrx.BuildOpts) == 16
-    assert ctypes.sizeof(lrx.TraceConfig) == 24
+    assert ctypes.sizeof(lrx.TraceConfig) == 32  # ABI 3: + max_visits, deadline_us
 
 
 def test_variant_constants_match_the_header():
