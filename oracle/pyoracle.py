@@ -18,6 +18,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liblrx_oracle.so")
 REF_LIB_PATH = os.path.join(HERE, "_ref", "liblrx_refcl.so")
 REF_MBVH_LIB_PATH = os.path.join(HERE, "_ref", "liblrx_refcl_mbvh.so")
+# the reference's CUDA kernel text (stitched by build_ref.sh from the LuxCore
+# tree) and the host harness that compiles and launches it on the GPU
+REFCU_SRC_PATH = os.path.join(HERE, "_ref", "refcu_bvh_kernel.cu")
+REFCU_LIB_PATH = os.path.join(HERE, "_build", "liblrx_refcu.so")
 
 ACCEL_BVH, ACCEL_MBVH = 0, 1
 
@@ -54,6 +58,77 @@ def build(force: bool = False) -> str:
                            "-std=c++17", "-pthread", src, "-o", tmp])
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
+
+
+def _cuda_home() -> str | None:
+    for c in (os.environ.get("CUDA_HOME"), "/usr/local/cuda"):
+        if c and os.path.exists(os.path.join(c, "include", "nvrtc.h")):
+            return c
+    return None
+
+
+def build_refcu(force: bool = False) -> str | None:
+    """Compile the host harness of the reference's CUDA kernel (NVRTC +
+    driver API; it holds no kernel code of its own).  None when the CUDA
+    toolkit's NVRTC is absent."""
+    cuda = _cuda_home()
+    if cuda is None:
+        return None
+    src = os.path.join(HERE, "refcu_harness.cpp")
+    if not force and os.path.exists(REFCU_LIB_PATH) and os.path.getmtime(REFCU_LIB_PATH) >= os.path.getmtime(src):
+        return REFCU_LIB_PATH
+    os.makedirs(os.path.dirname(REFCU_LIB_PATH), exist_ok=True)
+    lib64 = os.path.join(cuda, "lib64")
+    tmp = REFCU_LIB_PATH + f".tmp{os.getpid()}"
+    subprocess.check_call(["g++", "-O2", "-fPIC", "-shared", "-std=c++17", src, "-o", tmp,
+                           "-I", os.path.join(cuda, "include"), "-L", lib64, "-L", os.path.join(lib64, "stubs"),
+                           f"-Wl,-rpath,{lib64}", "-lnvrtc", "-lcuda"])
+    os.replace(tmp, REFCU_LIB_PATH)
+    return REFCU_LIB_PATH
+
+
+class RefCudaKernel:
+    """The reference's own CUDA intersection kernel (bvh.cl's
+    Accelerator_Intersect_RayBuffer, compiled by NVRTC as the reference's
+    CUDA device compiles it -- with its PATHOCL engine's --use_fast_math, or
+    without it) on the current GPU, over the oracle's
+    BVHArrayNode[] (OracleScene.bvh_nodes) and the concatenated mesh
+    vertices.  `available` is False, with `reason`, when the kernel text (a
+    build product of the reference tree) or the harness is missing."""
+
+    def __init__(self, fast_math: bool = True):
+        self.available, self.reason, self.info = False, "", ""
+        self.fast_math = 1 if fast_math else 0
+        if not os.path.exists(REFCU_SRC_PATH):
+            self.reason = "reference kernel text not built (oracle/build_ref.sh needs the LuxCore source tree)"
+            return
+        path = build_refcu()
+        if path is None:
+            self.reason = "NVRTC not found"
+            return
+        try:
+            self.L = ctypes.CDLL(path)
+        except OSError as e:  # no CUDA driver on this machine
+            self.reason = f"harness not loadable: {e}"
+            return
+        self.L.refcu_load.restype = ctypes.c_int
+        self.L.refcu_load.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_size_t]
+        self.L.refcu_trace.restype = ctypes.c_int
+        self.L.refcu_trace.argtypes = [ctypes.c_int, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32,
+                                       ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_void_p]
+        buf = ctypes.create_string_buffer(4096)
+        rc = self.L.refcu_load(REFCU_SRC_PATH.encode(), self.fast_math, buf, len(buf))
+        self.info = buf.value.decode(errors="replace")
+        if rc != 0:
+            self.reason = f"refcu_load failed ({rc}): {self.info}"
+            return
+        self.available = True
+
+    def trace(self, d_rays: int, d_hits: int, count: int, d_verts: int, d_nodes: int, block: int = 32,
+              stream: int = 0):
+        rc = self.L.refcu_trace(self.fast_math, d_rays, d_hits, count, d_verts, d_nodes, block, ctypes.c_void_p(stream))
+        if rc != 0:
+            raise RuntimeError(f"refcu_trace: CUresult {rc}")
 
 
 def lib():
