@@ -277,6 +277,54 @@ def reference_layout_bytes(o, sets, stride: int = 16):
     return out
 
 
+def reference_gpu_arm(torch, oracle_scene, scene_desc, sets, ref_hits, stride, stream, device, reps=3):
+    """The reference's own CUDA kernel (bvh.cl as its CUDA device compiles it,
+    oracle.pyoracle.RefCudaKernel) on this GPU over the oracle's
+    BVHArrayNode[] with 32-thread blocks: Mrays/s per set (CUDA events on
+    `stream`, `reps` launches after one warm-up) and its hits' parity with
+    the oracle on the CPU sample.  The reference kernel has no any-hit mode,
+    so every set, shadow rays included, is a closest-hit trace."""
+    from oracle import pyoracle as po
+    from oracle.parity import compare
+    k = po.RefCudaKernel(fast_math=True)
+    if not k.available:
+        return {"unavailable": k.reason}
+    nodes = torch.from_numpy(oracle_scene.bvh_nodes().copy()).to(device)
+    verts = torch.from_numpy(np.ascontiguousarray(np.concatenate([m.vertices for m in scene_desc.meshes]),
+                                                  np.float32).copy()).to(device)
+    st = stream.cuda_stream
+    per_ms, per_mrays, parity = {}, {}, {}
+    total_rays, total_ms = 0, 0.0
+    for (name, rays, _mode), rh in zip(sets, ref_hits):
+        n = rays.shape[0]
+        d_r = torch.from_numpy(np.ascontiguousarray(rays).view(np.uint8).reshape(-1).copy()).to(device)
+        d_h = torch.empty(n * HIT_BYTES, dtype=torch.uint8, device=device)
+        torch.cuda.synchronize()
+        k.trace(d_r.data_ptr(), d_h.data_ptr(), n, verts.data_ptr(), nodes.data_ptr(), 32, st)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            k.trace(d_r.data_ptr(), d_h.data_ptr(), n, verts.data_ptr(), nodes.data_ptr(), 32, st)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        per_ms[name] = round(ms, 4)
+        per_mrays[name] = round(n / (ms / 1e3) / 1e6, 1)
+        total_rays += n
+        total_ms += ms
+        hits = d_h.cpu().numpy().view(W.HIT_DTYPE)
+        c = compare(np.ascontiguousarray(hits[::stride]), rh, oracle_scene, np.ascontiguousarray(rays[::stride]))
+        parity[name] = {kk: c[kk] for kk in ("n", "agree", "ties", "bad_disagreements", "bitexact_t")}
+        del d_r, d_h
+    return {"Mrays": round(total_rays / (total_ms / 1e3) / 1e6, 1), "ms_per_step": round(total_ms, 4),
+            "per_set_ms": per_ms, "per_set_Mrays": per_mrays, "parity_vs_oracle": parity,
+            "compiled": k.info, "block": 32,
+            "layout": "the oracle's BVHArrayNode[] (classic builder, 4-ary), one vertex page, one node page; "
+                      "every set traced closest-hit (no any-hit mode in the reference kernel)",
+            "sample": f"parity on every {stride}th ray of each set, against the oracle's BVHAccel (fast math "
+                      "moves t, b1, b2 in the last bits and flips a few near-ties)"}
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -619,6 +667,7 @@ def run_lrx(args):
     if rank == 0:
         cpu = None
         parity = None
+        ref_gpu = None
         if not args.no_cpu_baseline:
             threads = os.cpu_count() or 1
             frac = args.ref_fraction
@@ -628,6 +677,9 @@ def run_lrx(args):
                    "sample": f"every {frac}th ray of each of the 3 sets ({n_s} rays), oracle BVHAccel::Intersect "
                              f"restatement, classic-builder BVH, {threads} threads"}
             parity = parity_block(oracle_scene, sets, step_hits, ref_hits, frac)
+            if not args.no_ref_gpu:
+                ref_gpu = reference_gpu_arm(torch, oracle_scene, scene_desc, sets, ref_hits, frac, stream,
+                                            f"cuda:{local}")
             # the reference layout's bytes per ray on the same rays, beside this
             # build's (roofline.bytes_per_ray): a worse tree cannot raise the
             # roofline fraction unnoticed
@@ -666,6 +718,7 @@ def run_lrx(args):
                          "bytes_per_ray": round(tot_alg / rays_per_step, 1)},
             "cpu_baseline": cpu,
             "parity": parity,
+            "reference_gpu": ref_gpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
                     "api": ("lrx_trace_host_batches over the 3 sets (pinned host buffers)" if args.step_form == "batched"
@@ -675,6 +728,22 @@ def run_lrx(args):
             "gpu_launches_per_step": launches_per_step,
             "clocks": clk,
         }
+        if ws == 1 and not args.no_extras:
+            # the metric's second half, bounded: uneven batches (batched over
+            # plain with the same autotuned configs) and the serving loop
+            # (p50 / p99, batched over plain); outside the timed region
+            dev.clear()
+            for key, fn in (("batching", lambda: batching_line(args, 3)),
+                            ("serving", lambda: serving_line(args, [2000.0, 800.0], 1.0, budget_runs=False))):
+                t_x = time.perf_counter()
+                try:
+                    x = fn()
+                    cfg = {k: v for k, v in x["config"].items() if k != "autotuned"}
+                    line[key] = {"metric": x["metric"], "value": x["value"], "unit": x["unit"], **cfg,
+                                 "wall_s": round(time.perf_counter() - t_x, 1)}
+                except Exception as e:  # reported in the line; the headline stands
+                    line[key] = {"error": repr(e)[:500]}
+                log(f"[bench] {time.strftime('%H:%M:%S')} {key} done in {time.perf_counter() - t_x:.1f}s")
         print(json.dumps(line), flush=True)
     scene.close()
     d.close()
@@ -915,6 +984,15 @@ def device_random_rays(torch, n, extent, seed, device):
 
 
 def run_batching(args):
+    print(json.dumps(batching_line(args, args.steps)), flush=True)
+    return 0
+
+
+def batching_line(args, steps: int) -> dict:
+    """BASELINE config 4 (uneven batches over 8 scenes): one lrx_trace per
+    RayBuffer against one lrx_trace_batches call, eager and as replayed CUDA
+    graphs, each timed over `steps` repetitions with the same autotuned
+    per-scene configs (plus the plain form under the library defaults)."""
     import torch
 
     from luxcore_gb300 import lrx
@@ -949,11 +1027,11 @@ def run_batching(args):
             stream.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            for _ in range(args.steps):
+            for _ in range(steps):
                 plain()
             e1.record(stream)
         e1.synchronize()
-        return e0.elapsed_time(e1) / args.steps
+        return e0.elapsed_time(e1) / steps
 
     default_ms = timed_plain_default()
 
@@ -994,15 +1072,15 @@ def run_batching(args):
         return lambda: g.replay()
 
     res = {}
-    res["plain"] = timed(plain, args.steps)
+    res["plain"] = timed(plain, steps)
     plain_hits = [h.clone() for _, _, h, _, _ in items[:8]]
-    res["batched"] = timed(batched, args.steps)
+    res["batched"] = timed(batched, steps)
     same = all(torch.equal(a, b[2]) for a, b in zip(plain_hits, items[:8]))
-    res["plain_graph"] = timed(graphed(plain), args.steps)
+    res["plain_graph"] = timed(graphed(plain), steps)
     for _, _, h, _, _ in items[:8]:
         h.zero_()
     torch.cuda.synchronize()
-    res["batched_graph"] = timed(graphed(batched), args.steps)
+    res["batched_graph"] = timed(graphed(batched), steps)
     same = same and all(torch.equal(a, b[2]) for a, b in zip(plain_hits, items[:8]))
     for s in scenes:
         if s.device_status(st) != 0:
@@ -1011,7 +1089,7 @@ def run_batching(args):
     mrays["plain_default_config"] = round(total_rays / (default_ms / 1e3) / 1e6, 1)
     line = {
         "metric": "Mrays/s on uneven batches (batched queue kernel + CUDA graph vs one launch per RayBuffer)",
-        "value": mrays["batched_graph"], "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": 1,
+        "value": mrays["batched_graph"], "unit": UNIT, "n_gpus": 1, "steps": steps, "warmup": 1,
         "ms_per_step": round(res["batched_graph"][0], 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": f"{len(items)} batches log-uniform [1024, 2097152] rays over 8 scenes "
@@ -1025,8 +1103,10 @@ def run_batching(args):
                             "the batched form uses); plain_default_config: the library defaults, no autotune",
                    "results_equal_plain": bool(same), "autotuned": tuned},
     }
-    print(json.dumps(line), flush=True)
-    return 0
+    for s in scenes:
+        s.close()
+    del items
+    return line
 
 
 # ---------------------------------------------------------------------------
@@ -1068,6 +1148,45 @@ def serving_scenes(max_tris):
 
 
 def run_serving(args):
+    line = serving_line(args, args.serve_rates, args.serve_seconds, budget_runs=True)
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def wavefront_pools(torch, descs, extents, pool_n, device, seed):
+    """Per scene, the bounce (closest-hit) and shadow (any-hit) rays of a
+    PATHOCL-style wavefront path tracer over it (luxcore_gb300.pathocl,
+    1,048,576 tasks, camera outside the scene's cube looking in, one light
+    near its top), pool_n of each, cycled if the scene yields fewer."""
+    from luxcore_gb300 import lrx
+    from luxcore_gb300.pathocl import WavefrontPaths
+    pools = []
+    for k, (d, ext) in enumerate(zip(descs, extents)):
+        sc = lrx.Scene(d, treelet_passes=0)
+        wp = WavefrontPaths(sc, d, 1024, 1024, max_depth=4, eye=(0.5 * ext, -0.6 * ext, 0.8 * ext),
+                            look=(0.5 * ext, 0.5 * ext, 0.4 * ext), light=(0.45 * ext, 0.55 * ext, 0.95 * ext),
+                            seed=seed + k, device=device)
+        b, sh = wp.harvest(pool_n, pool_n)
+        torch.cuda.synchronize()
+        sc.close()
+        out = []
+        for r in (b, sh):
+            if r.shape[0] == 0:
+                raise RuntimeError(f"serving scene {k}: the wavefront produced no rays")
+            reps = (pool_n + r.shape[0] - 1) // r.shape[0]
+            out.append(r.repeat(reps, 1)[:pool_n].contiguous())
+        pools.append((out[0], out[1]))
+        del wp, b, sh
+    return pools
+
+
+def serving_line(args, rates, seconds: float, budget_runs: bool) -> dict:
+    """BASELINE config 5: 64 sessions over 12 scenes with Poisson arrivals at
+    each rate in `rates`, `seconds` each, batched (continuous batching) and
+    plain servers; with budget_runs also a scaled HBM budget that forces
+    evictions (with and without the blob cache).  Rays: the bounce and shadow
+    rays of a wavefront path tracer over each scene (--serve-rays wavefront)
+    or uniformly random rays (random)."""
     import torch
 
     from luxcore_gb300 import lrx
@@ -1078,12 +1197,17 @@ def run_serving(args):
     counts, descs, extents = serving_scenes(args.serve_max_tris)
     log(f"[serving] scenes {counts} generated in {time.perf_counter() - t0:.1f}s")
     pool_n = SERVE_SIZE_RANGE[1]
-    pools = []
-    for k, ext in enumerate(extents):
-        closest = device_random_rays(torch, pool_n, ext, W.BASE_SEED + 2000 + k, dev)
-        anyr = device_random_rays(torch, pool_n, ext, W.BASE_SEED + 3000 + k, dev)
-        anyr[:, 7] = torch.rand(pool_n, device=dev) * (0.5 * ext) + 0.05 * ext  # shadow-ray lengths
-        pools.append((closest, anyr))
+    t0 = time.perf_counter()
+    if args.serve_rays == "wavefront":
+        pools = wavefront_pools(torch, descs, extents, pool_n, dev, W.BASE_SEED + 2000)
+    else:
+        pools = []
+        for k, ext in enumerate(extents):
+            closest = device_random_rays(torch, pool_n, ext, W.BASE_SEED + 2000 + k, dev)
+            anyr = device_random_rays(torch, pool_n, ext, W.BASE_SEED + 3000 + k, dev)
+            anyr[:, 7] = torch.rand(pool_n, device=dev) * (0.5 * ext) + 0.05 * ext  # shadow-ray lengths
+            pools.append((closest, anyr))
+    log(f"[serving] {args.serve_rays} ray pools ready in {time.perf_counter() - t0:.1f}s")
     n_sess, k_buf = args.sessions, 4
     hits = [[torch.empty(pool_n * HIT_BYTES, dtype=torch.uint8, device=dev) for _ in range(k_buf)]
             for _ in range(n_sess)]
@@ -1108,7 +1232,7 @@ def run_serving(args):
                 c, _ = pools[k]
                 server.wait(server.submit(ids[k], c.data_ptr(), hits[0][0].data_ptr(), 1024, lrx.LRX_TRACE_CLOSEST))
         server.reset_stats()
-        sched = schedule(rate, args.serve_seconds, W.BASE_SEED + 77)
+        sched = schedule(rate, seconds, W.BASE_SEED + 77)
         step = [0] * n_sess
         inflight = [[None] * k_buf for _ in range(n_sess)]
         deferred = 0
@@ -1153,7 +1277,7 @@ def run_serving(args):
 
     full = 150 << 30
     res = {}
-    for rate in args.serve_rates:
+    for rate in rates:
         res[f"batched@{rate}"] = one_run(lrx.LRX_SERVE_BATCHED, full, rate)
         res[f"plain@{rate}"] = one_run(lrx.LRX_SERVE_PLAIN, full, rate)
     # scaled budget: ~40 % of the scene bytes, so scenes are evicted and rebuilt
@@ -1164,12 +1288,13 @@ def run_serving(args):
         probe_max = max(probe_max, s.info()["device_bytes"])
         s.close()
     small = int(max(probe_total * 0.4, probe_max * 1.25))  # the largest scene must still fit
-    low_rate = min(args.serve_rates)
-    res[f"batched@{low_rate}-budget40pct"] = one_run(lrx.LRX_SERVE_BATCHED, small, low_rate)
-    res[f"batched@{low_rate}-budget40pct-no-blob-cache"] = one_run(lrx.LRX_SERVE_BATCHED, small, low_rate,
-                                                                   cache=False)
-    head = res[f"batched@{args.serve_rates[0]}"]
-    plain = res[f"plain@{args.serve_rates[0]}"]
+    if budget_runs:
+        low_rate = min(rates)
+        res[f"batched@{low_rate}-budget40pct"] = one_run(lrx.LRX_SERVE_BATCHED, small, low_rate)
+        res[f"batched@{low_rate}-budget40pct-no-blob-cache"] = one_run(lrx.LRX_SERVE_BATCHED, small, low_rate,
+                                                                       cache=False)
+    head = res[f"batched@{rates[0]}"]
+    plain = res[f"plain@{rates[0]}"]
     line = {
         "metric": "served p50/p99 batch latency and Mrays/s (continuous batching vs plain launch)",
         "value": head["Mrays_per_s"], "unit": UNIT, "n_gpus": 1, "steps": 1, "warmup": 1,
@@ -1178,13 +1303,18 @@ def run_serving(args):
         "config": {"workload": f"{n_sess} sessions over 12 scenes ({min(counts)}-{max(counts)} triangles, 4 "
                                f"instanced), Poisson arrivals, sizes log-uniform {list(SERVE_SIZE_RANGE)}, "
                                f"bounce (closest) / shadow (any) alternating per session",
+                   "rays": ("bounce and shadow rays of a wavefront path tracer over each scene (1,048,576 tasks, "
+                            "depth 4)" if args.serve_rays == "wavefront" else "uniformly random rays"),
+                   "seconds_per_run": seconds,
                    "scene_bytes_total_GB": round(probe_total / 2 ** 30, 3), "budgets_GB": [150, round(small / 2 ** 30, 3)],
                    "runs": res,
-                   "p99_over_p50": round(head["p99_us"] / max(head["p50_us"], 1e-9), 2),
-                   "batched_over_plain_Mrays": round(head["Mrays_per_s"] / max(plain["Mrays_per_s"], 1e-9), 3)},
+                   "p99_over_p50": {k: round(v["p99_us"] / max(v["p50_us"], 1e-9), 2) for k, v in res.items()},
+                   "batched_over_plain_Mrays": {f"@{r}": round(res[f"batched@{r}"]["Mrays_per_s"] /
+                                                               max(res[f"plain@{r}"]["Mrays_per_s"], 1e-9), 3)
+                                                for r in rates}},
     }
-    print(json.dumps(line), flush=True)
-    return 0
+    del pools, hits
+    return line
 
 
 def main():
@@ -1198,6 +1328,10 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=2.0)
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[2000.0, 800.0])
     ap.add_argument("--serve-streams", type=int, default=4)
+    ap.add_argument("--serve-rays", default="wavefront", choices=["wavefront", "random"],
+                    help="serving ray pools: a wavefront path tracer's bounce and shadow rays, or random rays")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default workload: skip the bounded batching and serving runs after the main line's timing")
     ap.add_argument("--workload", default="heightfield", choices=["heightfield", "batching", "serving", "instanced",
                                                                       "motion", "pathocl"],
                     help="heightfield = the headline line; batching = uneven batches, plain vs queue kernel")
@@ -1209,6 +1343,8 @@ def main():
     ap.add_argument("--ref-fraction", type=int, default=4,
                     help="CPU legs trace every Nth ray of each set")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-ref-gpu", action="store_true",
+                    help="skip the reference's own CUDA kernel on this GPU (needs the CPU baseline's oracle)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer (lrx_trace_host) leg")
     ap.add_argument("--no-big-bounce", action="store_true", help="skip the 8 M-ray bounce launch")
     ap.add_argument("--sweep", action="store_true", help="also time other launch configurations")

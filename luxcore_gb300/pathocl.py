@@ -14,7 +14,9 @@ and a small AdvancePaths written with torch element-wise ops on the device
 stands in for the reference's shading kernels (which are out of scope):
 Lambertian surfaces of one albedo, one point light, a pinhole camera, a
 fixed depth limit, and finished paths restarted as new camera samples so
-the buffer stays full.  Only plain (non-instanced) objects are shaded.
+the buffer stays full.  Plain and instanced objects are shaded (an
+instance's normal is its mesh's, under the inverse transpose of the
+instance transform); motion-blurred objects are not.
 
 Task states:
   NEXT_VERTEX  the task's ray is a path ray (camera or bounce); after the
@@ -48,26 +50,33 @@ class WavefrontPaths:
                  light=(0.3, 0.7, 0.9), light_power: float = 1.0, albedo: float = 0.6, background: float = 0.2,
                  seed: int = 1, device: str = "cuda", stream=None):
         import torch
-        if desc.has_instances:
-            raise ValueError("the wavefront stand-in shades plain objects only")
+        if desc.has_motion:
+            raise ValueError("the wavefront stand-in does not shade motion-blurred objects")
         self.torch = torch
         self.scene, self.n = scene, width * height
         self.width, self.height, self.max_depth = width, height, max_depth
         self.device = device
         self.stream = stream if stream is not None else torch.cuda.current_stream()
         f32 = dict(dtype=torch.float32, device=device)
-        # geometry for the normals: every object's mesh, object order = meshIndex
-        verts, tris, base = [], [], 0
-        self.obj_tri_base = []
-        for mi, _m in desc.objects:
-            m = desc.meshes[mi]
+        # geometry for the normals: each mesh once; per object (in meshIndex
+        # order) its mesh's first triangle and the matrix that takes the mesh's
+        # normals to world space (identity for plain objects, the inverse
+        # transpose of the instance transform's 3x3 part for instances)
+        verts, tris, tri_base, vbase, tbase = [], [], [], 0, 0
+        for m in desc.meshes:
             verts.append(torch.from_numpy(np.ascontiguousarray(m.vertices, np.float32)))
-            tris.append(torch.from_numpy(np.ascontiguousarray(m.triangles, np.int64)) + base)
-            self.obj_tri_base.append(sum(t.shape[0] for t in tris[:-1]))
-            base += m.vertices.shape[0]
+            tris.append(torch.from_numpy(np.ascontiguousarray(m.triangles, np.int64)) + vbase)
+            tri_base.append(tbase)
+            vbase += m.vertices.shape[0]
+            tbase += m.triangles.shape[0]
         self.verts = torch.cat(verts).to(device)
         self.tris = torch.cat(tris).to(device)
-        self.obj_tri_base = torch.tensor(self.obj_tri_base, dtype=torch.int64, device=device)
+        nmat = np.tile(np.eye(3, dtype=np.float32), (len(desc.objects), 1, 1))
+        for k, (_mi, m) in enumerate(desc.objects):
+            if m is not None:
+                nmat[k] = np.linalg.inv(np.asarray(m, np.float64).reshape(4, 4)[:3, :3]).T.astype(np.float32)
+        self.obj_tri_base = torch.tensor([tri_base[mi] for mi, _m in desc.objects], dtype=torch.int64, device=device)
+        self.obj_nmat = torch.from_numpy(nmat).to(device)
         # camera frame
         e = np.array(eye, np.float64)
         fwd = np.array(look, np.float64) - e
@@ -154,10 +163,11 @@ class WavefrontPaths:
         hv = nv & hit
         t = self.hits[:, 0]
         o = self.rays[:, 0:3] + self.rays[:, 3:6] * torch.where(hv, t, zero)[:, None]
-        tid = (self.obj_tri_base[mesh.clamp(min=0).long()] + hits_i[:, 4].long()).clamp(0, self.tris.shape[0] - 1)
+        obj = mesh.clamp(min=0).long()
+        tid = (self.obj_tri_base[obj] + hits_i[:, 4].long()).clamp(0, self.tris.shape[0] - 1)
         tri = self.tris[tid]
         p0, p1, p2 = self.verts[tri[:, 0]], self.verts[tri[:, 1]], self.verts[tri[:, 2]]
-        nrm = torch.linalg.cross(p1 - p0, p2 - p0)
+        nrm = torch.einsum("nij,nj->ni", self.obj_nmat[obj], torch.linalg.cross(p1 - p0, p2 - p0))
         nrm = nrm / nrm.norm(dim=1, keepdim=True).clamp(min=1e-30)
         nrm = torch.where(((nrm * self.rays[:, 3:6]).sum(1) > 0)[:, None], -nrm, nrm)
         self.vertex = torch.where(hv[:, None], o, self.vertex)
@@ -197,6 +207,33 @@ class WavefrontPaths:
         for _ in range(count):
             self.trace()
             self.advance()
+
+    def harvest(self, n_bounce: int, n_shadow: int, max_iterations: int = 64):
+        """Runs iterations until it has seen n_bounce bounce rays (path rays
+        past the camera vertex) and n_shadow shadow rays (unmasked direct-
+        light rays), and returns the first of each as two (n, 12) float32
+        ray tensors on the device -- the rays a PATHOCL wavefront hands the
+        engine, for workloads that replay them.  Fewer come back if the
+        scene yields fewer within max_iterations (a scene the camera barely
+        sees)."""
+        torch = self.torch
+        bounce, shadow, nb, ns = [], [], 0, 0
+        for _ in range(max_iterations):
+            if nb >= n_bounce and ns >= n_shadow:
+                break
+            flags = self.rays.view(torch.int32)[:, 9]
+            live = (flags & W.RAY_FLAGS_MASKED) == 0
+            if nb < n_bounce:
+                b = self.rays[live & (self.state == NEXT_VERTEX) & (self.depth > 0)]
+                bounce.append(b.clone())
+                nb += b.shape[0]
+            if ns < n_shadow:
+                sh = self.rays[live & (self.state == DIRECT_LIGHT)]
+                shadow.append(sh.clone())
+                ns += sh.shape[0]
+            self.iterate()
+        cat = lambda parts, n: (torch.cat(parts)[:n] if parts else torch.zeros((0, RAY_WORDS), device=self.device))
+        return cat(bounce, n_bounce), cat(shadow, n_shadow)
 
     @property
     def traced(self) -> int:
