@@ -3,16 +3,23 @@
 # LuxCore source tree) for the CPU through oracle/refcl_prelude.h, into
 # oracle/_ref/, and stitches its CUDA BVH kernel text there for the GPU arm.
 # Test infrastructure only: the result pins the oracle (tests/golden/).
-# Usage: oracle/build_ref.sh [path to the LuxCore source tree]
+# Usage: oracle/build_ref.sh [--tree] [path to the LuxCore source tree]
 # The tree is the argument, else $LUXCORE_REFERENCE_TREE, else the copy this
 # project was developed beside.  Exits 3 (nothing built) when it is absent,
-# as on a machine that has only this repository.
+# as on a machine that has only this repository.  --tree only prints the
+# tree's path (tests that compile against its headers use it).
 set -e
+PRINT_TREE=0
+if [ "$1" = "--tree" ]; then PRINT_TREE=1; shift; fi
 REF="${1:-${LUXCORE_REFERENCE_TREE:-/root/reference}}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 if [ ! -f "$REF/include/luxrays/accelerators/bvh.cl" ]; then
 	echo "reference tree not found at $REF" >&2
 	exit 3
+fi
+if [ "$PRINT_TREE" = 1 ]; then
+	echo "$REF"
+	exit 0
 fi
 mkdir -p "$HERE/_ref"
 # bvh.cl (BVHKernel) and mbvh.cl (MBVHKernel with transforms and motion systems)
