@@ -503,7 +503,8 @@ def run_lrx(args):
     alt = {}
     if args.sweep:
         for bs, pp, var, rf in [(64, 8, 64, 8), (64, 8, 72, 8), (128, 8, 72, 8), (64, 0, 72, 8), (64, 8, 65, 8),
-                                (64, 8, 16, 0), (64, 8, 80, 8)]:
+                                (64, 8, 16, 0), (64, 8, 80, 8), (64, 8, 0xC0, 8), (64, 8, 0x440, 8),
+                                (64, 8, 0x840, 8), (64, 8, 0x410, 0), (64, 8, 0x810, 0)]:
             scene.set_trace_config(bs, pp, var, refill=rf)
             key = f"b{bs}-p{pp}-v{var}-r{rf}"
             alt[key] = {}

@@ -248,6 +248,10 @@ typedef struct lrx_trace_config {
 #define LRX_VARIANT_COMPACT 0x100u     /* with PERSISTENT: compact the indices of the unmasked rays
                                           first (stable) and trace only those -- for wavefront
                                           buffers where finished paths leave masked rays */
+#define LRX_VARIANT_SMEM_STACK16 0x400u /* the top 16 traversal-stack entries in shared memory
+                                          (ABI 3; blocks <= 256) */
+#define LRX_VARIANT_SMEM_STACK32 0x800u /* the top 32 entries in shared memory (ABI 3; blocks <= 128);
+                                          with either, deeper entries stay in local memory */
 
 /* Sets / reads the launch configuration lrx_trace uses for this scene.
  * No reference counterpart (the reference fixes 32-thread blocks,

@@ -775,8 +775,10 @@ lrx_status lrx_scene_set_trace_config(lrx_scene *s, const lrx_trace_config *c) {
 	lrx_trace_config in{};  // fields the caller's struct lacks stay 0
 	std::memcpy(&in, c, std::min<size_t>(c->struct_size, sizeof(in)));
 	const uint32_t bs = in.block_size ? in.block_size : kTraceBlock;
+	// shared-memory stacks deeper than 8 entries: at most 32 KB of shared memory per block
+	const uint32_t smem_depth = (uint32_t)smem_stack_depth(in.variant);
 	if (bs < 32 || bs > 512 || (bs & 31) || in.postpone > 32 || (in.variant & ~kVarAll) || in.modes > 3u ||
-			in.refill > 32) {
+			in.refill > 32 || (smem_depth > 8 && 8u * smem_depth * bs > 32768u)) {
 		set_error("lrx_scene_set_trace_config: value out of range");
 		return LRX_ERR_INVALID_ARGUMENT;
 	}
@@ -827,7 +829,8 @@ lrx_status lrx_scene_autotune(lrx_scene *s, const void *d_rays, uint32_t count, 
 	static const uint32_t kPostpone[] = {0, 8};
 	static const uint32_t kVariants[] = {0, LRX_VARIANT_STREAM_RAYS, LRX_VARIANT_SORT_RAYS, LRX_VARIANT_PERSISTENT,
 			LRX_VARIANT_PERSISTENT | LRX_VARIANT_STREAM_RAYS, LRX_VARIANT_PERSISTENT | LRX_VARIANT_SMEM_STACK,
-			LRX_VARIANT_PERSISTENT | LRX_VARIANT_SCENE_L2_KEEP};
+			LRX_VARIANT_PERSISTENT | LRX_VARIANT_SMEM_STACK16, LRX_VARIANT_PERSISTENT | LRX_VARIANT_SMEM_STACK32,
+			LRX_VARIANT_SORT_RAYS | LRX_VARIANT_SMEM_STACK16, LRX_VARIANT_PERSISTENT | LRX_VARIANT_SCENE_L2_KEEP};
 	for (uint32_t bs : kBlocks) {
 		for (uint32_t pp : kPostpone) {
 			for (uint32_t var : kVariants) {

@@ -137,8 +137,18 @@ constexpr uint32_t kVarSortOctantOnly = 0x20u;  // ... by direction octant only 
 constexpr uint32_t kVarPersistent = 0x40u;  // persistent warps with warp-level ray fetch
 constexpr uint32_t kVarSmemStack = 0x80u;  // top of the traversal stack in shared memory
 constexpr uint32_t kVarCompact = 0x100u;   // with kVarPersistent: trace only the unmasked rays, compacted first
-constexpr uint32_t kVarAll = 0x1ffu;       // every defined variant bit
 constexpr uint32_t kVarMotion = 0x200u;    // internal build bit: instance entry samples motion systems
+constexpr uint32_t kVarSmemStack16 = 0x400u;  // the top 16 stack entries in shared memory
+constexpr uint32_t kVarSmemStack32 = 0x800u;  // the top 32 stack entries in shared memory
+constexpr uint32_t kVarAll = 0xdffu;       // every public variant bit
+// The shared-memory stack bit of a variant (the deepest one asked for), or 0.
+constexpr uint32_t smem_stack_bits(uint32_t v) {
+	return (v & kVarSmemStack32) ? kVarSmemStack32 : (v & kVarSmemStack16) ? kVarSmemStack16 : (v & kVarSmemStack);
+}
+// Stack entries per thread in shared memory for a compile-time variant.
+constexpr int smem_stack_depth(uint32_t v) {
+	return (v & kVarSmemStack32) ? 32 : (v & kVarSmemStack16) ? 16 : (v & kVarSmemStack) ? 8 : 0;
+}
 constexpr uint32_t kSortMinRays = 32768;   // smaller batches are traced in caller order
 
 lrx_status launch_trace(const TraceArgs &a, cudaStream_t stream);

@@ -204,25 +204,27 @@ struct TravState {
 };
 // The traversal stack lives apart from TravState so that the state's scalars
 // stay in registers (a dynamically indexed member would put the whole
-// struct in local memory).  With LRX_VARIANT_SMEM_STACK its first
-// kSmemStack entries -- the top of a short stack, where nearly all pushes
-// and pops land -- are in shared memory instead, thread t's entry e at
-// top[e * blockDim.x] (consecutive lanes in consecutive 8-byte words, no
-// bank conflicts); deeper entries stay in local memory.
+// struct in local memory).  With a shared-memory stack (LRX_VARIANT_SMEM_STACK,
+// _SMEM_STACK16, _SMEM_STACK32) its first SD = 8, 16 or 32 entries -- the top
+// of a short stack, where nearly all pushes and pops land -- are in shared
+// memory instead, thread t's entry e at top[e * blockDim.x] (consecutive
+// lanes in consecutive 8-byte words, no bank conflicts); deeper entries, the
+// fallback when a walk goes deeper, stay in local memory.  SD trades
+// local-memory traffic against shared memory (8 * SD bytes per thread, taken
+// from the SM's L1) -- a per-scene choice of the autotuner.
 typedef uint2 TravStack[kStackSize];
-constexpr int kSmemStack = 8;
 struct StackTop {
 	uint2 *top;
 	uint32_t stride;
 };
-template <bool SMEM>
+template <int SD>
 __device__ __forceinline__ void stack_put(TravStack &st, StackTop t, int i, uint2 v) {
-	if (SMEM && i < kSmemStack) t.top[i * t.stride] = v;
+	if (SD > 0 && i < SD) t.top[i * t.stride] = v;
 	else st[i] = v;
 }
-template <bool SMEM>
+template <int SD>
 __device__ __forceinline__ uint2 stack_get(const TravStack &st, StackTop t, int i) {
-	if (SMEM && i < kSmemStack) return t.top[i * t.stride];
+	if (SD > 0 && i < SD) return t.top[i * t.stride];
 	return st[i];
 }
 
@@ -470,7 +472,7 @@ __device__ __forceinline__ int ray_begin(const TraceArgs &a, uint32_t i, bool st
 // instance entries raise, each by a bounded amount once per instance leaf
 // bit -- or consumes a stack entry or an instance bit, so a ray finishes in
 // a bounded number of trips.
-template <bool ANY, bool TWO_LEVEL, bool COUNT, bool MM3, bool SMEM = false, bool MOTION = false>
+template <bool ANY, bool TWO_LEVEL, bool COUNT, bool MM3, int SMEM = 0, bool MOTION = false>
 __device__ __forceinline__ bool ray_step(const TraceArgs &a, TravState &s, TravStack &stack, bool keep, uint64_t pol,
 		Counts &c, StackTop top = StackTop{nullptr, 0}) {
 #define LRX_PUSH(V)                                          \
@@ -604,7 +606,7 @@ template <bool ANY, bool TWO_LEVEL, bool COUNT, uint32_t CV>
 __device__ __forceinline__ void trace_ray(const TraceArgs &a, uint32_t tid, bool active, Counts &cnt,
 		StackTop top = StackTop{nullptr, 0}) {
 	constexpr bool MM3 = (CV & kVarMinMax3) != 0;
-	constexpr bool SMEM = (CV & kVarSmemStack) != 0;
+	constexpr int SMEM = smem_stack_depth(CV);
 	constexpr bool MOTION = (CV & kVarMotion) != 0;
 	if (!active) return;
 	const uint32_t i = a.order ? a.order[tid] : tid;  // the ray this thread traces
@@ -629,7 +631,7 @@ __device__ __forceinline__ void trace_ray(const TraceArgs &a, uint32_t tid, bool
 template <bool ANY, bool TWO_LEVEL, bool COUNT, uint32_t CV>
 __global__ void __launch_bounds__((CV & kVarOccupancy) ? 64 : (TWO_LEVEL ? 896 : 1024), (CV & kVarOccupancy) ? 20 : 0)
 k_trace(TraceArgs a) {
-	extern __shared__ uint2 s_stack_top[];  // kSmemStack entries per thread with SMEM_STACK, else empty
+	extern __shared__ uint2 s_stack_top[];  // smem_stack_depth(CV) entries per thread, else empty
 	const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
 	// this thread's ray is on its way into L1 while thread 0 looks up the
 	// launch's start: the block waits for the two at once
@@ -704,9 +706,9 @@ uint32_t next_launch_id() {
 template <bool ANY, bool TWO_LEVEL, uint32_t CV>
 __global__ void __launch_bounds__(kTraceBlock, TWO_LEVEL ? 7 : 8) k_trace_fetch(TraceArgs a, uint32_t refill) {
 	constexpr bool MM3 = (CV & kVarMinMax3) != 0;
-	constexpr bool SMEM = (CV & kVarSmemStack) != 0;
+	constexpr int SMEM = smem_stack_depth(CV);
 	constexpr bool MOTION = (CV & kVarMotion) != 0;
-	extern __shared__ uint2 s_stack_top[];  // kSmemStack entries per thread with SMEM_STACK, else empty
+	extern __shared__ uint2 s_stack_top[];  // SMEM entries per thread with a shared-memory stack, else empty
 	const StackTop top{s_stack_top + threadIdx.x, blockDim.x};
 	uint32_t *slot = g_queue[a.launch_id % kQueueSlots];
 	note_block_start();
@@ -1107,7 +1109,7 @@ lrx_status launch_trace_queue(const QueueParams &p, cudaStream_t st) {
 // most one ray per thread), all sharing one counter slot.
 template <bool ANY, bool TWO_LEVEL, uint32_t CV>
 static lrx_status launch_fetch(const TraceArgs &a, uint32_t bs, cudaStream_t st) {
-	const size_t smem_bytes = (CV & kVarSmemStack) ? sizeof(uint2) * kSmemStack * bs : 0;
+	const size_t smem_bytes = sizeof(uint2) * smem_stack_depth(CV) * bs;
 	static ResidentCache cache[kTraceBlock / 32];  // by block size 32, 64, 96, 128
 	int resident = 0;
 	const lrx_status rc = resident_blocks(cache[bs / 32 - 1], (const void *)k_trace_fetch<ANY, TWO_LEVEL, CV>, (int)bs,
@@ -1155,9 +1157,11 @@ lrx_status launch_trace(const TraceArgs &a_in, cudaStream_t st) {
 		// persistent warps with ray fetch; block size capped at kTraceBlock
 		const uint32_t fbs = std::min(bs, kTraceBlock);
 		const bool mm3 = (a.variant & kVarMinMax3) != 0;
-		const bool smem = (a.variant & kVarSmemStack) != 0;
-#define LRX_FETCH(A, T)                                                                           \
-	(smem ? launch_fetch<A, T, kVarSmemStack>(a, fbs, st)                                          \
+		const uint32_t smem = smem_stack_bits(a.variant);
+#define LRX_FETCH(A, T)                                                                                   \
+	(smem == kVarSmemStack32 ? launch_fetch<A, T, kVarSmemStack32>(a, fbs, st)                              \
+	 : smem == kVarSmemStack16 ? launch_fetch<A, T, kVarSmemStack16>(a, fbs, st)                            \
+	 : smem ? launch_fetch<A, T, kVarSmemStack>(a, fbs, st)                                                 \
 		  : (mm3 ? launch_fetch<A, T, kVarMinMax3>(a, fbs, st) : launch_fetch<A, T, 0u>(a, fbs, st)))
 		if (a.any_hit) return a.two_level ? LRX_FETCH(true, true) : LRX_FETCH(true, false);
 		return a.two_level ? LRX_FETCH(false, true) : LRX_FETCH(false, false);
@@ -1166,13 +1170,15 @@ lrx_status launch_trace(const TraceArgs &a_in, cudaStream_t st) {
 	// compile-time variants; the occupancy-bounded build only takes <= 64-thread blocks
 	uint32_t cv = a.variant & (kVarMinMax3 | kVarOccupancy);
 	if (bs > 64) cv &= ~kVarOccupancy;
-	if (a.variant & kVarSmemStack) cv = kVarSmemStack;  // a build of its own (no other compile-time bits)
+	if (smem_stack_bits(a.variant)) cv = smem_stack_bits(a.variant);  // builds of their own (no other compile-time bits)
 	if (cnt) cv = 0;
-	const size_t smem = cv == kVarSmemStack ? sizeof(uint2) * kSmemStack * bs : 0;
+	const size_t smem = sizeof(uint2) * (cv == kVarSmemStack32 ? 32 : cv == kVarSmemStack16 ? 16 : cv == kVarSmemStack ? 8 : 0) * bs;
 #define LRX_LAUNCH(A, T, C, V) k_trace<A, T, C, V><<<grid, bs, smem, st>>>(a)
 #define LRX_LAUNCH_V(A, T)                                         \
 	switch (cv) {                                                  \
 	case kVarSmemStack: LRX_LAUNCH(A, T, false, kVarSmemStack); break; \
+	case kVarSmemStack16: LRX_LAUNCH(A, T, false, kVarSmemStack16); break; \
+	case kVarSmemStack32: LRX_LAUNCH(A, T, false, kVarSmemStack32); break; \
 	case kVarMinMax3: LRX_LAUNCH(A, T, false, kVarMinMax3); break; \
 	case kVarOccupancy: LRX_LAUNCH(A, T, false, kVarOccupancy); break; \
 	case kVarMinMax3 | kVarOccupancy: LRX_LAUNCH(A, T, false, kVarMinMax3 | kVarOccupancy); break; \

@@ -34,6 +34,8 @@ LRX_VARIANT_SORT_OCTANT = 0x20
 LRX_VARIANT_PERSISTENT = 0x40
 LRX_VARIANT_SMEM_STACK = 0x80
 LRX_VARIANT_COMPACT = 0x100
+LRX_VARIANT_SMEM_STACK16 = 0x400
+LRX_VARIANT_SMEM_STACK32 = 0x800
 
 STATUS_NAMES = {0: "LRX_OK", 1: "LRX_ERR_INVALID_ARGUMENT", 2: "LRX_ERR_CUDA", 3: "LRX_ERR_OUT_OF_MEMORY",
                 4: "LRX_ERR_BUILD", 5: "LRX_ERR_DEVICE", 6: "LRX_ERR_NOT_SUPPORTED", 7: "LRX_ERR_BUDGET",
@@ -181,6 +183,20 @@ def load(path: str | None = None):
         L.lrx_scene_load.argtypes = [vp, ctypes.c_size_t, vp, ctypes.POINTER(vp)]
         _lib = L
         return L
+
+
+def rank_slice(count: int, rank: int, world_size: int) -> tuple:
+    """Ray range [begin, end) that replica `rank` of `world_size` traces of a
+    RayBuffer of `count` rays: contiguous, sizes differing by at most one,
+    in rank order -- so the ranks' hit slices concatenated in rank order are
+    the whole buffer's hits.  Each GPU holds a full scene replica and traces
+    its slice with no exchange between GPUs, as the reference gives each
+    intersection device its own tasks (src/slg/engines/pathocl/pathocl.cpp:217-247)."""
+    if world_size < 1 or not 0 <= rank < world_size or count < 0:
+        raise ValueError("bad rank / world size / count")
+    base, extra = divmod(count, world_size)
+    begin = rank * base + min(rank, extra)
+    return begin, begin + base + (1 if rank < extra else 0)
 
 
 def check(status: int):

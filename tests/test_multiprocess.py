@@ -61,3 +61,54 @@ def test_reference_arm_under_torchrun_two_ranks():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] == "port"
+
+
+def _slice_rank_main(rank, world, port, out):
+    os.environ.update({"RANK": str(rank), "WORLD_SIZE": str(world), "LOCAL_RANK": str(rank),
+                       "MASTER_ADDR": "127.0.0.1", "MASTER_PORT": str(port)})
+    sys.path.insert(0, ROOT)
+    import numpy as np
+    import torch.distributed as dist
+
+    from luxcore_gb300 import lrx
+    from luxcore_gb300 import workloads as W
+    from oracle import pyoracle as po
+    dist.init_process_group("gloo")
+    desc, rays = W.config1(n_tris=3000, n_rays=10007, seed=91)
+    b, e = lrx.rank_slice(rays.shape[0], rank, world)
+    hits, _ = po.OracleScene(desc).intersect(rays[b:e])   # this rank's replica, its slice only
+    parts = [None] * world
+    dist.all_gather_object(parts, (rank, b, e, hits.tobytes()))
+    dist.destroy_process_group()
+    if rank == 0:
+        full, _ = po.OracleScene(desc).intersect(rays)
+        got = np.frombuffer(b"".join(p[3] for p in sorted(parts)), W.HIT_DTYPE)
+        out.put((sorted((p[1], p[2]) for p in parts), bool(np.array_equal(got.view(np.uint8), full.view(np.uint8)))))
+
+
+def test_ray_slices_of_two_gloo_ranks_concatenate_to_the_whole_buffer():
+    import torch.multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = free_port()
+    procs = [ctx.Process(target=_slice_rank_main, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    ranges, equal = q.get(timeout=300)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert ranges == [(0, 5004), (5004, 10007)]
+    assert equal
+
+
+def test_rank_slice_covers_the_buffer():
+    from luxcore_gb300 import lrx
+    for n in (0, 1, 7, 1000, 1 << 20):
+        for w in (1, 2, 3, 8):
+            s = [lrx.rank_slice(n, r, w) for r in range(w)]
+            assert s[0][0] == 0 and s[-1][1] == n
+            assert all(a[1] == b[0] for a, b in zip(s, s[1:]))
+            assert max(e - b for b, e in s) - min(e - b for b, e in s) <= 1
+    with pytest.raises(ValueError):
+        lrx.rank_slice(10, 2, 2)

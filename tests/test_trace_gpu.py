@@ -27,14 +27,16 @@ KERNEL_CONFIGS = [(128, 0, 0), (64, 8, 0), (256, 24, 0), (64, 8, 0xF), (128, 8, 
                   (64, 8, 0x10), (32, 8, 0x1F), (64, 8, 0x30),
                   (64, 8, 0x40), (128, 0, 0x41, 1), (32, 8, 0x46, 32),
                   (64, 8, 0x50, 8), (64, 8, 0xC0, 8), (256, 8, 0x80), (64, 8, 0x90),
-                  (64, 8, 0x140, 8)]
+                  (64, 8, 0x140, 8), (64, 8, 0x440, 8), (128, 8, 0x840, 8), (64, 8, 0x410), (128, 0, 0x800)]
 KERNELS = pytest.mark.parametrize("kernel", KERNEL_CONFIGS,
                                   ids=["b128", "b64-p8", "b256-p24", "b64-p8-allvariants", "b128-p8-mm3-hints",
                                        "b64-p8-sorted", "b32-p8-sorted-all", "b64-p8-octsort",
                                        "b64-p8-persistent", "b128-persistent-refill1",
                                        "b32-p8-persistent-refill32-hints", "b64-p8-sorted-persistent-refill8",
                                        "b64-p8-persistent-smemstack", "b256-p8-smemstack", "b64-p8-sorted-smemstack",
-                                       "b64-p8-persistent-compact"])
+                                       "b64-p8-persistent-compact", "b64-p8-persistent-smemstack16",
+                                       "b128-p8-persistent-smemstack32", "b64-p8-sorted-smemstack16",
+                                       "b128-smemstack32"])
 
 
 def make_scene(desc, kernel=(64, 8, 0), **kw):
@@ -400,7 +402,10 @@ def test_trace_config_struct_versions(torch_cuda):
     assert L.lrx_scene_get_trace_config(s.handle, ctypes.byref(got)) == 0
     assert (got.struct_size, got.block_size, got.refill) == (20, 64, 77)  # nothing past 20 bytes written
     for bad in [lrx.TraceConfig(16, 64, 8, 0, 0, 0), lrx.TraceConfig(24, 64, 8, 0x80000000, 0, 0),
-                lrx.TraceConfig(24, 64, 8, 0x40, 0, 33), lrx.TraceConfig(24, 48, 8, 0, 0, 0)]:
+                lrx.TraceConfig(24, 64, 8, 0x40, 0, 33), lrx.TraceConfig(24, 48, 8, 0, 0, 0),
+                # a 32-entry shared-memory stack takes 256 B a thread: at most 128 threads a block
+                lrx.TraceConfig(24, 256, 8, lrx.LRX_VARIANT_SMEM_STACK32, 0, 0),
+                lrx.TraceConfig(24, 512, 8, lrx.LRX_VARIANT_SMEM_STACK16, 0, 0)]:
         assert L.lrx_scene_set_trace_config(s.handle, ctypes.byref(bad)) == lrx.LRX_ERR_INVALID_ARGUMENT
 
 
@@ -672,3 +677,23 @@ def test_scene_blob_round_trip(torch_cuda):
     for mode in (lrx.LRX_TRACE_CLOSEST, lrx.LRX_TRACE_ANY):
         ha, hb = gpu_trace(torch, a, anyr, mode), gpu_trace(torch, b, anyr, mode)
         assert np.array_equal(ha.view(np.uint32), hb.view(np.uint32))
+
+
+def test_replicas_tracing_slices_equal_one_replica(torch_cuda):
+    """Two scene replicas (as two GPUs would hold), each tracing its
+    lrx.rank_slice of one RayBuffer, one after the other on this GPU with no
+    exchange between them: the slices' hits concatenated in rank order equal
+    one replica tracing the whole buffer, byte for byte, and the oracle's."""
+    scene_desc, rays = W.config1(n_tris=30000, n_rays=200003, seed=93)
+    whole = gpu_trace(torch_cuda, lrx.Scene(scene_desc), rays)
+    parts = []
+    for rank in range(2):
+        b, e = lrx.rank_slice(rays.shape[0], rank, 2)
+        replica = lrx.Scene(scene_desc)
+        parts.append(gpu_trace(torch_cuda, replica, rays[b:e]))
+        replica.close()
+    got = np.concatenate(parts)
+    assert np.array_equal(got.view(np.uint8), whole.view(np.uint8))
+    oracle = po.OracleScene(scene_desc)
+    ref, _ = oracle.intersect(rays)
+    assert_parity(got, ref, oracle, rays)
