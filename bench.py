@@ -523,12 +523,17 @@ def run_lrx(args):
     builds = {}
     if args.build_sweep:
         # the same sets on trees built with 0-3 treelet passes, leaf size 2, and
-        # 4- and 6-wide nodes (default launch configs)
-        for passes, leaf, width in ((0, 3, 8), (1, 3, 8), (2, 3, 8), (3, 3, 8), (2, 2, 8), (2, 3, 4), (2, 3, 6)):
+        # 4- and 6-wide nodes, the 4-wide ones also in 64-byte node records
+        # (default launch configs)
+        C4 = lrx.LRX_NODES_COMPACT4
+        for passes, leaf, width, layout in ((0, 3, 8, 0), (1, 3, 8, 0), (2, 3, 8, 0), (3, 3, 8, 0), (2, 2, 8, 0),
+                                            (2, 3, 4, 0), (2, 3, 4, C4), (2, 2, 4, C4), (2, 3, 6, 0)):
             with torch.cuda.stream(stream):
-                sc = lrx.Scene(scene_desc, stream=st, treelet_passes=passes, leaf_max=leaf, node_width=width)
+                sc = lrx.Scene(scene_desc, stream=st, treelet_passes=passes, leaf_max=leaf, node_width=width,
+                               node_layout=layout)
             inf = sc.info()
-            row = {"build_ms": round(inf["build_ms"], 2), "wide_nodes": inf["node_count"], "depth": inf["max_depth"]}
+            row = {"build_ms": round(inf["build_ms"], 2), "wide_nodes": inf["node_count"], "depth": inf["max_depth"],
+                   "node_bytes": inf["node_bytes"]}
             for name, dr, dh, n, mode in dev:
                 cb = torch.zeros(4, dtype=torch.int64, device=f"cuda:{local}")
                 torch.cuda.synchronize()
@@ -545,7 +550,16 @@ def run_lrx(args):
                 row[name] = {"Mrays": round(n * 5 / (e0.elapsed_time(e1) / 1e3) / 1e6, 1),
                              "nodes_per_ray": round(nn / n, 2), "tris_per_ray": round(nt / n, 2)}
             sc.close()
-            builds[f"treelet{passes}-leaf{leaf}-width{width}"] = row
+            builds[f"treelet{passes}-leaf{leaf}-width{width}" + ("-nodes64" if layout else "")] = row
+        # the build lrx_scene_create_autotuned keeps for each set (its
+        # candidates: width 8 / 4 in 80-byte records, width 4 in 64-byte
+        # records, leaf 3 / 2; each at its tuned launch config), on the
+        # set's first 262,144 rays
+        for name, dr, dh, n, mode in dev:
+            with torch.cuda.stream(stream):
+                sc, opts, cfg = lrx.Scene.autotuned(scene_desc, dr.data_ptr(), min(n, 1 << 18), mode, st)
+            builds[f"autotuned-{name}"] = {**opts, **cfg}
+            sc.close()
         log(f"[bench] {time.strftime('%H:%M:%S')} build sweep done")
 
     if args.sweep:
@@ -1107,7 +1121,50 @@ def batching_line(args, steps: int) -> dict:
     for s in scenes:
         s.close()
     del items
+    if args.build_sweep:
+        line["config"]["build_sweep"] = batching_build_sweep(torch, lrx, tri_counts, extents, stream)
     return line
+
+
+def batching_build_sweep(torch, lrx, tri_counts, extents, stream) -> dict:
+    """Per scene of the uneven-batch workload: closest- and any-hit Mrays/s
+    of a 262,144-ray random sample under each candidate build of the
+    autotuner -- node width 8 or 4, 80- or 64-byte node records, 3 or 2
+    triangles per leaf -- at the library's default launch configs, and the
+    build lrx_scene_create_autotuned keeps for each mode (tuned launch
+    config included)."""
+    st = stream.cuda_stream
+    n = 1 << 18
+    C4 = lrx.LRX_NODES_COMPACT4
+    out = {}
+    for k, (tris, ext) in enumerate(zip(tri_counts.tolist(), extents.tolist())):
+        desc = W.SceneDesc([W.random_triangles(int(tris), W.BASE_SEED + 40 + k, extent=ext)])
+        rec = device_random_rays(torch, n, float(ext), W.BASE_SEED + 5000 + k, "cuda:0")
+        hits = torch.empty(n * HIT_BYTES, dtype=torch.uint8, device="cuda:0")
+        row = {}
+        for width, layout, leaf in ((8, 0, 3), (8, 0, 2), (4, 0, 3), (4, 0, 2), (4, C4, 3), (4, C4, 2)):
+            with torch.cuda.stream(stream):
+                sc = lrx.Scene(desc, stream=st, leaf_max=leaf, node_width=width, node_layout=layout)
+            r = {}
+            for mode in (lrx.LRX_TRACE_CLOSEST, lrx.LRX_TRACE_ANY):
+                sc.trace(rec.data_ptr(), hits.data_ptr(), n, mode, st)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(5):
+                    sc.trace(rec.data_ptr(), hits.data_ptr(), n, mode, st)
+                e1.record(stream)
+                e1.synchronize()
+                r["closest" if mode == lrx.LRX_TRACE_CLOSEST else "any"] = round(
+                    n * 5 / (e0.elapsed_time(e1) / 1e3) / 1e6, 1)
+            sc.close()
+            row[f"width{width}-leaf{leaf}" + ("-nodes64" if layout else "")] = r
+        for mode in (lrx.LRX_TRACE_CLOSEST, lrx.LRX_TRACE_ANY):
+            sc, opts, cfg = lrx.Scene.autotuned(desc, rec.data_ptr(), n, mode, st)
+            row["autotuned_" + ("closest" if mode == lrx.LRX_TRACE_CLOSEST else "any")] = {**opts, **cfg}
+            sc.close()
+        out[f"scene{k}-{int(tris)}tri"] = row
+        log(f"[batching] build sweep scene {k}: {row}")
+    return out
 
 
 # ---------------------------------------------------------------------------

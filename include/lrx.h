@@ -24,7 +24,7 @@
 extern "C" {
 #endif
 
-#define LRX_ABI_VERSION 3u
+#define LRX_ABI_VERSION 4u
 #define LRX_NULL_INDEX 0xffffffffu      /* luxrays_types.cl:21 */
 #define LRX_RAY_FLAGS_MASKED 0x1u       /* ray_types.cl:22 */
 
@@ -88,8 +88,20 @@ typedef struct lrx_build_opts {
 	uint32_t leaf_max;       /* triangles per leaf, 1..3 (default 3) */
 	uint32_t treelet_passes; /* treelet SAH restructuring passes (default 2, 0 = plain LBVH) */
 	uint32_t node_width;     /* children per wide node, 4..8 (0 = 8); narrower nodes give deeper
-	                            trees in the same 80-byte node format */
+	                            trees, by default in the same 80-byte node record */
+	/* Added in ABI 4 (a caller passing the 16-byte struct of ABI 1-3 gets
+	   LRX_NODES_WIDE8): */
+	uint32_t node_layout;    /* LRX_NODES_* -- the node record the scene's tree is stored in */
 } lrx_build_opts;
+
+/* Node records (lrx_build_opts.node_layout).  The 80-byte record holds up to
+   8 children; the 64-byte record up to 4 -- a quarter less to fetch per
+   visit and half the slab tests, for trees of node_width 4 over flat scenes
+   (a scene with objects, two-level, keeps the 80-byte record and is
+   rejected with LRX_ERR_NOT_SUPPORTED).  lrx_scene_create_autotuned times
+   both on its sample. */
+#define LRX_NODES_WIDE8 0u
+#define LRX_NODES_COMPACT4 1u
 
 typedef struct lrx_scene lrx_scene;
 
@@ -100,10 +112,10 @@ typedef struct lrx_scene_info {
 	uint32_t instance_count;
 	uint32_t blas_count;
 	uint32_t two_level;
-	uint64_t node_count;           /* 80-B wide nodes, all levels */
+	uint64_t node_count;           /* wide nodes, all levels */
 	uint64_t device_bytes;         /* device memory held by the scene */
 	uint32_t max_depth;            /* deepest wide-node path */
-	uint32_t reserved;
+	uint32_t node_bytes;           /* bytes per node record: 80, or 64 (LRX_NODES_COMPACT4; ABI 4) */
 	double build_ms;               /* device build time (excludes host->device copy) */
 } lrx_scene_info;
 
@@ -271,13 +283,16 @@ lrx_status lrx_scene_autotune(lrx_scene *scene, const void *d_sample_rays, uint3
 		void *stream, lrx_trace_config *chosen);
 
 /* Builds the scene under each candidate build -- node width {8, 4} x
- * triangles per leaf {3, 2}, with opts' treelet passes (opts nullable: 2) --
- * autotunes each candidate's launch configuration for `mode` on the sample
- * rays (lrx_scene_autotune), and keeps the candidate whose tuned
- * configuration traces the sample fastest; the others are destroyed.
- * chosen_opts / chosen_config (nullable) receive the kept build options and
- * launch configuration.  Synchronises `stream`.  Closest-hit results do not
- * depend on the choice (ties go to the lowest index in every tree).
+ * triangles per leaf {3, 2}, and for flat scenes also the 4-wide trees in
+ * the 64-byte node record (LRX_NODES_COMPACT4), with opts' treelet passes
+ * (opts nullable: 2) -- autotunes each candidate's launch configuration for
+ * `mode` on the sample rays (lrx_scene_autotune), and keeps the candidate
+ * whose tuned configuration traces the sample fastest; the others are
+ * destroyed.  chosen_opts / chosen_config (nullable) receive the kept build
+ * options (as many bytes as chosen_opts->struct_size holds, at least the
+ * 16 bytes of ABI 1-3) and launch configuration.  Synchronises `stream`.
+ * Closest-hit results do not depend on the choice (ties go to the lowest
+ * index in every tree).
  * No reference counterpart (the reference builds one fixed tree). */
 lrx_status lrx_scene_create_autotuned(const lrx_mesh_desc *meshes, uint32_t mesh_count,
 		const lrx_object_desc *objects, uint32_t object_count, const lrx_build_opts *opts,

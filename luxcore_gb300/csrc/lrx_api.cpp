@@ -405,9 +405,14 @@ lrx_status lrx_scene_create_motion(const lrx_mesh_desc *meshes, uint32_t mesh_co
 			return LRX_ERR_INVALID_ARGUMENT;
 		}
 		*out_scene = nullptr;
-		if (opts && opts->struct_size >= sizeof(lrx_build_opts) && opts->node_width &&
-				(opts->node_width < 4 || opts->node_width > 8)) {
+		const lrx_build_opts bopts = read_build_opts(opts);
+		if (bopts.node_width < 4 || bopts.node_width > 8) {
 			set_error("lrx_scene_create: node_width must be 0 or in [4, 8]");
+			return LRX_ERR_INVALID_ARGUMENT;
+		}
+		if (bopts.node_layout > LRX_NODES_COMPACT4 ||
+				(bopts.node_layout == LRX_NODES_COMPACT4 && bopts.node_width != 4)) {
+			set_error("lrx_scene_create: node_layout must be LRX_NODES_WIDE8, or LRX_NODES_COMPACT4 with node_width 4");
 			return LRX_ERR_INVALID_ARGUMENT;
 		}
 		int dev = 0;
@@ -459,19 +464,7 @@ lrx_status lrx_scene_create_motion(const lrx_mesh_desc *meshes, uint32_t mesh_co
 		s->motions = std::move(motion_list);
 		s->device = dev;
 		s->mesh_count = mesh_count;
-		s->opts.struct_size = sizeof(lrx_build_opts);
-		s->opts.leaf_max = 3;
-		s->opts.treelet_passes = 2;
-		s->opts.node_width = 8;
-		if (opts && opts->struct_size >= sizeof(lrx_build_opts)) {
-			if (opts->leaf_max) s->opts.leaf_max = std::min(3u, opts->leaf_max);
-			s->opts.treelet_passes = opts->treelet_passes;
-			if (opts->node_width) s->opts.node_width = opts->node_width;
-		}
-		if (s->opts.node_width < 4 || s->opts.node_width > 8) {
-			set_error("lrx_scene_create: node_width must be 0 or in [4, 8]");
-			return LRX_ERR_INVALID_ARGUMENT;
-		}
+		s->opts = bopts;
 		cudaStream_t st = (cudaStream_t)stream;
 		const auto t0 = std::chrono::steady_clock::now();
 
@@ -483,6 +476,10 @@ lrx_status lrx_scene_create_motion(const lrx_mesh_desc *meshes, uint32_t mesh_co
 			any_inst |= (objs[i].flags & LRX_OBJECT_INSTANCE) != 0;
 		}
 		s->two_level = any_inst;
+		if (any_inst && s->opts.node_layout == LRX_NODES_COMPACT4) {
+			set_error("lrx_scene_create: 64-byte node records (LRX_NODES_COMPACT4) need a flat scene");
+			return LRX_ERR_NOT_SUPPORTED;
+		}
 
 		std::vector<BlasBuild> builds;
 		builds.reserve(mesh_count + 1);
@@ -610,6 +607,7 @@ lrx_status lrx_scene_create_motion(const lrx_mesh_desc *meshes, uint32_t mesh_co
 		s->tlas_node_offset = node_off;
 		s->info.max_depth = max_depth;
 		s->info.node_count = node_off;
+		s->info.node_bytes = node_record_bytes(s->opts);
 		if (s->two_level) {
 			// instance records, then the motion intervals the traversal samples
 			size_t bytes = sizeof(InstRecord) * (tlas_prims + 1);
@@ -631,6 +629,12 @@ lrx_status lrx_scene_create_motion(const lrx_mesh_desc *meshes, uint32_t mesh_co
 			if (!s->blas.empty()) {
 				std::memcpy(s->bounds_lo, s->blas[0].lo, sizeof(s->bounds_lo));
 				std::memcpy(s->bounds_hi, s->blas[0].hi, sizeof(s->bounds_hi));
+			}
+			if (s->opts.node_layout == LRX_NODES_COMPACT4) {  // the tree in 64-byte records
+				DevBuf packed;
+				if ((rc = packed.alloc(sizeof(Node4) * ((size_t)node_off + 1))) != LRX_OK) return rc;
+				if ((rc = pack_nodes4(s->nodes.as<WideNode>(), packed.as<Node4>(), node_off, st)) != LRX_OK) return rc;
+				s->nodes = std::move(packed);
 			}
 		}
 		// scratch is kept only where instance updates need it
@@ -746,6 +750,7 @@ extern "C++" lrx_status lrx::trace_common(lrx_scene *s, const void *d_rays, void
 	a.root = s->root;
 	a.two_level = s->two_level ? 1u : 0u;
 	a.motion = s->motions.empty() ? 0u : 1u;
+	a.nodes4 = s->opts.node_layout == LRX_NODES_COMPACT4 ? 1u : 0u;
 	a.rays = d_rays;
 	a.hits = d_hits;
 	a.count = count;
@@ -875,12 +880,16 @@ lrx_status lrx_scene_create_autotuned(const lrx_mesh_desc *meshes, uint32_t mesh
 		return LRX_ERR_INVALID_ARGUMENT;
 	}
 	*out_scene = nullptr;
-	lrx_build_opts base{};
-	base.struct_size = sizeof(lrx_build_opts);
-	base.treelet_passes = 2;
-	if (opts && opts->struct_size >= sizeof(lrx_build_opts)) base.treelet_passes = opts->treelet_passes;
-	// candidate builds: node width x triangles per leaf
-	static const uint32_t kWidths[] = {8, 4};
+	lrx_build_opts base = read_build_opts(opts);  // its treelet passes; the rest is the candidates'
+	// candidate builds: (node width, node record) x triangles per leaf -- the
+	// 64-byte record only for flat scenes
+	bool flat = true;
+	for (uint32_t i = 0; objects && i < object_count; ++i) flat &= !(objects[i].flags & LRX_OBJECT_INSTANCE);
+	struct Shape {
+		uint32_t width, layout;
+	};
+	std::vector<Shape> shapes = {{8, LRX_NODES_WIDE8}, {4, LRX_NODES_WIDE8}};
+	if (flat) shapes.push_back({4, LRX_NODES_COMPACT4});
 	static const uint32_t kLeaves[] = {3, 2};
 	cudaStream_t st = (cudaStream_t)stream;
 	lrx_scene *best = nullptr;
@@ -890,10 +899,11 @@ lrx_status lrx_scene_create_autotuned(const lrx_mesh_desc *meshes, uint32_t mesh
 	lrx_status rc = LRX_OK;
 	void *hits = nullptr;
 	cudaEvent_t e0 = nullptr, e1 = nullptr;
-	for (uint32_t w : kWidths) {
+	for (const Shape &sh : shapes) {
 		for (uint32_t leaf : kLeaves) {
 			lrx_build_opts o = base;
-			o.node_width = w;
+			o.node_width = sh.width;
+			o.node_layout = sh.layout;
 			o.leaf_max = leaf;
 			lrx_scene *cand = nullptr;
 			if ((rc = lrx_scene_create(meshes, mesh_count, objects, object_count, &o, stream, &cand)) != LRX_OK) break;
@@ -944,7 +954,12 @@ lrx_status lrx_scene_create_autotuned(const lrx_mesh_desc *meshes, uint32_t mesh
 	}
 	cudaStreamSynchronize(st);
 	*out_scene = best;
-	if (chosen_opts) *chosen_opts = best_opts;
+	if (chosen_opts) {  // as many bytes as the caller's struct holds (ABI 1-3: no node_layout)
+		const size_t n = std::min<size_t>(std::max<size_t>(chosen_opts->struct_size, kBuildOptsAbi3Size),
+				sizeof(lrx_build_opts));
+		std::memcpy(chosen_opts, &best_opts, n);
+		chosen_opts->struct_size = (uint32_t)n;
+	}
 	if (chosen_config) {  // as many bytes as the caller's struct holds
 		const size_t n = chosen_config->struct_size >= sizeof(lrx_trace_config) ? sizeof(lrx_trace_config)
 				: offsetof(lrx_trace_config, refill);

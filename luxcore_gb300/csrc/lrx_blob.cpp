@@ -47,7 +47,7 @@ struct Hash64 {
 };
 
 constexpr char kBlobMagic[8] = {'L', 'R', 'X', 'S', 'C', 'E', 'N', 'E'};
-constexpr uint32_t kBlobVersion = 3;  // 3: the trace configs carry the failure bounds
+constexpr uint32_t kBlobVersion = 4;  // 3: the trace configs carry the failure bounds; 4: the node record
 
 struct BlobWriter {
 	unsigned char *p;  // null: only count
@@ -122,15 +122,11 @@ lrx_status lrx_scene_key(const lrx_mesh_desc *meshes, uint32_t mesh_count, const
 		if (o.flags & LRX_OBJECT_INSTANCE) h.words(o.transform, sizeof(o.transform));
 		if ((o.flags & LRX_OBJECT_INSTANCE) && (o.flags & LRX_OBJECT_HAS_INVERSE)) h.words(o.inverse, sizeof(o.inverse));
 	}
-	uint32_t leaf_max = 3, passes = 2, width = 8;  // the lrx_scene_create defaults
-	if (opts && opts->struct_size >= sizeof(lrx_build_opts)) {
-		if (opts->leaf_max) leaf_max = std::min(3u, opts->leaf_max);
-		passes = opts->treelet_passes;
-		if (opts->node_width) width = opts->node_width;
-	}
-	h.value(leaf_max);
-	h.value(passes);
-	if (width != 8) h.value(width);  // keys of default-width scenes as before
+	const lrx_build_opts o = read_build_opts(opts);  // over the lrx_scene_create defaults
+	h.value(o.leaf_max);
+	h.value(o.treelet_passes);
+	if (o.node_width != 8) h.value(o.node_width);  // keys of default-width scenes as before
+	if (o.node_layout != LRX_NODES_WIDE8) h.value(o.node_layout);  // and of 80-byte-record scenes
 	*key = h.h;
 	return LRX_OK;
 }
@@ -280,14 +276,16 @@ static lrx_status scene_from_blob(const void *blob, size_t bytes, cudaStream_t s
 			len[k] = r.value<uint64_t>();
 			arr[k] = r.take(len[k]);
 		}
-		if (!r.ok || r.n != r.size || len[0] % sizeof(WideNode) || len[1] % sizeof(TriRecord) ||
-				len[2] % 16 || s->obj_blas.size() != s->obj_flags.size() || s->obj_motion.size() != s->obj_flags.size() ||
-				(s->root != kNull && (uint64_t)s->root * sizeof(WideNode) >= len[0])) {
+		const uint64_t nb = node_record_bytes(s->opts);
+		if (!r.ok || r.n != r.size || s->opts.node_layout > LRX_NODES_COMPACT4 ||
+				(s->opts.node_layout == LRX_NODES_COMPACT4 && s->two_level) || len[0] % nb ||
+				len[1] % sizeof(TriRecord) || len[2] % 16 || s->obj_blas.size() != s->obj_flags.size() ||
+				s->obj_motion.size() != s->obj_flags.size() || (s->root != kNull && (uint64_t)s->root * nb >= len[0])) {
 			set_error("lrx_scene_load: malformed blob");
 			return LRX_ERR_INVALID_ARGUMENT;
 		}
 		lrx_status rc;
-		if ((rc = s->nodes.alloc(std::max<size_t>(len[0], sizeof(WideNode)))) != LRX_OK) return rc;
+		if ((rc = s->nodes.alloc(std::max<size_t>(len[0], nb))) != LRX_OK) return rc;
 		if ((rc = s->tris.alloc(std::max<size_t>(len[1], sizeof(TriRecord)))) != LRX_OK) return rc;
 		if (len[2] && (rc = s->insts.alloc(len[2])) != LRX_OK) return rc;
 		if ((rc = s->status.alloc(64)) != LRX_OK) return rc;

@@ -782,6 +782,55 @@ lrx_status launch_relocate_nodes(const WideNode *src, WideNode *dst, uint32_t n,
 	return LRX_OK;
 }
 
+// 80-byte record -> 64-byte record: the occupied slots (non-zero meta byte)
+// in slot order, each with its meta byte and its six quantised planes.  The
+// internal children keep their order, so child_base + rank still finds
+// them; a node with more than 4 children sets *err.
+__global__ void k_pack_nodes4(const WideNode *__restrict__ src, Node4 *__restrict__ dst, uint32_t n, uint32_t *err) {
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	const WideNode nd = src[i];
+	// per slot half (slots 0-3, 4-7): meta, then qlo x/y/z and qhi x/y/z
+	const uint32_t word[7][2] = {{nd.w[1].z, nd.w[1].w}, {nd.w[2].x, nd.w[2].y}, {nd.w[2].z, nd.w[2].w},
+			{nd.w[3].x, nd.w[3].y}, {nd.w[3].z, nd.w[3].w}, {nd.w[4].x, nd.w[4].y}, {nd.w[4].z, nd.w[4].w}};
+	uint32_t packed[7] = {0, 0, 0, 0, 0, 0, 0};
+	uint32_t p = 0;
+	for (int s = 0; s < 8; ++s) {
+		const uint32_t sh = (s & 3) * 8;
+		if (!((word[0][s >> 2] >> sh) & 0xffu)) continue;  // empty slot
+		if (p == 4) {
+			atomicOr(err, 1u);
+			return;
+		}
+		for (int k = 0; k < 7; ++k) packed[k] |= ((word[k][s >> 2] >> sh) & 0xffu) << (8 * p);
+		++p;
+	}
+	Node4 o;
+	o.w[0] = nd.w[0];
+	o.w[1] = make_uint4(nd.w[1].x, nd.w[1].y, packed[0], packed[1]);
+	o.w[2] = make_uint4(packed[2], packed[3], packed[4], packed[5]);
+	o.w[3] = make_uint4(packed[6], 0u, 0u, 0u);
+	dst[i] = o;
+}
+
+lrx_status pack_nodes4(const WideNode *src, Node4 *dst, uint32_t n, cudaStream_t st) {
+	if (!n) return LRX_OK;
+	DevBuf err;
+	lrx_status rc;
+	if ((rc = err.alloc(sizeof(uint32_t))) != LRX_OK) return rc;
+	LRX_CUDA(cudaMemsetAsync(err.ptr, 0, sizeof(uint32_t), st));
+	k_pack_nodes4<<<blocks_for(n, 256), 256, 0, st>>>(src, dst, n, err.as<uint32_t>());
+	LRX_CUDA(cudaGetLastError());
+	uint32_t h = 0;
+	LRX_CUDA(cudaMemcpyAsync(&h, err.ptr, sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+	LRX_CUDA(cudaStreamSynchronize(st));
+	if (h) {
+		set_error("64-byte node records hold at most 4 children (build with node_width 4)");
+		return LRX_ERR_BUILD;
+	}
+	return LRX_OK;
+}
+
 __global__ void k_triangle_records(uint32_t n, const uint32_t *__restrict__ order, const float *__restrict__ v,
 		const uint32_t *__restrict__ idx, const uint32_t *__restrict__ tri_object, uint32_t object_const,
 		TriRecord *__restrict__ dst) {

@@ -44,6 +44,20 @@ struct alignas(16) WideNode {
 };
 static_assert(sizeof(WideNode) == 80, "WideNode is 80 bytes");
 
+// The 64-byte record of a node with at most 4 children (LRX_NODES_COMPACT4):
+//   w[0] = as WideNode's (origin, exponents, imask over the 8 octant slots)
+//   w[1] = (child_base, tri_base, meta[0..3], qlo_x[0..3])
+//   w[2] = (qlo_y[0..3], qlo_z[0..3], qhi_x[0..3], qhi_y[0..3])
+//   w[3] = (qhi_z[0..3], 0, 0, 0)
+// Position p holds the p-th occupied slot of the 80-byte record in slot
+// order, with its meta byte unchanged: an internal child's still names its
+// octant slot s (bit 24 + s), and its node index is still child_base +
+// popc(imask & ((1 << s) - 1)).
+struct alignas(16) Node4 {
+	uint4 w[4];
+};
+static_assert(sizeof(Node4) == 64, "Node4 is 64 bytes");
+
 struct alignas(16) TriRecord {
 	float4 a, b, c;
 };

@@ -15,6 +15,7 @@
 namespace lrx {
 
 struct WideNode;
+struct Node4;
 struct TriRecord;
 struct InstRecord;
 
@@ -89,6 +90,11 @@ lrx_status launch_triangle_boxes(uint32_t n_tris, const float *d_verts, const ui
 lrx_status launch_relocate_nodes(const WideNode *src, WideNode *dst, uint32_t n,
 		uint32_t node_offset, uint32_t tri_offset, cudaStream_t stream);
 
+// Repacks a tree of at most 4 children per node from 80-byte records into
+// 64-byte ones (LRX_NODES_COMPACT4).  Synchronises `stream`; LRX_ERR_BUILD
+// if a node holds more than 4 children.
+lrx_status pack_nodes4(const WideNode *src, Node4 *dst, uint32_t n, cudaStream_t stream);
+
 // Writes triangle records for one mesh in leaf order.  d_tri_object, when
 // not null, holds (object index, triangle index) per triangle of a merged
 // mesh; otherwise every record gets object_const and its own index.
@@ -130,6 +136,7 @@ struct TraceArgs {
 	uint32_t refill = 0;           // persistent fetch: idle lanes that trigger a warp's claim (0 = 16)
 	const uint32_t *count_dev = nullptr;  // persistent fetch: rays to claim, read on the device (<= count)
 	uint32_t motion = 0;           // two-level scene with motion instances: the kVarMotion builds trace it
+	uint32_t nodes4 = 0;           // flat scene in 64-byte node records: the kVarNodes4 builds trace it
 };
 constexpr uint32_t kTraceBlock = 128;
 constexpr uint32_t kVarSortRays = 0x10u;   // reorder rays by octant + origin before tracing
@@ -140,6 +147,7 @@ constexpr uint32_t kVarCompact = 0x100u;   // with kVarPersistent: trace only th
 constexpr uint32_t kVarMotion = 0x200u;    // internal build bit: instance entry samples motion systems
 constexpr uint32_t kVarSmemStack16 = 0x400u;  // the top 16 stack entries in shared memory
 constexpr uint32_t kVarSmemStack32 = 0x800u;  // the top 32 stack entries in shared memory
+constexpr uint32_t kVarNodes4 = 0x1000u;   // internal build bit: the scene's nodes are 64-byte records
 constexpr uint32_t kVarAll = 0xdffu;       // every public variant bit
 // The shared-memory stack bit of a variant (the deepest one asked for), or 0.
 constexpr uint32_t smem_stack_bits(uint32_t v) {

@@ -68,10 +68,12 @@ static lrx_status side_streams(int dev, SideStreams **out) {
 }
 
 // A batch traced by a launch of its own rather than in the queue launch:
-// one on a scene with motion instances, or -- when the call holds at most
+// one on a scene with motion instances or with 64-byte node records (the
+// queue kernels trace neither), or -- when the call holds at most
 // kMaxDirectBatches batches of kDirectBatchRays rays or more -- one of those.
 static bool direct_batch(const lrx_batch &b, bool big_direct) {
-	return b.count != 0 && ((big_direct && b.count >= kDirectBatchRays) || !b.scene->motions.empty());
+	return b.count != 0 && ((big_direct && b.count >= kDirectBatchRays) || !b.scene->motions.empty() ||
+			b.scene->opts.node_layout == LRX_NODES_COMPACT4);
 }
 
 lrx_status lrx_trace_batches_ex(const lrx_batch *batches, uint32_t n_batches, void *stream,

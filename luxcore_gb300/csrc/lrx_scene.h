@@ -4,6 +4,7 @@
 // the public ABI.
 #pragma once
 
+#include <cstddef>
 #include <cstdint>
 #include <mutex>
 #include <vector>
@@ -24,6 +25,34 @@ struct Blas {
 // option existed: the 8-wide default).
 inline uint32_t node_width(const lrx_build_opts &o) {
 	return o.node_width ? o.node_width : 8u;
+}
+
+// Size of lrx_build_opts in ABI 1-3 (it ended after node_width).
+constexpr uint32_t kBuildOptsAbi3Size = (uint32_t)offsetof(lrx_build_opts, node_layout);
+
+// The build options a caller's struct (nullable) asks for, over the library
+// defaults -- 3 triangles per leaf, 2 treelet passes, 8-wide nodes in the
+// 80-byte record; fields beyond the caller's struct_size keep their
+// defaults, and a struct smaller than the ABI 1-3 one is ignored.
+inline lrx_build_opts read_build_opts(const lrx_build_opts *in) {
+	lrx_build_opts o{};
+	o.struct_size = sizeof(lrx_build_opts);
+	o.leaf_max = 3;
+	o.treelet_passes = 2;
+	o.node_width = 8;
+	o.node_layout = LRX_NODES_WIDE8;
+	if (in && in->struct_size >= kBuildOptsAbi3Size) {
+		if (in->leaf_max) o.leaf_max = in->leaf_max < 3u ? in->leaf_max : 3u;
+		o.treelet_passes = in->treelet_passes;
+		if (in->node_width) o.node_width = in->node_width;
+		if (in->struct_size >= sizeof(lrx_build_opts)) o.node_layout = in->node_layout;
+	}
+	return o;
+}
+
+// Bytes per node record of a scene's tree.
+inline uint32_t node_record_bytes(const lrx_build_opts &o) {
+	return o.node_layout == LRX_NODES_COMPACT4 ? (uint32_t)sizeof(Node4) : (uint32_t)sizeof(WideNode);
 }
 
 // Makes `dev` current for the guard's lifetime.

@@ -115,19 +115,22 @@ __device__ __forceinline__ float2 plane_pair(uint32_t w, float a, float b) {
 	return fma2(add2(q, make_float2(-8388608.f, -8388608.f)), make_float2(a, a), make_float2(b, b));
 }
 
-// Slab test of the 8 quantised child boxes.  t = q * (scale * idir) +
-// (origin - o) * idir; NaN plane distances (zero direction components) are
-// dropped by fminf/fmaxf, which only ever keeps a child.  A hit child adds
-// its meta bits to one 32-bit mask -- bits 0-23 its triangles, bit
-// 24 + (slot ^ octant) an internal child -- with the octant XOR and the bit
-// fields taken for four slots at a time from a meta word; empty slots
-// (meta 0) add nothing whatever their planes.
-template <bool MM3>
+// Slab test of the 8 quantised child boxes (N4: the 4 of a 64-byte
+// record).  t = q * (scale * idir) + (origin - o) * idir; NaN plane
+// distances (zero direction components) are dropped by fminf/fmaxf, which
+// only ever keeps a child.  A hit child adds its meta bits to one 32-bit
+// mask -- bits 0-23 its triangles, bit 24 + (slot ^ octant) an internal
+// child -- with the octant XOR and the bit fields taken for four children at
+// a time from a meta word; empty positions (meta 0) add nothing whatever
+// their planes.
+template <bool MM3, bool N4 = false>
 __device__ __forceinline__ NodeHits intersect_node(const WideNode *__restrict__ nodes, uint32_t idx,
 		const ActiveRay &r, float tmin, float tmax, bool keep, uint64_t pol) {
-	const uint4 *p = reinterpret_cast<const uint4 *>(nodes + idx);
+	constexpr int kWords = N4 ? 4 : 5;  // 16-byte words per record
+	const uint4 *p = reinterpret_cast<const uint4 *>(nodes) + (size_t)kWords * idx;
 	const uint4 w0 = ld_scene(p, keep, pol), w1 = ld_scene(p + 1, keep, pol), w2 = ld_scene(p + 2, keep, pol),
-			w3 = ld_scene(p + 3, keep, pol), w4 = ld_scene(p + 4, keep, pol);
+			w3 = ld_scene(p + 3, keep, pol);
+	const uint4 w4 = N4 ? make_uint4(0u, 0u, 0u, 0u) : ld_scene(p + 4, keep, pol);
 	NodeHits h;
 	h.child_base = w1.x;
 	h.tri_base = w1.y;
@@ -140,17 +143,22 @@ __device__ __forceinline__ NodeHits intersect_node(const WideNode *__restrict__ 
 	const float by = (__uint_as_float(w0.y) - r.o.y) * r.idir.y;
 	const float bz = (__uint_as_float(w0.z) - r.o.z) * r.idir.z;
 	const bool px = r.idir.x >= 0.f, py = r.idir.y >= 0.f, pz = r.idir.z >= 0.f;
-	// qlo_x = w2.xy, qlo_y = w2.zw, qlo_z = w3.xy, qhi_x = w3.zw, qhi_y = w4.xy, qhi_z = w4.zw
-	const uint32_t nx[2] = {px ? w2.x : w3.z, px ? w2.y : w3.w};
-	const uint32_t fx[2] = {px ? w3.z : w2.x, px ? w3.w : w2.y};
-	const uint32_t ny[2] = {py ? w2.z : w4.x, py ? w2.w : w4.y};
-	const uint32_t fy[2] = {py ? w4.x : w2.z, py ? w4.y : w2.w};
-	const uint32_t nz[2] = {pz ? w3.x : w4.z, pz ? w3.y : w4.w};
-	const uint32_t fz[2] = {pz ? w4.z : w3.x, pz ? w4.w : w3.y};
+	// 80-byte record: qlo_x = w2.xy, qlo_y = w2.zw, qlo_z = w3.xy, qhi_x = w3.zw, qhi_y = w4.xy,
+	// qhi_z = w4.zw, meta = w1.zw; 64-byte record: qlo_x = w1.w, qlo_y = w2.x, qlo_z = w2.y,
+	// qhi_x = w2.z, qhi_y = w2.w, qhi_z = w3.x, meta = w1.z (one word each, four children)
+	const uint32_t qlx[2] = {N4 ? w1.w : w2.x, w2.y}, qly[2] = {N4 ? w2.x : w2.z, w2.w};
+	const uint32_t qlz[2] = {N4 ? w2.y : w3.x, w3.y}, qhx[2] = {N4 ? w2.z : w3.z, w3.w};
+	const uint32_t qhy[2] = {N4 ? w2.w : w4.x, w4.y}, qhz[2] = {N4 ? w3.x : w4.z, w4.w};
+	const uint32_t nx[2] = {px ? qlx[0] : qhx[0], px ? qlx[1] : qhx[1]};
+	const uint32_t fx[2] = {px ? qhx[0] : qlx[0], px ? qhx[1] : qlx[1]};
+	const uint32_t ny[2] = {py ? qly[0] : qhy[0], py ? qly[1] : qhy[1]};
+	const uint32_t fy[2] = {py ? qhy[0] : qly[0], py ? qhy[1] : qly[1]};
+	const uint32_t nz[2] = {pz ? qlz[0] : qhz[0], pz ? qlz[1] : qhz[1]};
+	const uint32_t fz[2] = {pz ? qhz[0] : qlz[0], pz ? qhz[1] : qlz[1]};
 	// per meta word: bit position (internal slots XORed with the octant) and bit run, bytewise
-	uint32_t bpos[2], brun[2];
+	uint32_t bpos[2] = {0u, 0u}, brun[2] = {0u, 0u};
 #pragma unroll
-	for (int H = 0; H < 2; ++H) {
+	for (int H = 0; H < (N4 ? 1 : 2); ++H) {
 		const uint32_t m4 = H ? w1.w : w1.z;
 		const uint32_t inner4 = (m4 & (m4 << 1)) & 0x10101010u;  // bits 4 and 3 set: position >= 24
 		bpos[H] = (m4 ^ ((inner4 >> 4) * r.oct)) & 0x1f1f1f1fu;
@@ -175,7 +183,10 @@ __device__ __forceinline__ NodeHits intersect_node(const WideNode *__restrict__ 
 		if (tn0 <= tf0) hm |= ((brun[H] >> (8 * K)) & 0xffu) << ((bpos[H] >> (8 * K)) & 0xffu);      \
 		if (tn1 <= tf1) hm |= ((brun[H] >> (8 * K + 8)) & 0xffu) << ((bpos[H] >> (8 * K + 8)) & 0xffu); \
 	}
-	LRX_PAIR(0) LRX_PAIR(2) LRX_PAIR(4) LRX_PAIR(6)
+	LRX_PAIR(0) LRX_PAIR(2)
+	if (!N4) {
+		LRX_PAIR(4) LRX_PAIR(6)
+	}
 #undef LRX_PAIR
 	h.ihits = hm >> 24;
 	h.tmask = hm & 0x00ffffffu;
@@ -472,7 +483,7 @@ __device__ __forceinline__ int ray_begin(const TraceArgs &a, uint32_t i, bool st
 // instance entries raise, each by a bounded amount once per instance leaf
 // bit -- or consumes a stack entry or an instance bit, so a ray finishes in
 // a bounded number of trips.
-template <bool ANY, bool TWO_LEVEL, bool COUNT, bool MM3, int SMEM = 0, bool MOTION = false>
+template <bool ANY, bool TWO_LEVEL, bool COUNT, bool MM3, int SMEM = 0, bool MOTION = false, bool N4 = false>
 __device__ __forceinline__ bool ray_step(const TraceArgs &a, TravState &s, TravStack &stack, bool keep, uint64_t pol,
 		Counts &c, StackTop top = StackTop{nullptr, 0}) {
 #define LRX_PUSH(V)                                          \
@@ -496,7 +507,7 @@ __device__ __forceinline__ bool ray_step(const TraceArgs &a, TravState &s, TravS
 			return true;
 		}
 		if (COUNT) ++c.nodes;
-		const NodeHits h = intersect_node<MM3>(a.nodes, node, s.ray, s.mint, s.best_t, keep, pol);
+		const NodeHits h = intersect_node<MM3, N4>(a.nodes, node, s.ray, s.mint, s.best_t, keep, pol);
 		s.ng = make_uint2(h.child_base, (h.ihits << 24) | h.imask);
 		s.tg = make_uint2(h.tri_base, h.tmask);
 	} else {
@@ -608,6 +619,7 @@ __device__ __forceinline__ void trace_ray(const TraceArgs &a, uint32_t tid, bool
 	constexpr bool MM3 = (CV & kVarMinMax3) != 0;
 	constexpr int SMEM = smem_stack_depth(CV);
 	constexpr bool MOTION = (CV & kVarMotion) != 0;
+	constexpr bool N4 = (CV & kVarNodes4) != 0;
 	if (!active) return;
 	const uint32_t i = a.order ? a.order[tid] : tid;  // the ray this thread traces
 	const bool keep = (a.variant & kVarSceneEvictLast) != 0;
@@ -618,7 +630,7 @@ __device__ __forceinline__ void trace_ray(const TraceArgs &a, uint32_t tid, bool
 	const int k = ray_begin(a, i, stream, s);
 	if (k == kRayMasked) return;
 	if (k == kRayTraverse) {
-		while (!ray_step<ANY, TWO_LEVEL, COUNT, MM3, SMEM, MOTION>(a, s, stack, keep, pol, cnt, top)) {
+		while (!ray_step<ANY, TWO_LEVEL, COUNT, MM3, SMEM, MOTION, N4>(a, s, stack, keep, pol, cnt, top)) {
 		}
 		if (s.sp < 0) return;  // abandoned
 	}
@@ -708,6 +720,7 @@ __global__ void __launch_bounds__(kTraceBlock, TWO_LEVEL ? 7 : 8) k_trace_fetch(
 	constexpr bool MM3 = (CV & kVarMinMax3) != 0;
 	constexpr int SMEM = smem_stack_depth(CV);
 	constexpr bool MOTION = (CV & kVarMotion) != 0;
+	constexpr bool N4 = (CV & kVarNodes4) != 0;
 	extern __shared__ uint2 s_stack_top[];  // SMEM entries per thread with a shared-memory stack, else empty
 	const StackTop top{s_stack_top + threadIdx.x, blockDim.x};
 	uint32_t *slot = g_queue[a.launch_id % kQueueSlots];
@@ -750,7 +763,7 @@ __global__ void __launch_bounds__(kTraceBlock, TWO_LEVEL ? 7 : 8) k_trace_fetch(
 			if (drained) break;
 			continue;  // every lane idle: the next trip claims 32 rays
 		}
-		if (rid != kNull && ray_step<ANY, TWO_LEVEL, false, MM3, SMEM, MOTION>(a, s, stack, keep, pol, cnt, top)) {
+		if (rid != kNull && ray_step<ANY, TWO_LEVEL, false, MM3, SMEM, MOTION, N4>(a, s, stack, keep, pol, cnt, top)) {
 			if (s.sp >= 0) ray_write(a, rid, s, stream);  // an abandoned ray writes nothing
 			rid = kNull;
 		}
@@ -1158,18 +1171,19 @@ lrx_status launch_trace(const TraceArgs &a_in, cudaStream_t st) {
 		const uint32_t fbs = std::min(bs, kTraceBlock);
 		const bool mm3 = (a.variant & kVarMinMax3) != 0;
 		const uint32_t smem = smem_stack_bits(a.variant);
-#define LRX_FETCH(A, T)                                                                                   \
-	(smem == kVarSmemStack32 ? launch_fetch<A, T, kVarSmemStack32>(a, fbs, st)                              \
-	 : smem == kVarSmemStack16 ? launch_fetch<A, T, kVarSmemStack16>(a, fbs, st)                            \
-	 : smem ? launch_fetch<A, T, kVarSmemStack>(a, fbs, st)                                                 \
-		  : (mm3 ? launch_fetch<A, T, kVarMinMax3>(a, fbs, st) : launch_fetch<A, T, 0u>(a, fbs, st)))
-		if (a.any_hit) return a.two_level ? LRX_FETCH(true, true) : LRX_FETCH(true, false);
-		return a.two_level ? LRX_FETCH(false, true) : LRX_FETCH(false, false);
+#define LRX_FETCH(A, T, N)                                                                                \
+	(smem == kVarSmemStack32 ? launch_fetch<A, T, kVarSmemStack32 | N>(a, fbs, st)                          \
+	 : smem == kVarSmemStack16 ? launch_fetch<A, T, kVarSmemStack16 | N>(a, fbs, st)                        \
+	 : smem ? launch_fetch<A, T, kVarSmemStack | N>(a, fbs, st)                                             \
+		  : (mm3 ? launch_fetch<A, T, kVarMinMax3 | N>(a, fbs, st) : launch_fetch<A, T, N>(a, fbs, st)))
+		if (a.nodes4) return a.any_hit ? LRX_FETCH(true, false, kVarNodes4) : LRX_FETCH(false, false, kVarNodes4);
+		if (a.any_hit) return a.two_level ? LRX_FETCH(true, true, 0u) : LRX_FETCH(true, false, 0u);
+		return a.two_level ? LRX_FETCH(false, true, 0u) : LRX_FETCH(false, false, 0u);
 #undef LRX_FETCH
 	}
 	// compile-time variants; the occupancy-bounded build only takes <= 64-thread blocks
 	uint32_t cv = a.variant & (kVarMinMax3 | kVarOccupancy);
-	if (bs > 64) cv &= ~kVarOccupancy;
+	if (bs > 64 || a.nodes4) cv &= ~kVarOccupancy;  // (no occupancy-bounded builds for 64-byte records)
 	if (smem_stack_bits(a.variant)) cv = smem_stack_bits(a.variant);  // builds of their own (no other compile-time bits)
 	if (cnt) cv = 0;
 	const size_t smem = sizeof(uint2) * (cv == kVarSmemStack32 ? 32 : cv == kVarSmemStack16 ? 16 : cv == kVarSmemStack ? 8 : 0) * bs;
@@ -1184,13 +1198,25 @@ lrx_status launch_trace(const TraceArgs &a_in, cudaStream_t st) {
 	case kVarMinMax3 | kVarOccupancy: LRX_LAUNCH(A, T, false, kVarMinMax3 | kVarOccupancy); break; \
 	default: LRX_LAUNCH(A, T, false, 0u); break;                   \
 	}
-	if (a.any_hit) {
+#define LRX_LAUNCH_N4(A)                                                        \
+	switch (cv) {                                                               \
+	case kVarSmemStack: LRX_LAUNCH(A, false, false, kVarSmemStack | kVarNodes4); break; \
+	case kVarSmemStack16: LRX_LAUNCH(A, false, false, kVarSmemStack16 | kVarNodes4); break; \
+	case kVarSmemStack32: LRX_LAUNCH(A, false, false, kVarSmemStack32 | kVarNodes4); break; \
+	case kVarMinMax3: LRX_LAUNCH(A, false, false, kVarMinMax3 | kVarNodes4); break; \
+	default: LRX_LAUNCH(A, false, false, kVarNodes4); break;                    \
+	}
+	if (a.nodes4) {
+		if (a.any_hit) { if (cnt) LRX_LAUNCH(true, false, true, kVarNodes4); else LRX_LAUNCH_N4(true); }
+		else { if (cnt) LRX_LAUNCH(false, false, true, kVarNodes4); else LRX_LAUNCH_N4(false); }
+	} else if (a.any_hit) {
 		if (a.two_level) { if (cnt) LRX_LAUNCH(true, true, true, 0u); else LRX_LAUNCH_V(true, true); }
 		else { if (cnt) LRX_LAUNCH(true, false, true, 0u); else LRX_LAUNCH_V(true, false); }
 	} else {
 		if (a.two_level) { if (cnt) LRX_LAUNCH(false, true, true, 0u); else LRX_LAUNCH_V(false, true); }
 		else { if (cnt) LRX_LAUNCH(false, false, true, 0u); else LRX_LAUNCH_V(false, false); }
 	}
+#undef LRX_LAUNCH_N4
 #undef LRX_LAUNCH_V
 #undef LRX_LAUNCH
 	LRX_CUDA(cudaGetLastError());

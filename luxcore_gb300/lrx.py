@@ -23,6 +23,7 @@ LRX_TRACE_ANY = 1
 LRX_OBJECT_INSTANCE = 0x1
 LRX_OBJECT_HAS_INVERSE = 0x2
 LRX_ERR_INVALID_ARGUMENT = 1
+LRX_ERR_NOT_SUPPORTED = 6
 
 # lrx_trace_config.variant bits (include/lrx.h)
 LRX_VARIANT_MINMAX3 = 0x1
@@ -74,7 +75,12 @@ class ObjectDesc(ctypes.Structure):
 
 class BuildOpts(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_uint32), ("leaf_max", ctypes.c_uint32),
-                ("treelet_passes", ctypes.c_uint32), ("node_width", ctypes.c_uint32)]
+                ("treelet_passes", ctypes.c_uint32), ("node_width", ctypes.c_uint32),
+                ("node_layout", ctypes.c_uint32)]
+
+
+LRX_NODES_WIDE8 = 0      # 80-byte records, up to 8 children
+LRX_NODES_COMPACT4 = 1   # 64-byte records, up to 4 children (node_width 4, flat scenes)
 
 
 class TraceConfig(ctypes.Structure):
@@ -103,11 +109,11 @@ class SceneInfo(ctypes.Structure):
                 ("object_count", ctypes.c_uint32), ("instance_count", ctypes.c_uint32),
                 ("blas_count", ctypes.c_uint32), ("two_level", ctypes.c_uint32),
                 ("node_count", ctypes.c_uint64), ("device_bytes", ctypes.c_uint64),
-                ("max_depth", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("max_depth", ctypes.c_uint32), ("node_bytes", ctypes.c_uint32),
                 ("build_ms", ctypes.c_double)]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 _lib = None
@@ -403,12 +409,13 @@ def _mesh_descs(scene: W.SceneDesc, keep: list):
     return meshes
 
 
-def scene_key(scene: W.SceneDesc, leaf_max: int = 3, treelet_passes: int = 2, node_width: int = 8) -> int:
+def scene_key(scene: W.SceneDesc, leaf_max: int = 3, treelet_passes: int = 2, node_width: int = 8,
+              node_layout: int = LRX_NODES_WIDE8) -> int:
     """lrx_scene_key: content key of a scene's inputs and build options."""
     keep = []
     meshes = _mesh_descs(scene, keep)
     objs = _object_array(scene)
-    opts = BuildOpts(ctypes.sizeof(BuildOpts), leaf_max, treelet_passes, node_width)
+    opts = BuildOpts(ctypes.sizeof(BuildOpts), leaf_max, treelet_passes, node_width, node_layout)
     k = ctypes.c_uint64()
     check(load().lrx_scene_key(meshes, len(scene.meshes), objs, len(scene.objects), ctypes.byref(opts),
                                ctypes.byref(k)))
@@ -419,7 +426,7 @@ class Scene:
     """A device-resident scene (lrx_scene): meshes + objects of a SceneDesc."""
 
     def __init__(self, scene: W.SceneDesc | None, stream: int = 0, leaf_max: int = 3, treelet_passes: int = 2,
-                 node_width: int = 8, _handle=None):
+                 node_width: int = 8, node_layout: int = LRX_NODES_WIDE8, _handle=None):
         L = load()
         if _handle is not None:  # from_blob
             self.handle = _handle
@@ -428,7 +435,7 @@ class Scene:
         self._keep = []
         meshes = _mesh_descs(scene, self._keep)
         objs = _object_array(scene)
-        opts = BuildOpts(ctypes.sizeof(BuildOpts), leaf_max, treelet_passes, node_width)
+        opts = BuildOpts(ctypes.sizeof(BuildOpts), leaf_max, treelet_passes, node_width, node_layout)
         h = ctypes.c_void_p()
         if scene.has_motion:
             motions, n_motion = _motion_array(scene, self._keep)
@@ -465,16 +472,17 @@ class Scene:
     def autotuned(cls, scene: W.SceneDesc, d_rays: int, count: int, mode: int = LRX_TRACE_CLOSEST, stream: int = 0,
                   treelet_passes: int = 2):
         """lrx_scene_create_autotuned: the fastest of the candidate builds (node
-        width x leaf size) on the sample rays, each at its autotuned launch
-        configuration.  Returns (scene, build options, trace config) dicts."""
+        width and record x leaf size) on the sample rays, each at its
+        autotuned launch configuration.  Returns (scene, build options, trace
+        config) dicts."""
         if scene.has_motion:
             raise ValueError("autotuned builds take static scenes")
         L = load()
         keep = []
         meshes = _mesh_descs(scene, keep)
         objs = _object_array(scene)
-        opts = BuildOpts(ctypes.sizeof(BuildOpts), 0, treelet_passes, 0)
-        chosen = BuildOpts(ctypes.sizeof(BuildOpts), 0, 0, 0)
+        opts = BuildOpts(ctypes.sizeof(BuildOpts), 0, treelet_passes, 0, 0)
+        chosen = BuildOpts(ctypes.sizeof(BuildOpts), 0, 0, 0, 0)
         cfg = TraceConfig()
         cfg.struct_size = ctypes.sizeof(TraceConfig)
         h = ctypes.c_void_p()
@@ -483,7 +491,7 @@ class Scene:
                                            ctypes.byref(h), ctypes.byref(chosen), ctypes.byref(cfg)))
         sc = cls(scene, _handle=h)
         return (sc, {"leaf_max": chosen.leaf_max, "treelet_passes": chosen.treelet_passes,
-                     "node_width": chosen.node_width},
+                     "node_width": chosen.node_width, "node_layout": chosen.node_layout},
                 {"block_size": cfg.block_size, "postpone": cfg.postpone, "variant": cfg.variant, "refill": cfg.refill})
 
     @classmethod

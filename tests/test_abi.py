@@ -34,7 +34,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_abi_version_and_error_string(lib):
-    assert lib.lrx_abi_version() == 3
+    assert lib.lrx_abi_version() == 4
     assert isinstance(lib.lrx_last_error(), bytes)
 
 
@@ -43,7 +43,8 @@ def test_struct_layouts():
     assert W.RAY_DTYPE.fields["mint"][1] == 24 and W.RAY_DTYPE.fields["flags"][1] == 36
     assert ctypes.sizeof(lrx.MeshDesc) == 24
     assert ctypes.sizeof(lrx.ObjectDesc) == 136
-    assert ctypes.sizeof(lrx.BuildOpts) == 16
+    assert ctypes.sizeof(lrx.BuildOpts) == 20  # ABI 4: + node_layout
+    assert ctypes.sizeof(lrx.SceneInfo) == 64
     assert ctypes.sizeof(lrx.TraceConfig) == 32  # ABI 3: + max_visits, deadline_us
 
 
@@ -53,6 +54,10 @@ def test_variant_constants_match_the_header():
     assert defs, "no variant defines parsed"
     for name, val in defs.items():
         assert getattr(lrx, name) == int(val, 16), name
+    nodes = dict(re.findall(r"#define (LRX_NODES_[A-Z0-9_]+) ([0-9]+)u", src))
+    assert set(nodes) == {"LRX_NODES_WIDE8", "LRX_NODES_COMPACT4"}
+    for name, val in nodes.items():
+        assert getattr(lrx, name) == int(val), name
 
 
 def test_null_arguments_are_rejected_without_a_device(lib):
@@ -75,6 +80,16 @@ def test_bad_node_width_is_rejected_without_a_device(lib):
         opts = lrx.BuildOpts(ctypes.sizeof(lrx.BuildOpts), 3, 2, w)
         assert lib.lrx_scene_create(None, 0, None, 0, ctypes.byref(opts), None, ctypes.byref(h)) == 1
         assert b"node_width" in lib.lrx_last_error()
+    # 64-byte records take 4-wide trees; an unknown record is refused
+    for w, layout in ((8, lrx.LRX_NODES_COMPACT4), (5, lrx.LRX_NODES_COMPACT4), (4, 2)):
+        opts = lrx.BuildOpts(ctypes.sizeof(lrx.BuildOpts), 3, 2, w, layout)
+        assert lib.lrx_scene_create(None, 0, None, 0, ctypes.byref(opts), None, ctypes.byref(h)) == 1
+        assert b"node_layout" in lib.lrx_last_error()
+    # a caller of ABI 1-3 passes the 16-byte struct: its options are read,
+    # node_layout is not (a bad width is still refused)
+    opts = lrx.BuildOpts(16, 3, 2, 9, lrx.LRX_NODES_COMPACT4)
+    assert lib.lrx_scene_create(None, 0, None, 0, ctypes.byref(opts), None, ctypes.byref(h)) == 1
+    assert b"node_width" in lib.lrx_last_error()
 
 
 def test_package_has_no_cpu_fallback():
