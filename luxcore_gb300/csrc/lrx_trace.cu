@@ -487,17 +487,28 @@ __device__ __forceinline__ int ray_begin(const TraceArgs &a, uint32_t i, bool st
 // lanes than `postpone` still hold rays.  Triangle groups are then tested at
 // once: deferring them could not gather `postpone` lanes any more, and only
 // adds trips and delays the shrinking of t (bounce rays -0.7 % launch time).
+//
+// No path returns before the node test or the triangle loop: a push past
+// the stack's end is dropped and counted, and the stack and visit bounds are
+// checked once, at the end of the trip (before any pop, so a dropped entry
+// is never read).  An early return on those never-taken paths would leave
+// the lanes that pushed and those that did not without a point to
+// reconverge before the node test, which the warp then ran twice.
 template <bool ANY, bool TWO_LEVEL, bool COUNT, bool MM3, int SMEM = 0, bool MOTION = false, bool N4 = false>
 __device__ __forceinline__ bool ray_step(const TraceArgs &a, TravState &s, TravStack &stack, bool keep, uint64_t pol,
 		Counts &c, StackTop top = StackTop{nullptr, 0}, bool sparse = false) {
-#define LRX_PUSH(V)                                          \
-	{                                                        \
-		if (s.sp >= kStackSize) {                            \
-			atomicOr(a.status, kStatusStackOverflow);        \
-			s.sp = -1;                                       \
-			return true;                                     \
-		}                                                    \
-		stack_put<SMEM>(stack, top, s.sp++, (V));            \
+#define LRX_PUSH(V)                                                     \
+	{                                                                   \
+		if (s.sp < kStackSize) stack_put<SMEM>(stack, top, s.sp, (V));  \
+		++s.sp;                                                         \
+	}
+	// the trip's bounds: a stack that overflowed, or the visit budget spent,
+	// abandons the ray (status word bit, no hit written)
+#define LRX_BOUNDS()                                                                              \
+	if (s.sp > kStackSize || s.visits > a.visit_limit) {                                         \
+		atomicOr(a.status, s.sp > kStackSize ? kStatusStackOverflow : kStatusVisitLimit);        \
+		s.sp = -1;                                                                               \
+		return true;                                                                             \
 	}
 	if (s.ng.y > 0x00ffffffu) {
 		const uint32_t j = __ffs(s.ng.y >> 24) - 1;
@@ -505,11 +516,7 @@ __device__ __forceinline__ bool ray_step(const TraceArgs &a, TravState &s, TravS
 		const uint32_t sl = j ^ s.ray.oct;
 		const uint32_t node = s.ng.x + __popc(s.ng.y & ((1u << sl) - 1u) & 0xffu);
 		if (s.ng.y > 0x00ffffffu) LRX_PUSH(s.ng);
-		if (++s.visits > a.visit_limit) {
-			atomicOr(a.status, kStatusVisitLimit);
-			s.sp = -1;
-			return true;
-		}
+		++s.visits;
 		if (COUNT) ++c.nodes;
 		const NodeHits h = intersect_node<MM3, N4>(a.nodes, node, s.ray, s.mint, s.best_t, keep, pol);
 		s.ng = make_uint2(h.child_base, (h.ihits << 24) | h.imask);
@@ -544,6 +551,7 @@ __device__ __forceinline__ bool ray_step(const TraceArgs &a, TravState &s, TravS
 			s.inst_sp = s.sp;
 			s.ng = info.x == kNull ? make_uint2(0u, 0u) : make_uint2(info.x, (1u << (24 + s.ray.oct)) | 1u);
 			s.tg = make_uint2(0u, 0u);
+			LRX_BOUNDS()
 			return false;
 		}
 	} else {
@@ -584,6 +592,7 @@ __device__ __forceinline__ bool ray_step(const TraceArgs &a, TravState &s, TravS
 			}
 		}
 	}
+	LRX_BOUNDS()
 	if (s.ng.y <= 0x00ffffffu) {
 		if (TWO_LEVEL && s.inst_sp == s.sp) {  // this instance's BLAS is exhausted
 			s.inst_sp = -1;
@@ -594,6 +603,7 @@ __device__ __forceinline__ bool ray_step(const TraceArgs &a, TravState &s, TravS
 		s.ng = stack_get<SMEM>(stack, top, --s.sp);
 	}
 	return false;
+#undef LRX_BOUNDS
 #undef LRX_PUSH
 }
 
