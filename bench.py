@@ -175,7 +175,7 @@ def load_peaks():
 # the rays of the launch; the capture's command and table are in
 # profiles/trace_heightfield_ncu.md).  A constant of that capture, not a
 # figure of this run: the line says so in roofline.traffic_source.
-TRAFFIC_PER_RAY = {"primary": 153.6, "bounce": 297.3, "shadow": 197.6}
+TRAFFIC_PER_RAY = {"primary": 154.1, "bounce": 297.3, "shadow": 198.2}
 TRAFFIC_SOURCE = ("ncu capture of the traversal launches of one step (profiles/trace_heightfield_ncu.md), "
                   "not this run; DRAM bytes per launch averaged over the three sets")
 
@@ -749,7 +749,7 @@ def run_lrx(args):
             # (p50 / p99, batched over plain); outside the timed region
             dev.clear()
             for key, fn in (("batching", lambda: batching_line(args, 3)),
-                            ("serving", lambda: serving_line(args, [2000.0, 800.0], 1.0, budget_runs=False))):
+                            ("serving", lambda: serving_line(args, [2000.0, 800.0], 2.0, budget_runs=False))):
                 t_x = time.perf_counter()
                 try:
                     x = fn()
