@@ -1,9 +1,9 @@
 // GPU BVH builder: 63-bit Morton codes -> radix sort -> bottom-up LBVH
 // (one thread per leaf climbing with an atomic per internal node, the
 // agglomerative formulation of Apetrei 2014 over the Karras 2012 ordering)
-// -> optional treelet restructuring -> greedy top-down collapse into 8-wide
-// nodes with outward-rounded 8-bit child boxes (the compressed wide BVH of
-// Ylitie, Karras and Laine 2017).
+// -> optional treelet restructuring -> SAH-optimal top-down collapse into
+// 8-wide nodes with outward-rounded 8-bit child boxes (the compressed wide
+// BVH of Ylitie, Karras and Laine 2017).
 //
 // Replaces the reference's CPU builders (src/luxrays/core/bvh/
 // bvhclassicbuild.cpp:124-233, bvhembreebuild.cpp:218-357): any correct BVH
@@ -350,6 +350,98 @@ __global__ void __launch_bounds__(128) k_treelet(uint32_t n, const uint32_t *__r
 }
 
 // ---------------------------------------------------------------------------
+// Which binary nodes become wide nodes: the SAH-optimal collapse of Ylitie,
+// Karras and Laine 2017 (section 3.1), by dynamic programming bottom-up over
+// the binary tree.  C(x, i) is the least cost of covering x's subtree with
+// at most i roots -- each root a leaf slot (<= leaf_max primitives) or a wide
+// node of its own:
+//   C(x, 1) = kWideTri * A(x) * count(x)      if count(x) <= leaf_max
+//           = kWideNode * A(x) + D(x, width)  otherwise (x is a wide node)
+//   D(x, j) = min over k in [1, j-1] of C(left, k) + C(right, j - k)
+//   C(x, i) = min(C(x, 1), D(x, i))           for i >= 2
+// and a primitive costs kWideTri * its area for any i.  Per node the pass
+// stores C(x, 1..8) and a decision word: byte 0 the k of D(x, width) (how
+// a wide node at x spreads its slots over its two subtrees), byte i-1 for
+// i >= 2 the k of D(x, i), or 0 when x itself is the cheaper single root.
+// A wide node test takes about four times the instructions of a triangle
+// test, but runs on about eight times as many lanes of a warp (triangle
+// groups are small and ragged): per ray the two cost about the same, and
+// weights of 1 : 1 gave the fastest trees on the heightfield's three ray sets
+// (1 : 0.25 and 1 : 0.5 left more triangles per leaf and ran 1.4 % and 0.4 %
+// slower).
+// ---------------------------------------------------------------------------
+
+constexpr float kWideNode = 1.0f, kWideTri = 1.0f;
+
+__device__ __forceinline__ void wide_child_costs(uint32_t ref, const uint32_t *__restrict__ sorted,
+		const float4 *__restrict__ plo, const float4 *__restrict__ phi, const float4 *wcost, float c[8]) {
+	if (ref & kLeafFlag) {
+		const uint32_t p = sorted[ref & ~kLeafFlag];
+		const float4 a = plo[p], b = phi[p];
+		const float v = kWideTri * box_area(make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z));
+#pragma unroll
+		for (int k = 0; k < 8; ++k) c[k] = v;
+	} else {
+		const float4 u = __ldcg(&wcost[2 * ref]), w = __ldcg(&wcost[2 * ref + 1]);
+		c[0] = u.x; c[1] = u.y; c[2] = u.z; c[3] = u.w;
+		c[4] = w.x; c[5] = w.y; c[6] = w.z; c[7] = w.w;
+	}
+}
+
+__global__ void __launch_bounds__(128) k_wide_cost(uint32_t n, const uint32_t *__restrict__ sorted,
+		const float4 *__restrict__ plo, const float4 *__restrict__ phi, const uint32_t *bchild, const float4 *bn_lo,
+		const float4 *bn_hi, const uint2 *bmeta, const uint32_t *lparent, uint32_t *visits, uint32_t leaf_max,
+		uint32_t width, float4 *wcost, uint2 *wdec) {
+	const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+	if (i >= n) return;
+	const uint32_t *meta = reinterpret_cast<const uint32_t *>(bmeta);  // [2k] leaf count, [2k + 1] parent
+	uint32_t node = __ldcg(&lparent[i]);
+	// each step moves to the parent, so the climb ends within n steps
+	for (uint32_t step = 0; step < n && node != kNull; ++step) {
+		__threadfence();
+		if (atomicAdd(&visits[node], 1u) == 0u) return;  // the sibling subtree's thread continues
+		__threadfence();
+		float cl[8], cr[8];
+		wide_child_costs(__ldcg(&bchild[2 * node]), sorted, plo, phi, wcost, cl);
+		wide_child_costs(__ldcg(&bchild[2 * node + 1]), sorted, plo, phi, wcost, cr);
+		const float4 lo4 = __ldcg(&bn_lo[node]), hi4 = __ldcg(&bn_hi[node]);
+		const float area = box_area(make_float3(lo4.x, lo4.y, lo4.z), make_float3(hi4.x, hi4.y, hi4.z));
+		const uint32_t count = __ldcg(&meta[2 * node]);
+		float dist[9];
+		uint32_t split[9];
+		for (uint32_t j = 2; j <= width; ++j) {
+			float best = INFINITY;
+			uint32_t bk = 1;
+			for (uint32_t k = 1; k < j; ++k) {
+				const float c = cl[k - 1] + cr[j - k - 1];
+				if (c < best) {
+					best = c;
+					bk = k;
+				}
+			}
+			dist[j] = best;
+			split[j] = bk;
+		}
+		const float c1 = count <= leaf_max ? kWideTri * area * (float)count : kWideNode * area + dist[width];
+		float c[8];
+		uint32_t dec[8];
+		c[0] = c1;
+		dec[0] = split[width];
+		for (uint32_t k = 2; k <= 8; ++k) {
+			const uint32_t j = k <= width ? k : width;
+			const bool use = dist[j] < c1;
+			c[k - 1] = use ? dist[j] : c1;
+			dec[k - 1] = use ? split[j] : 0u;
+		}
+		__stcg(&wcost[2 * node], make_float4(c[0], c[1], c[2], c[3]));
+		__stcg(&wcost[2 * node + 1], make_float4(c[4], c[5], c[6], c[7]));
+		__stcg(&wdec[node], make_uint2(dec[0] | dec[1] << 8 | dec[2] << 16 | dec[3] << 24,
+				dec[4] | dec[5] << 8 | dec[6] << 16 | dec[7] << 24));
+		node = __ldcg(&meta[2 * node + 1]);
+	}
+}
+
+// ---------------------------------------------------------------------------
 // Collapse to 8-wide quantised nodes
 // ---------------------------------------------------------------------------
 
@@ -388,7 +480,7 @@ __global__ void __launch_bounds__(128) k_collapse(const uint2 *__restrict__ item
 		const float4 *__restrict__ bn_lo, const float4 *__restrict__ bn_hi, const uint2 *__restrict__ bmeta,
 		const uint32_t *__restrict__ sorted, const float4 *__restrict__ plo, const float4 *__restrict__ phi,
 		uint32_t leaf_max, uint32_t width, WideNode *__restrict__ wnodes, uint32_t *__restrict__ prim_order,
-		uint32_t *counters, uint32_t cap) {
+		uint32_t *counters, uint32_t cap, const uint2 *__restrict__ wdec) {
 	// cap = primitive count: bounds the node array, the leaf order and each queue
 	const uint32_t n_items = min(*n_items_ptr, cap);
 	for (uint32_t it = blockIdx.x * blockDim.x + threadIdx.x; it < n_items; it += gridDim.x * blockDim.x) {
@@ -400,6 +492,38 @@ __global__ void __launch_bounds__(128) k_collapse(const uint2 *__restrict__ item
 			cref[0] = item.x;
 			load_ref_box(item.x, sorted, plo, phi, bn_lo, bn_hi, cb[0]);
 			cnt = 1;
+		} else if (wdec) {
+			// the SAH-optimal cover of the subtree by at most `width` roots
+			// (k_wide_cost's decisions); each split divides a slot budget j
+			// into k and j - k, so the roots never exceed `width`
+			uint32_t st_ref[8], st_j[8];
+			int sp = 0;
+			cnt = 0;
+			const uint32_t k0 = wdec[item.x].x & 0xffu;
+			st_ref[sp] = bchild[2 * item.x + 1];
+			st_j[sp++] = width - k0;
+			st_ref[sp] = bchild[2 * item.x];
+			st_j[sp++] = k0;
+			while (sp > 0 && cnt < 8) {
+				--sp;
+				const uint32_t r = st_ref[sp], j = st_j[sp];
+				uint32_t k = 0;
+				if (!(r & kLeafFlag) && j >= 2 && j <= 8) {
+					const uint2 d = wdec[r];
+					k = ((j <= 4 ? d.x : d.y) >> (8 * ((j - 1) & 3))) & 0xffu;
+				}
+				if (k == 0 || k >= j || sp + 2 > 8) {  // r is one root
+					cref[cnt] = r;
+					load_ref_box(r, sorted, plo, phi, bn_lo, bn_hi, cb[cnt]);
+					++cnt;
+				} else {
+					st_ref[sp] = bchild[2 * r + 1];
+					st_j[sp++] = j - k;
+					st_ref[sp] = bchild[2 * r];
+					st_j[sp++] = k;
+				}
+			}
+			if (sp > 0 || k0 == 0 || k0 >= width) atomicOr(&counters[C_ERR], 64u);  // never: a cover lost a subtree
 		} else {
 			cref[0] = bchild[2 * item.x];
 			cref[1] = bchild[2 * item.x + 1];
@@ -668,6 +792,21 @@ lrx_status build_wide_bvh(uint32_t n, const float4 *d_lo, const float4 *d_hi, ui
 		LRX_CUDA(cudaGetLastError());
 	}
 
+	// Which binary nodes become wide nodes (the SAH-optimal cover, above);
+	// its tables live only for the collapse
+	DevBuf wtab;
+	const uint2 *wdec = nullptr;
+	if (n > 1) {
+		if ((rc = wtab.alloc((sizeof(float4) * 2 + sizeof(uint2)) * (size_t)ni)) != LRX_OK) return rc;
+		float4 *wcost = wtab.as<float4>();
+		uint2 *dec = reinterpret_cast<uint2 *>(wcost + 2 * (size_t)ni);
+		LRX_CUDA(cudaMemsetAsync(S.other_bound.ptr, 0, sizeof(uint32_t) * ni, st));  // visit counters
+		k_wide_cost<<<blocks_for(n, 128), 128, 0, st>>>(n, sorted, d_lo, d_hi, bchild, bn_lo, bn_hi, bmeta, lparent,
+				S.other_bound.as<uint32_t>(), leaf_max, node_width, wcost, dec);
+		LRX_CUDA(cudaGetLastError());
+		wdec = dec;
+	}
+
 	// Level-synchronous collapse
 	k_init_collapse<<<1, 1, 0, st>>>(S.queue_a.as<uint2>(), counters);
 	LRX_CUDA(cudaGetLastError());
@@ -693,7 +832,7 @@ lrx_status build_wide_bvh(uint32_t n, const float4 *d_lo, const float4 *d_hi, ui
 		LRX_CUDA(cudaMemsetAsync(counters + cout, 0, sizeof(uint32_t), st));
 		k_collapse<<<std::min(blocks_for(n_in, 128), 152u * 16u), 128, 0, st>>>(qin, counters + cin, qout,
 				counters + cout, bchild, bn_lo, bn_hi, bmeta, sorted, d_lo, d_hi, leaf_max, node_width,
-				S.wide_nodes.as<WideNode>(), S.prim_order.as<uint32_t>(), counters, n);
+				S.wide_nodes.as<WideNode>(), S.prim_order.as<uint32_t>(), counters, n, wdec);
 		LRX_CUDA(cudaGetLastError());
 		std::swap(qin, qout);
 		std::swap(cin, cout);
