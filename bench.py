@@ -175,7 +175,7 @@ def load_peaks():
 # the rays of the launch; the capture's command and table are in
 # profiles/trace_heightfield_ncu.md).  A constant of that capture, not a
 # figure of this run: the line says so in roofline.traffic_source.
-TRAFFIC_PER_RAY = {"primary": 154.1, "bounce": 297.3, "shadow": 198.2}
+TRAFFIC_PER_RAY = {"primary": 147.4, "bounce": 274.7, "shadow": 194.8}
 TRAFFIC_SOURCE = ("ncu capture of the traversal launches of one step (profiles/trace_heightfield_ncu.md), "
                   "not this run; DRAM bytes per launch averaged over the three sets")
 
