@@ -1004,8 +1004,9 @@ def run_batching(args):
 
 
 def batching_line(args, steps: int) -> dict:
-    """BASELINE config 4 (uneven batches over 8 scenes): one lrx_trace per
-    RayBuffer against one lrx_trace_batches call, eager and as replayed CUDA
+    """The uneven-batch workload (512 batches of log-uniform size over 8
+    random-triangle scenes): one lrx_trace per RayBuffer against one
+    lrx_trace_batches call, eager and as replayed CUDA
     graphs, each timed over `steps` repetitions with the same autotuned
     per-scene configs (plus the plain form under the library defaults)."""
     import torch
@@ -1239,7 +1240,7 @@ def wavefront_pools(torch, descs, extents, pool_n, device, seed):
 
 
 def serving_line(args, rates, seconds: float, budget_runs: bool) -> dict:
-    """BASELINE config 5: 64 sessions over 12 scenes with Poisson arrivals at
+    """The serving workload: 64 sessions over 12 scenes with Poisson arrivals at
     each rate in `rates`, `seconds` each, batched (continuous batching) and
     plain servers; with budget_runs also a scaled HBM budget that forces
     evictions (with and without the blob cache).  Rays: the bounce and shadow
