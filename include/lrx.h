@@ -207,9 +207,11 @@ typedef struct lrx_host_batch {
 
 /* lrx_trace_host over several batches whose copies and traces overlap: the
  * batches are cut into chunks of at most 1,048,576 rays, and each chunk is
- * copied in, traced (its scene's lrx_trace path) and copied out on a side
- * stream (up to 4, round robin, forked from `stream`), so one chunk's copies
- * run while another is traced.  Returns once every hit is in host memory
+ * copied in, traced (its scene's lrx_trace path, except that a configuration
+ * with LRX_VARIANT_SORT_RAYS runs persistent warps on the chunk instead: the
+ * chunks are traced side by side, and a sort of each gains less than it
+ * costs) and copied out on a side stream (up to 4, round robin, forked from
+ * `stream`), so one chunk's copies run while another is traced.  Returns once every hit is in host memory
  * (`stream` synchronised).  Page-locked host buffers let the copies run
  * asynchronously.  Masked rays keep the caller's hit contents: a mapped
  * (page-locked) hit buffer is not copied in -- only its masked slots are

@@ -406,7 +406,7 @@ lrx_status lrx_trace_host_batches(const lrx_host_batch *batches, uint32_t n_batc
 						if (!mapped) LRX_CUDA(cudaMemcpyAsync(d_hits, hh, hb, cudaMemcpyHostToDevice, s_in));
 						LRX_CUDA(cudaEventRecord(in_done, s_in));
 						LRX_CUDA(cudaStreamWaitEvent(s_tr, in_done, 0));
-						lrx_status t = trace_common(b.scene, d_rays, d_hits, n, b.mode, nullptr, s_tr);
+						lrx_status t = trace_common(b.scene, d_rays, d_hits, n, b.mode, nullptr, s_tr, nullptr, true);
 						if (t == LRX_OK && mapped)
 							t = launch_restore_masked_hits(d_rays, n, static_cast<const lrx_hit *>(mapped_hits) + c0,
 									d_hits, s_tr);

@@ -117,8 +117,10 @@ uint32_t scene_blas_visits(const lrx_scene *s);
 // One trace launch of `count` rays with the scene's configuration for `mode`,
 // validating every argument (the body of lrx_trace and lrx_trace_counted).
 // `fixed`, when given, is the scratch of sorted and compacted launches
-// instead of the stream-ordered pool.
+// instead of the stream-ordered pool.  `pipeline_chunk`: a chunk of the
+// host-buffer pipeline, traced beside others -- a configuration that sorts
+// rays takes persistent warps instead (refill 8 unless set).
 lrx_status trace_common(lrx_scene *s, const void *d_rays, void *d_hits, uint32_t count, uint32_t mode,
-		uint64_t *d_counters, cudaStream_t st, const FixedScratch *fixed = nullptr);
+		uint64_t *d_counters, cudaStream_t st, const FixedScratch *fixed = nullptr, bool pipeline_chunk = false);
 
 }  // namespace lrx
