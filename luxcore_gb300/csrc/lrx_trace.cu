@@ -555,14 +555,16 @@ __device__ __forceinline__ bool ray_step(const TraceArgs &a, TravState &s, TravS
 			return false;
 		}
 	} else {
+		// Any-hit never defers: the hit it returns must depend only on the
+		// ray and the tree, not on which rays share its warp.  The decision is
+		// taken once per trip, as the lanes enter the triangle stage (taking it
+		// again every iteration deferred a group in mid-loop too rarely to pay
+		// for the test: bounce rays -0.7 %).
+		if (!ANY && !sparse && s.tg.y && s.ng.y > 0x00ffffffu && __popc(__activemask()) < a.postpone) {
+			LRX_PUSH(s.tg);  // test later, when the warp does triangles together
+			s.tg.y = 0;
+		}
 		while (s.tg.y) {
-			// Any-hit never defers: the hit it returns must depend only on the
-			// ray and the tree, not on which rays share its warp.
-			if (!ANY && !sparse && s.ng.y > 0x00ffffffu && __popc(__activemask()) < a.postpone) {
-				LRX_PUSH(s.tg);  // test later, when the warp does triangles together
-				s.tg.y = 0;
-				break;
-			}
 			const uint32_t k = __ffs(s.tg.y) - 1;
 			s.tg.y &= s.tg.y - 1;
 			const float4 *tp = reinterpret_cast<const float4 *>(a.tris + s.tg.x + k);
