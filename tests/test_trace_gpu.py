@@ -284,7 +284,10 @@ def test_host_batches_overlap_and_match_device_traces(torch_cuda):
     jobs = [(sf, frays, lrx.LRX_TRACE_CLOSEST, True), (si, irays, lrx.LRX_TRACE_ANY, False),
             (sf, frays[:0], lrx.LRX_TRACE_CLOSEST, False), (si, irays[:20000], lrx.LRX_TRACE_CLOSEST, True),
             (sf, frays[:33333], lrx.LRX_TRACE_ANY, False),
-            (sf, np.tile(frays, 17)[:1_100_000], lrx.LRX_TRACE_CLOSEST, True)]  # more than one chunk
+            (sf, np.tile(frays, 17)[:1_100_000], lrx.LRX_TRACE_CLOSEST, True),  # more than one chunk
+            # any hit over more than one chunk: the scene's sorted configuration
+            # runs persistent warps on the pipeline's chunks, same hits
+            (sf, np.tile(frays, 17)[:1_200_000], lrx.LRX_TRACE_ANY, True)]
     keep, items, want = [], [], []
     for sc, r, mode, pinned in jobs:
         want.append(gpu_trace(torch, sc, r, mode) if r.shape[0] else None)
