@@ -8,12 +8,44 @@
 #include <stdexcept>
 #include <string>
 
+#include "luxrays/core/context.h"
+#include "luxrays/utils/properties.h"
+
 namespace luxrays {
 
 namespace {
 
 void check(lrx_status st, const char *what) {
 	if (st != LRX_OK) throw std::runtime_error(std::string(what) + ": " + lrx_last_error());
+}
+
+// The tree's build options from the context's configuration, where the
+// reference's accelerators read theirs (BVHAccel::ToBVHParams,
+// src/luxrays/accelerators/bvhaccel.cpp:39-62):
+//   accelerator.gb300.nodewidth      children per wide node, 4-8 (8)
+//   accelerator.gb300.nodelayout     "wide8" (80-byte records) or "compact4"
+//                                    (64-byte records, node width 4, flat scenes)
+//   accelerator.gb300.leafsize       triangles per leaf, 1-3 (3)
+//   accelerator.gb300.treeletpasses  treelet SAH passes (2)
+// accelerator.bvh.treetype describes the reference's CPU tree and is not
+// read: its default (4) is not the shape this engine traverses fastest.
+lrx_build_opts BuildOptions(const Context *ctx) {
+	lrx_build_opts o;
+	std::memset(&o, 0, sizeof(o));
+	o.struct_size = sizeof(o);
+	o.node_width = 8;
+	o.leaf_max = 3;
+	o.treelet_passes = 2;
+	o.node_layout = LRX_NODES_WIDE8;
+	if (!ctx) return o;
+	const Properties &cfg = ctx->GetConfig();
+	o.node_width = (uint32_t)cfg.Get(Property("accelerator.gb300.nodewidth")(8)).Get<int>();
+	o.leaf_max = (uint32_t)cfg.Get(Property("accelerator.gb300.leafsize")(3)).Get<int>();
+	o.treelet_passes = (uint32_t)cfg.Get(Property("accelerator.gb300.treeletpasses")(2)).Get<int>();
+	const std::string layout = cfg.Get(Property("accelerator.gb300.nodelayout")("wide8")).Get<std::string>();
+	if (layout == "compact4") o.node_layout = LRX_NODES_COMPACT4;
+	else if (layout != "wide8") throw std::runtime_error("GB300Accel: unknown accelerator.gb300.nodelayout: " + layout);
+	return o;  // the ranges are checked by lrx_scene_create
 }
 
 }  // namespace
@@ -99,12 +131,13 @@ void GB300Accel::Init(const std::deque<const Mesh *> &ms, const u_longlong, cons
 		lrx_scene_destroy(scene);
 		scene = nullptr;
 	}
+	const lrx_build_opts opts = BuildOptions(ctx);
 	if (motions.empty())
-		check(lrx_scene_create(md.data(), (uint32_t)md.size(), od.data(), (uint32_t)od.size(), nullptr, nullptr, &scene),
+		check(lrx_scene_create(md.data(), (uint32_t)md.size(), od.data(), (uint32_t)od.size(), &opts, nullptr, &scene),
 				"GB300Accel::Init");
 	else
 		check(lrx_scene_create_motion(md.data(), (uint32_t)md.size(), od.data(), (uint32_t)od.size(), motions.data(),
-				(uint32_t)motions.size(), nullptr, nullptr, &scene), "GB300Accel::Init");
+				(uint32_t)motions.size(), &opts, nullptr, &scene), "GB300Accel::Init");
 }
 
 void GB300Accel::Update() {
