@@ -388,7 +388,7 @@ def run_lrx(args):
         scene = lrx.Scene(scene_desc, stream=st, **build_kw)
     build_s = time.perf_counter() - t0
     if args.block_size is not None or args.postpone is not None or args.variant is not None:
-        scene.set_trace_config(args.block_size or 64, 8 if args.postpone is None else args.postpone,
+        scene.set_trace_config(args.block_size or 64, 0 if args.postpone is None else args.postpone,
                                args.variant or 0, refill=args.refill or 0)
     saved_cfg = {m: scene.trace_config(m) for m in (lrx.LRX_TRACE_CLOSEST, lrx.LRX_TRACE_ANY)}
     info = scene.info()

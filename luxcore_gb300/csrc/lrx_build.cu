@@ -481,6 +481,7 @@ __global__ void __launch_bounds__(128) k_collapse(const uint2 *__restrict__ item
 		const uint32_t *__restrict__ sorted, const float4 *__restrict__ plo, const float4 *__restrict__ phi,
 		uint32_t leaf_max, uint32_t width, WideNode *__restrict__ wnodes, uint32_t *__restrict__ prim_order,
 		uint32_t *counters, uint32_t cap, const uint2 *__restrict__ wdec) {
+	// wdec: k_wide_cost's decisions, present whenever the tree has an internal node
 	// cap = primitive count: bounds the node array, the leaf order and each queue
 	const uint32_t n_items = min(*n_items_ptr, cap);
 	for (uint32_t it = blockIdx.x * blockDim.x + threadIdx.x; it < n_items; it += gridDim.x * blockDim.x) {
@@ -492,7 +493,7 @@ __global__ void __launch_bounds__(128) k_collapse(const uint2 *__restrict__ item
 			cref[0] = item.x;
 			load_ref_box(item.x, sorted, plo, phi, bn_lo, bn_hi, cb[0]);
 			cnt = 1;
-		} else if (wdec) {
+		} else {
 			// the SAH-optimal cover of the subtree by at most `width` roots
 			// (k_wide_cost's decisions); each split divides a slot budget j
 			// into k and j - k, so the roots never exceed `width`
@@ -524,32 +525,6 @@ __global__ void __launch_bounds__(128) k_collapse(const uint2 *__restrict__ item
 				}
 			}
 			if (sp > 0 || k0 == 0 || k0 >= width) atomicOr(&counters[C_ERR], 64u);  // never: a cover lost a subtree
-		} else {
-			cref[0] = bchild[2 * item.x];
-			cref[1] = bchild[2 * item.x + 1];
-			load_ref_box(cref[0], sorted, plo, phi, bn_lo, bn_hi, cb[0]);
-			load_ref_box(cref[1], sorted, plo, phi, bn_lo, bn_hi, cb[1]);
-			cnt = 2;
-		}
-		// Greedy: open the largest-area internal child until `width` (<= 8) slots are used.
-		while (cnt < (int)width) {
-			int best = -1;
-			float best_a = -1.f;
-			for (int k = 0; k < cnt; ++k) {
-				if (cref[k] & kLeafFlag) continue;
-				const float a = box_area(cb[k].lo, cb[k].hi);
-				if (a > best_a) {
-					best_a = a;
-					best = k;
-				}
-			}
-			if (best < 0) break;
-			const uint32_t b = cref[best];
-			cref[best] = bchild[2 * b];
-			cref[cnt] = bchild[2 * b + 1];
-			load_ref_box(cref[best], sorted, plo, phi, bn_lo, bn_hi, cb[best]);
-			load_ref_box(cref[cnt], sorted, plo, phi, bn_lo, bn_hi, cb[cnt]);
-			++cnt;
 		}
 		// Child primitive counts and node bounds
 		uint32_t ccount[8];

@@ -507,7 +507,7 @@ class Scene:
         check(load().lrx_scene_get_info(self.handle, ctypes.byref(inf)))
         return inf.as_dict()
 
-    def set_trace_config(self, block_size: int = 64, postpone: int = 8, variant: int = 0, modes: int = 0,
+    def set_trace_config(self, block_size: int = 64, postpone: int = 0, variant: int = 0, modes: int = 0,
                          refill: int = 0, max_visits: int = 0, deadline_us: int = 0):
         """modes: 1 = closest-hit launches, 2 = any-hit launches, 0 = both.
         refill: with LRX_VARIANT_PERSISTENT, idle lanes that trigger a warp's
