@@ -92,7 +92,10 @@ struct lrx_scene {
 	// launch time).  Any-hit batches are reordered by octant + origin first
 	// (+20 % on shadow rays; the sort costs more than it saves on closest-hit
 	// rays, and persistent warps add nothing after it); any hit never defers.
-	lrx_trace_config tcfg[2] = {{sizeof(lrx_trace_config), 64, 0, lrx::kVarPersistent, 1, 8},
+	// Once a closest-hit launch's rays are all claimed, idle lanes take
+	// subtrees of their warp's last rays (the drain split: primary -4.6 %,
+	// bounce -4.0 % launch time on 1 M rays, neutral on 8 M; flat scenes).
+	lrx_trace_config tcfg[2] = {{sizeof(lrx_trace_config), 64, 0, lrx::kVarPersistent | lrx::kVarDrainSplit, 1, 8},
 			{sizeof(lrx_trace_config), 64, 8, lrx::kVarSortRays, 2, 0}};
 	lrx_scene_info info{};
 	lrx::BuildScratch scratch;

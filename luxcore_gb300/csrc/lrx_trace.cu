@@ -707,6 +707,105 @@ uint32_t next_launch_id() {
 	return next.fetch_add(1u);
 }
 
+// Closest-hit order of two hits as ray_step's acceptance keeps them: the
+// smaller t, and at an exact tie the lower (meshIndex, triangleIndex).  A
+// ray with no hit yet holds (maxt, kNull, kNull); every hit ray_step accepts
+// orders below it, and a hit at t == maxt is never accepted.  The order does
+// not depend on the order the hits were found in, so parts of one ray's walk
+// can run on different lanes and their best hits merge to the same answer.
+__device__ __forceinline__ bool hit_key_less(float t, uint32_t mesh, uint32_t tri, float bt, uint32_t bmesh,
+		uint32_t btri) {
+	return t < bt || (t == bt && (mesh < bmesh || (mesh == bmesh && tri < btri)));
+}
+
+// Drain split (persistent fetch, flat closest hit), once the launch's rays
+// are all claimed.  A warp's last rays would otherwise finish one node fetch
+// at a time on a few lanes while the rest idle; here lanes with nothing to do
+// take subtrees of them:
+// - a helper pulls its owner's best hit when that orders below its own, so
+//   it culls with every hit the ray has found so far;
+// - the k-th free lane (lane order) pairs with the k-th working lane that has
+//   stack entries; that lane pops its top entry (a node group, or a deferred
+//   triangle group) and the free lane starts a walk of it with a copy of the
+//   ray and of its best hit (so ties keep their order), as a helper of the
+//   ray's owner -- the owner of the donor, when the donor is itself a helper;
+// - each owner adds its new helpers' lanes to `link` (a helper's `link` is
+//   its owner's lane).
+// Every lane runs every ballot, shuffle and match here (the branches around
+// them are warp-uniform).  A donated entry is walked exactly once, by its
+// taker, so a ray's walk visits what it would have visited alone, less what
+// its shared hits cull.
+template <int SMEM>
+__device__ __forceinline__ void split_drain(TravState &s, TravStack &stack, StackTop top, uint32_t lane, uint32_t rid,
+		bool &helper, bool waiting, uint32_t &link) {
+	constexpr uint32_t kAll = 0xffffffffu;
+	if (__any_sync(kAll, helper)) {
+		const uint32_t src = helper ? link : lane;
+		const float t = __shfl_sync(kAll, s.best_t, src);
+		const float b1 = __shfl_sync(kAll, s.best_b1, src);
+		const float b2 = __shfl_sync(kAll, s.best_b2, src);
+		const uint32_t mesh = __shfl_sync(kAll, s.best_mesh, src);
+		const uint32_t tri = __shfl_sync(kAll, s.best_tri, src);
+		if (helper && hit_key_less(t, mesh, tri, s.best_t, s.best_mesh, s.best_tri)) {
+			s.best_t = t;
+			s.best_b1 = b1;
+			s.best_b2 = b2;
+			s.best_mesh = mesh;
+			s.best_tri = tri;
+		}
+	}
+	const bool isfree = rid == kNull && !helper;
+	const uint32_t freem = __ballot_sync(kAll, isfree);
+	if (freem == 0u) return;
+	const bool working = (rid != kNull && !waiting) || helper;
+	const uint32_t donors = __ballot_sync(kAll, working && s.sp > 0);
+	if (donors == 0u) return;
+	const uint32_t n = min(__popc(freem), __popc(donors));
+	const uint32_t below = (1u << lane) - 1u;
+	const uint32_t kf = __popc(freem & below);
+	const bool take = isfree && kf < n;
+	const bool give = ((donors >> lane) & 1u) && __popc(donors & below) < n;
+	uint32_t src = lane;
+	if (take) {
+		uint32_t m = donors;  // the kf-th donor: drop the kf lowest set bits
+		for (uint32_t j = 0; j < kf; ++j) m &= m - 1u;
+		src = __ffs(m) - 1;
+	}
+	uint2 e = make_uint2(0u, 0u);
+	if (give) e = stack_get<SMEM>(stack, top, --s.sp);
+	e.x = __shfl_sync(kAll, e.x, src);
+	e.y = __shfl_sync(kAll, e.y, src);
+	const uint32_t root = __shfl_sync(kAll, helper ? link : lane, src);
+	// the donor's ray and best hit (a lane that takes nothing reads its own)
+	s.ray.o.x = __shfl_sync(kAll, s.ray.o.x, src);
+	s.ray.o.y = __shfl_sync(kAll, s.ray.o.y, src);
+	s.ray.o.z = __shfl_sync(kAll, s.ray.o.z, src);
+	s.ray.d.x = __shfl_sync(kAll, s.ray.d.x, src);
+	s.ray.d.y = __shfl_sync(kAll, s.ray.d.y, src);
+	s.ray.d.z = __shfl_sync(kAll, s.ray.d.z, src);
+	s.ray.idir.x = __shfl_sync(kAll, s.ray.idir.x, src);
+	s.ray.idir.y = __shfl_sync(kAll, s.ray.idir.y, src);
+	s.ray.idir.z = __shfl_sync(kAll, s.ray.idir.z, src);
+	s.ray.oct = __shfl_sync(kAll, s.ray.oct, src);
+	s.mint = __shfl_sync(kAll, s.mint, src);
+	s.best_t = __shfl_sync(kAll, s.best_t, src);
+	s.best_b1 = __shfl_sync(kAll, s.best_b1, src);
+	s.best_b2 = __shfl_sync(kAll, s.best_b2, src);
+	s.best_mesh = __shfl_sync(kAll, s.best_mesh, src);
+	s.best_tri = __shfl_sync(kAll, s.best_tri, src);
+	if (take) {
+		s.ng = e;
+		s.tg = make_uint2(0u, 0u);
+		s.sp = 0;
+		s.visits = 0;
+		helper = true;
+		link = root;
+	}
+	// an owner's group: itself and the lanes that just became its helpers
+	const uint32_t grp = __match_any_sync(kAll, take ? root : lane);
+	if (rid != kNull) link |= grp & ~(1u << lane);
+}
+
 // ---------------------------------------------------------------------------
 // Persistent single-batch kernel with warp-level ray fetch (after Aila and
 // Laine 2009, "dynamic fetch"): resident warps loop until the batch's ray
@@ -737,6 +836,7 @@ __global__ void __launch_bounds__(kTraceBlock, TWO_LEVEL ? 7 : 8) k_trace_fetch(
 	constexpr int SMEM = smem_stack_depth(CV);
 	constexpr bool MOTION = (CV & kVarMotion) != 0;
 	constexpr bool N4 = (CV & kVarNodes4) != 0;
+	constexpr bool SPLIT = !ANY && !TWO_LEVEL && (CV & kVarDrainSplit) != 0;
 	extern __shared__ uint2 s_stack_top[];  // SMEM entries per thread with a shared-memory stack, else empty
 	const StackTop top{s_stack_top + threadIdx.x, blockDim.x};
 	uint32_t *slot = g_queue[a.launch_id % kQueueSlots];
@@ -748,7 +848,7 @@ __global__ void __launch_bounds__(kTraceBlock, TWO_LEVEL ? 7 : 8) k_trace_fetch(
 	TravState s;
 	TravStack stack;
 	Counts cnt{0, 0, 0, 0};
-	uint32_t rid = kNull;  // ray this lane traces (kNull: idle)
+	uint32_t rid = kNull;  // ray this lane owns (kNull: none)
 	bool drained = false;  // warp-uniform: the counter has passed the batch
 	const uint32_t count = a.count_dev ? min(*a.count_dev, a.count) : a.count;  // rays to claim
 	for (;;) {
@@ -780,11 +880,68 @@ __global__ void __launch_bounds__(kTraceBlock, TWO_LEVEL ? 7 : 8) k_trace_fetch(
 			if (drained) break;
 			continue;  // every lane idle: the next trip claims 32 rays
 		}
+		if (SPLIT && drained) break;  // the warp's last rays: the drain loop below
 		const bool sparse = drained && __popc(busy) < a.postpone;  // warp-uniform
 		if (rid != kNull &&
 				ray_step<ANY, TWO_LEVEL, false, MM3, SMEM, MOTION, N4>(a, s, stack, keep, pol, cnt, top, sparse)) {
 			if (s.sp >= 0) ray_write(a, rid, s, stream);  // an abandoned ray writes nothing
 			rid = kNull;
+		}
+	}
+	if (SPLIT) {
+		// Drain loop (the counter is spent): lanes without a ray help the
+		// warp's remaining rays (split_drain).  A helper lane walks a subtree
+		// of the ray that lane `link` owns; an owner keeps its helpers' lanes
+		// in `link`, and once its own walk is done it waits (`waiting`) for
+		// them before writing; `lost`: some part of its walk was abandoned,
+		// so it writes nothing.  Ends when no lane holds a ray or a subtree.
+		bool helper = false, waiting = false, lost = false;
+		uint32_t link = 0u;
+		for (;;) {
+			split_drain<SMEM>(s, stack, top, lane, rid, helper, waiting, link);
+			const uint32_t busy = __ballot_sync(0xffffffffu, rid != kNull || helper);
+			if (busy == 0u) break;
+			const bool sparse = __popc(busy) < a.postpone;  // warp-uniform
+			const bool fin = ((rid != kNull && !waiting) || helper) &&
+					ray_step<ANY, TWO_LEVEL, false, MM3, SMEM, MOTION, N4>(a, s, stack, keep, pol, cnt, top, sparse);
+			// helpers done this trip hand their best hit to their owners, one at a time
+			for (uint32_t hf = __ballot_sync(0xffffffffu, helper && fin); hf; hf &= hf - 1u) {
+				const uint32_t h = __ffs(hf) - 1;
+				const float t = __shfl_sync(0xffffffffu, s.best_t, h);
+				const float b1 = __shfl_sync(0xffffffffu, s.best_b1, h);
+				const float b2 = __shfl_sync(0xffffffffu, s.best_b2, h);
+				const uint32_t mesh = __shfl_sync(0xffffffffu, s.best_mesh, h);
+				const uint32_t tri = __shfl_sync(0xffffffffu, s.best_tri, h);
+				const uint32_t own = __shfl_sync(0xffffffffu, link, h);
+				const bool hl = __shfl_sync(0xffffffffu, s.sp < 0 ? 1u : 0u, h) != 0u;
+				if (lane == own) {
+					link &= ~(1u << h);
+					lost |= hl;
+					if (hit_key_less(t, mesh, tri, s.best_t, s.best_mesh, s.best_tri)) {
+						s.best_t = t;
+						s.best_b1 = b1;
+						s.best_b2 = b2;
+						s.best_mesh = mesh;
+						s.best_tri = tri;
+					}
+				}
+			}
+			if (helper) {
+				if (fin) {
+					helper = false;
+					link = 0u;
+				}
+			} else if (rid != kNull) {
+				if (fin) {
+					waiting = true;
+					lost |= s.sp < 0;
+				}
+				if (waiting && link == 0u) {
+					if (!lost) ray_write(a, rid, s, stream);  // an abandoned ray writes nothing
+					rid = kNull;
+					waiting = lost = false;
+				}
+			}
 		}
 	}
 	__syncthreads();
@@ -1195,6 +1352,10 @@ lrx_status launch_trace(const TraceArgs &a_in, cudaStream_t st) {
 	 : smem == kVarSmemStack16 ? launch_fetch<A, T, kVarSmemStack16 | N>(a, fbs, st)                        \
 	 : smem ? launch_fetch<A, T, kVarSmemStack | N>(a, fbs, st)                                             \
 		  : (mm3 ? launch_fetch<A, T, kVarMinMax3 | N>(a, fbs, st) : launch_fetch<A, T, N>(a, fbs, st)))
+		// the drain split's builds: flat closest hit, local-memory stack, 2-input min/max
+		const bool split = (a.variant & kVarDrainSplit) && !a.any_hit && !a.two_level;
+		if (split) return a.nodes4 ? launch_fetch<false, false, kVarDrainSplit | kVarNodes4>(a, fbs, st)
+						   : launch_fetch<false, false, kVarDrainSplit>(a, fbs, st);
 		if (a.nodes4) return a.any_hit ? LRX_FETCH(true, false, kVarNodes4) : LRX_FETCH(false, false, kVarNodes4);
 		if (a.any_hit) return a.two_level ? LRX_FETCH(true, true, 0u) : LRX_FETCH(true, false, 0u);
 		return a.two_level ? LRX_FETCH(false, true, 0u) : LRX_FETCH(false, false, 0u);

@@ -37,6 +37,7 @@ LRX_VARIANT_SMEM_STACK = 0x80
 LRX_VARIANT_COMPACT = 0x100
 LRX_VARIANT_SMEM_STACK16 = 0x400
 LRX_VARIANT_SMEM_STACK32 = 0x800
+LRX_VARIANT_DRAIN_SPLIT = 0x2000
 
 STATUS_NAMES = {0: "LRX_OK", 1: "LRX_ERR_INVALID_ARGUMENT", 2: "LRX_ERR_CUDA", 3: "LRX_ERR_OUT_OF_MEMORY",
                 4: "LRX_ERR_BUILD", 5: "LRX_ERR_DEVICE", 6: "LRX_ERR_NOT_SUPPORTED", 7: "LRX_ERR_BUDGET",

@@ -36,7 +36,8 @@ LRX_ERR_DEVICE = 5
 # (block size, postpone, variant, refill): persistent warps, one thread per
 # ray, sorted before tracing
 FORMS = {"persistent": (64, 8, lrx.LRX_VARIANT_PERSISTENT, 8), "thread-per-ray": (64, 8, 0, 0),
-         "sorted": (64, 8, lrx.LRX_VARIANT_SORT_RAYS, 0)}
+         "sorted": (64, 8, lrx.LRX_VARIANT_SORT_RAYS, 0),
+         "drain-split": (64, 0, lrx.LRX_VARIANT_PERSISTENT | lrx.LRX_VARIANT_DRAIN_SPLIT, 8)}
 
 
 @pytest.fixture(scope="module")
@@ -112,7 +113,7 @@ def test_visit_budget_abandons_rays_and_reports(torch_cuda, flat, form, mode):
     scene.close()
 
 
-@pytest.mark.parametrize("form", ["persistent", "thread-per-ray"])
+@pytest.mark.parametrize("form", ["persistent", "thread-per-ray", "drain-split"])
 def test_deadline_stops_starting_rays_and_reports(torch_cuda, form):
     desc = W.SceneDesc([W.heightfield_mesh(512, W.BASE_SEED + 1)])
     rays = W.random_rays(1 << 21, 302)

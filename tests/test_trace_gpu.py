@@ -27,7 +27,8 @@ KERNEL_CONFIGS = [(128, 0, 0), (64, 8, 0), (256, 24, 0), (64, 8, 0xF), (128, 8, 
                   (64, 8, 0x10), (32, 8, 0x1F), (64, 8, 0x30),
                   (64, 8, 0x40), (128, 0, 0x41, 1), (32, 8, 0x46, 32),
                   (64, 8, 0x50, 8), (64, 8, 0xC0, 8), (256, 8, 0x80), (64, 8, 0x90),
-                  (64, 8, 0x140, 8), (64, 8, 0x440, 8), (128, 8, 0x840, 8), (64, 8, 0x410), (128, 0, 0x800)]
+                  (64, 8, 0x140, 8), (64, 8, 0x440, 8), (128, 8, 0x840, 8), (64, 8, 0x410), (128, 0, 0x800),
+                  (64, 0, 0x2040, 8), (128, 8, 0x2046, 1)]
 KERNELS = pytest.mark.parametrize("kernel", KERNEL_CONFIGS,
                                   ids=["b128", "b64-p8", "b256-p24", "b64-p8-allvariants", "b128-p8-mm3-hints",
                                        "b64-p8-sorted", "b32-p8-sorted-all", "b64-p8-octsort",
@@ -36,7 +37,8 @@ KERNELS = pytest.mark.parametrize("kernel", KERNEL_CONFIGS,
                                        "b64-p8-persistent-smemstack", "b256-p8-smemstack", "b64-p8-sorted-smemstack",
                                        "b64-p8-persistent-compact", "b64-p8-persistent-smemstack16",
                                        "b128-p8-persistent-smemstack32", "b64-p8-sorted-smemstack16",
-                                       "b128-smemstack32"])
+                                       "b128-smemstack32", "b64-persistent-drainsplit",
+                                       "b128-p8-persistent-drainsplit-hints-refill1"])
 
 
 def make_scene(desc, kernel=(64, 8, 0), **kw):
@@ -339,6 +341,44 @@ def test_deterministic_and_batch_independent(torch_cuda, kernel):
         assert np.array_equal(a.view(np.uint8), b.view(np.uint8)), mode
 
 
+@pytest.mark.parametrize("layout", ["wide8", "compact4"])
+def test_drain_split_hits_identical_to_the_plain_persistent_launch(torch_cuda, layout):
+    """The drain split moves parts of a ray's walk to other lanes and merges
+    their best hits; the merge order is the acceptance order itself, so every
+    hit is bit-identical to the walk on one lane.  524,288 rays on the 512x512
+    heightfield: about 3 rays per resident lane, so most of the launch is
+    drain and most rays get helpers."""
+    desc = W.SceneDesc([W.heightfield_mesh(512, W.BASE_SEED + 1)])
+    kw = {} if layout == "wide8" else {"node_width": 4, "node_layout": lrx.LRX_NODES_COMPACT4, "leaf_max": 2}
+    s = lrx.Scene(desc, **kw)
+    prim = W.pinhole_rays(512, 512)
+    s.set_trace_config(64, 0, lrx.LRX_VARIANT_PERSISTENT, modes=1, refill=8)
+    ph = gpu_trace(torch_cuda, s, prim)
+    sets = [prim, W.bounce_rays(desc, prim, ph, 1 << 19, 91), W.random_rays(1 << 19, 92)]
+    for rays in sets:
+        s.set_trace_config(64, 0, lrx.LRX_VARIANT_PERSISTENT, modes=1, refill=8)
+        plain = gpu_trace(torch_cuda, s, rays)
+        for pp, rf in ((0, 8), (8, 1), (24, 32)):
+            s.set_trace_config(64, pp, lrx.LRX_VARIANT_PERSISTENT | lrx.LRX_VARIANT_DRAIN_SPLIT, modes=1, refill=rf)
+            split = gpu_trace(torch_cuda, s, rays)
+            assert np.array_equal(split.view(np.uint8), plain.view(np.uint8)), (pp, rf)
+    # against the oracle on a stride sample of the bounce set
+    oracle = po.OracleScene(desc)
+    sample = sets[1][::8]
+    ref, _ = oracle.intersect(sample)
+    s.set_trace_config(64, 0, lrx.LRX_VARIANT_PERSISTENT | lrx.LRX_VARIANT_DRAIN_SPLIT, modes=1, refill=8)
+    st = assert_parity(gpu_trace(torch_cuda, s, sets[1])[::8], ref, oracle, sample, min_hit_rate=0.05)
+    assert st["bitexact_t"] == 1.0
+    s.close()
+
+
+def test_default_closest_config_is_the_drain_split(torch_cuda):
+    s = lrx.Scene(W.SceneDesc([W.heightfield_mesh(16, 3)]))
+    cfg = s.trace_config(lrx.LRX_TRACE_CLOSEST)
+    assert cfg["variant"] == lrx.LRX_VARIANT_PERSISTENT | lrx.LRX_VARIANT_DRAIN_SPLIT, cfg
+    s.close()
+
+
 def test_instance_update_matches_rebuilt_oracle(torch_cuda):
     scene, closest, _ = W.config3(n_rays=20000, n_meshes=2, freq=8, n_inst=64, extent=2.0, scale=(0.1, 0.3))
     s = lrx.Scene(scene)
@@ -408,7 +448,9 @@ def test_trace_config_struct_versions(torch_cuda):
                 lrx.TraceConfig(24, 64, 8, 0x40, 0, 33), lrx.TraceConfig(24, 48, 8, 0, 0, 0),
                 # a 32-entry shared-memory stack takes 256 B a thread: at most 128 threads a block
                 lrx.TraceConfig(24, 256, 8, lrx.LRX_VARIANT_SMEM_STACK32, 0, 0),
-                lrx.TraceConfig(24, 512, 8, lrx.LRX_VARIANT_SMEM_STACK16, 0, 0)]:
+                lrx.TraceConfig(24, 512, 8, lrx.LRX_VARIANT_SMEM_STACK16, 0, 0),
+                # the library's internal build bits (motion, 64-byte records) are not variants
+                lrx.TraceConfig(24, 64, 8, 0x200, 0, 0), lrx.TraceConfig(24, 64, 8, 0x1000, 0, 0)]:
         assert L.lrx_scene_set_trace_config(s.handle, ctypes.byref(bad)) == lrx.LRX_ERR_INVALID_ARGUMENT
 
 
