@@ -175,7 +175,7 @@ def load_peaks():
 # the rays of the launch; the capture's command and table are in
 # profiles/trace_heightfield_ncu.md).  A constant of that capture, not a
 # figure of this run: the line says so in roofline.traffic_source.
-TRAFFIC_PER_RAY = {"primary": 147.4, "bounce": 274.7, "shadow": 194.8}
+TRAFFIC_PER_RAY = {"primary": 146.6, "bounce": 271.5, "shadow": 194.5}
 TRAFFIC_SOURCE = ("ncu capture of the traversal launches of one step (profiles/trace_heightfield_ncu.md), "
                   "not this run; DRAM bytes per launch averaged over the three sets")
 
