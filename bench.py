@@ -676,10 +676,15 @@ def run_lrx(args):
             e2e_s = d.max(time.perf_counter() - t1)
             e2e_windows.append(rays_per_step * nw * ws / e2e_s / 1e6)
         e2e_value = round(float(np.median(e2e_windows)), 3)
-        t1 = time.perf_counter()
-        for _ in range(max(1, args.steps // 10)):
-            e2e_seq_step()
-        e2e_seq_value = round(rays_per_step * max(1, args.steps // 10) / (time.perf_counter() - t1) / 1e6, 3)
+        # the sequential form likewise: the median of three windows
+        seq_windows = []
+        n_seq = max(1, args.steps // 30)
+        for _ in range(3):
+            t1 = time.perf_counter()
+            for _ in range(n_seq):
+                e2e_seq_step()
+            seq_windows.append(rays_per_step * n_seq / (time.perf_counter() - t1) / 1e6)
+        e2e_seq_value = round(float(np.median(seq_windows)), 3)
     # lrx_trace_host copies rays and hits in (masked rays keep the caller's
     # hits); lrx_trace_host_batches copies only the rays of pinned buffers
     # (the hit buffer's masked slots -- none here -- are read back directly)
