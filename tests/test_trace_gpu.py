@@ -678,12 +678,16 @@ def test_compaction_skips_masked_rays(torch_cuda, masked_frac):
     rays["flags"][rng.random(rays.shape[0]) < masked_frac] = W.RAY_FLAGS_MASKED
     plain = make_scene(scene, (64, 8, lrx.LRX_VARIANT_PERSISTENT, 8))
     comp = make_scene(scene, (64, 8, lrx.LRX_VARIANT_PERSISTENT | lrx.LRX_VARIANT_COMPACT, 8))
+    # the drain split on the compacted list (device-side count, index indirection)
+    comp_split = make_scene(scene, (64, 0, lrx.LRX_VARIANT_PERSISTENT | lrx.LRX_VARIANT_COMPACT
+                                    | lrx.LRX_VARIANT_DRAIN_SPLIT, 8))
     for mode in (lrx.LRX_TRACE_CLOSEST, lrx.LRX_TRACE_ANY):
         a = gpu_trace(torch, plain, rays, mode)
-        b = gpu_trace(torch, comp, rays, mode)
-        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
         masked = (rays["flags"] & W.RAY_FLAGS_MASKED) != 0
-        assert (b.view(np.uint32).reshape(-1, 5)[masked] == SENT).all()
+        for c in (comp, comp_split):
+            b = gpu_trace(torch, c, rays, mode)
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+            assert (b.view(np.uint32).reshape(-1, 5)[masked] == SENT).all()
 
 
 def test_scene_blob_round_trip(torch_cuda):
