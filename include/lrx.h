@@ -266,11 +266,12 @@ typedef struct lrx_trace_config {
                                           (ABI 3; blocks <= 256) */
 #define LRX_VARIANT_SMEM_STACK32 0x800u /* the top 32 entries in shared memory (ABI 3; blocks <= 128);
                                           with either, deeper entries stay in local memory */
-#define LRX_VARIANT_DRAIN_SPLIT 0x2000u /* with PERSISTENT, closest hit on a flat scene: once the
-                                          launch's rays are all claimed, a warp's idle lanes take
-                                          pending subtrees of its remaining rays and merge their
-                                          hits back (results unchanged; the stack stays in local
-                                          memory and MINMAX3 is not used; ABI 4) */
+#define LRX_VARIANT_DRAIN_SPLIT 0x2000u /* with PERSISTENT, closest hit (not on scenes with
+                                          motion instances): once the launch's rays are all
+                                          claimed, a warp's idle lanes take pending subtrees of
+                                          its remaining rays and merge their hits back (results
+                                          unchanged; the stack stays in local memory and MINMAX3
+                                          is not used; ABI 4) */
 
 /* Sets / reads the launch configuration lrx_trace uses for this scene.
  * No reference counterpart (the reference fixes 32-thread blocks,
@@ -282,9 +283,8 @@ lrx_status lrx_scene_get_trace_config(const lrx_scene *scene, lrx_trace_config *
  * launch configuration -- block size {32, 64, 128} x postpone {0, 8} x
  * variant {none, streaming ray access, ray sort, persistent (refill 8),
  * persistent + streaming, persistent + shared-memory stack top, persistent +
- * L2-resident scene}, and for closest hit on flat scenes the persistent
- * shapes with a local-memory stack also with the drain split -- keeps the
- * fastest for
+ * L2-resident scene}, and for closest hit the persistent shapes with a
+ * local-memory stack also with the drain split -- keeps the fastest for
  * `mode` in the scene and returns it in `chosen` (nullable).  Synchronises
  * `stream`; do not trace the same scene from other threads meanwhile.
  * No reference counterpart (the reference fixes its launch shape). */

@@ -843,9 +843,9 @@ lrx_status lrx_scene_autotune(lrx_scene *s, const void *d_rays, uint32_t count, 
 			LRX_VARIANT_PERSISTENT | LRX_VARIANT_STREAM_RAYS, LRX_VARIANT_PERSISTENT | LRX_VARIANT_SMEM_STACK,
 			LRX_VARIANT_PERSISTENT | LRX_VARIANT_SMEM_STACK16, LRX_VARIANT_PERSISTENT | LRX_VARIANT_SMEM_STACK32,
 			LRX_VARIANT_SORT_RAYS | LRX_VARIANT_SMEM_STACK16, LRX_VARIANT_PERSISTENT | LRX_VARIANT_SCENE_L2_KEEP};
-	// closest hit on a flat scene: the persistent shapes also with the drain
-	// split (its builds keep the stack in local memory)
-	const bool try_split = m == 0 && !s->two_level;
+	// closest hit: the persistent shapes also with the drain split (its builds
+	// keep the stack in local memory)
+	const bool try_split = m == 0;
 	for (uint32_t bs : kBlocks) {
 		for (uint32_t pp : kPostpone) {
 			for (uint32_t v = 0; v < 2 * (sizeof(kVariants) / sizeof(kVariants[0])); ++v) {

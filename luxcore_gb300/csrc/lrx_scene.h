@@ -94,7 +94,7 @@ struct lrx_scene {
 	// rays, and persistent warps add nothing after it); any hit never defers.
 	// Once a closest-hit launch's rays are all claimed, idle lanes take
 	// subtrees of their warp's last rays (the drain split: primary -4.6 %,
-	// bounce -4.0 % launch time on 1 M rays, neutral on 8 M; flat scenes).
+	// bounce -4.0 % launch time on 1 M rays, neutral on 8 M).
 	lrx_trace_config tcfg[2] = {{sizeof(lrx_trace_config), 64, 0, lrx::kVarPersistent | lrx::kVarDrainSplit, 1, 8},
 			{sizeof(lrx_trace_config), 64, 8, lrx::kVarSortRays, 2, 0}};
 	lrx_scene_info info{};

@@ -718,7 +718,7 @@ __device__ __forceinline__ bool hit_key_less(float t, uint32_t mesh, uint32_t tr
 	return t < bt || (t == bt && (mesh < bmesh || (mesh == bmesh && tri < btri)));
 }
 
-// Drain split (persistent fetch, flat closest hit), once the launch's rays
+// Drain split (persistent fetch, closest hit), once the launch's rays
 // are all claimed.  A warp's last rays would otherwise finish one node fetch
 // at a time on a few lanes while the rest idle; here lanes with nothing to do
 // take subtrees of them:
@@ -731,11 +731,17 @@ __device__ __forceinline__ bool hit_key_less(float t, uint32_t mesh, uint32_t tr
 //   ray's owner -- the owner of the donor, when the donor is itself a helper;
 // - each owner adds its new helpers' lanes to `link` (a helper's `link` is
 //   its owner's lane).
+// Two-level scenes: a lane inside an instance's BLAS gives only entries of
+// that BLAS (above its `inst_sp`), with the instance-space ray and the
+// instance's object, and its taker walks them as a BLAS of its own (inst_sp
+// 0: its walk ends where that BLAS is exhausted); a lane at top level gives
+// TLAS entries with the world ray.  Either way the world ray and the ray's
+// time go along, for the instances a TLAS walk enters.
 // Every lane runs every ballot, shuffle and match here (the branches around
 // them are warp-uniform).  A donated entry is walked exactly once, by its
 // taker, so a ray's walk visits what it would have visited alone, less what
 // its shared hits cull.
-template <int SMEM>
+template <int SMEM, bool TWO_LEVEL>
 __device__ __forceinline__ void split_drain(TravState &s, TravStack &stack, StackTop top, uint32_t lane, uint32_t rid,
 		bool &helper, bool waiting, uint32_t &link) {
 	constexpr uint32_t kAll = 0xffffffffu;
@@ -758,7 +764,7 @@ __device__ __forceinline__ void split_drain(TravState &s, TravStack &stack, Stac
 	const uint32_t freem = __ballot_sync(kAll, isfree);
 	if (freem == 0u) return;
 	const bool working = (rid != kNull && !waiting) || helper;
-	const uint32_t donors = __ballot_sync(kAll, working && s.sp > 0);
+	const uint32_t donors = __ballot_sync(kAll, working && s.sp > (TWO_LEVEL ? max(s.inst_sp, 0) : 0));
 	if (donors == 0u) return;
 	const uint32_t n = min(__popc(freem), __popc(donors));
 	const uint32_t below = (1u << lane) - 1u;
@@ -793,11 +799,24 @@ __device__ __forceinline__ void split_drain(TravState &s, TravStack &stack, Stac
 	s.best_b2 = __shfl_sync(kAll, s.best_b2, src);
 	s.best_mesh = __shfl_sync(kAll, s.best_mesh, src);
 	s.best_tri = __shfl_sync(kAll, s.best_tri, src);
+	bool blas = false;
+	if (TWO_LEVEL) {
+		s.wo.x = __shfl_sync(kAll, s.wo.x, src);
+		s.wo.y = __shfl_sync(kAll, s.wo.y, src);
+		s.wo.z = __shfl_sync(kAll, s.wo.z, src);
+		s.wd.x = __shfl_sync(kAll, s.wd.x, src);
+		s.wd.y = __shfl_sync(kAll, s.wd.y, src);
+		s.wd.z = __shfl_sync(kAll, s.wd.z, src);
+		s.time = __shfl_sync(kAll, s.time, src);
+		s.inst_obj = __shfl_sync(kAll, s.inst_obj, src);
+		blas = __shfl_sync(kAll, s.inst_sp >= 0 ? 1u : 0u, src) != 0u;
+	}
 	if (take) {
 		s.ng = e;
 		s.tg = make_uint2(0u, 0u);
 		s.sp = 0;
 		s.visits = 0;
+		if (TWO_LEVEL) s.inst_sp = blas ? 0 : -1;  // (inst_obj: the donor's, kNull at top level)
 		helper = true;
 		link = root;
 	}
@@ -836,7 +855,7 @@ __global__ void __launch_bounds__(kTraceBlock, TWO_LEVEL ? 7 : 8) k_trace_fetch(
 	constexpr int SMEM = smem_stack_depth(CV);
 	constexpr bool MOTION = (CV & kVarMotion) != 0;
 	constexpr bool N4 = (CV & kVarNodes4) != 0;
-	constexpr bool SPLIT = !ANY && !TWO_LEVEL && (CV & kVarDrainSplit) != 0;
+	constexpr bool SPLIT = !ANY && (CV & kVarDrainSplit) != 0;
 	extern __shared__ uint2 s_stack_top[];  // SMEM entries per thread with a shared-memory stack, else empty
 	const StackTop top{s_stack_top + threadIdx.x, blockDim.x};
 	uint32_t *slot = g_queue[a.launch_id % kQueueSlots];
@@ -898,7 +917,7 @@ __global__ void __launch_bounds__(kTraceBlock, TWO_LEVEL ? 7 : 8) k_trace_fetch(
 		bool helper = false, waiting = false, lost = false;
 		uint32_t link = 0u;
 		for (;;) {
-			split_drain<SMEM>(s, stack, top, lane, rid, helper, waiting, link);
+			split_drain<SMEM, TWO_LEVEL>(s, stack, top, lane, rid, helper, waiting, link);
 			const uint32_t busy = __ballot_sync(0xffffffffu, rid != kNull || helper);
 			if (busy == 0u) break;
 			const bool sparse = __popc(busy) < a.postpone;  // warp-uniform
@@ -1325,6 +1344,7 @@ lrx_status launch_trace(const TraceArgs &a_in, cudaStream_t st) {
 	if (a.motion && a.two_level) {
 		// motion scenes: builds of their own (no MINMAX3 / SMEM_STACK / occupancy
 		// forms), so the static builds carry no motion code
+		// (no drain split: its motion build spills, and closest hit lost 1-2 %)
 		if ((a.variant & kVarPersistent) && !cnt && a.count <= kMaxFetchRays) {
 			const uint32_t fbs = std::min(bs, kTraceBlock);
 			return a.any_hit ? launch_fetch<true, true, kVarMotion>(a, fbs, st)
@@ -1352,10 +1372,11 @@ lrx_status launch_trace(const TraceArgs &a_in, cudaStream_t st) {
 	 : smem == kVarSmemStack16 ? launch_fetch<A, T, kVarSmemStack16 | N>(a, fbs, st)                        \
 	 : smem ? launch_fetch<A, T, kVarSmemStack | N>(a, fbs, st)                                             \
 		  : (mm3 ? launch_fetch<A, T, kVarMinMax3 | N>(a, fbs, st) : launch_fetch<A, T, N>(a, fbs, st)))
-		// the drain split's builds: flat closest hit, local-memory stack, 2-input min/max
-		const bool split = (a.variant & kVarDrainSplit) && !a.any_hit && !a.two_level;
+		// the drain split's builds: closest hit, local-memory stack, 2-input min/max
+		const bool split = (a.variant & kVarDrainSplit) && !a.any_hit;
 		if (split) return a.nodes4 ? launch_fetch<false, false, kVarDrainSplit | kVarNodes4>(a, fbs, st)
-						   : launch_fetch<false, false, kVarDrainSplit>(a, fbs, st);
+						   : a.two_level ? launch_fetch<false, true, kVarDrainSplit>(a, fbs, st)
+										 : launch_fetch<false, false, kVarDrainSplit>(a, fbs, st);
 		if (a.nodes4) return a.any_hit ? LRX_FETCH(true, false, kVarNodes4) : LRX_FETCH(false, false, kVarNodes4);
 		if (a.any_hit) return a.two_level ? LRX_FETCH(true, true, 0u) : LRX_FETCH(true, false, 0u);
 		return a.two_level ? LRX_FETCH(false, true, 0u) : LRX_FETCH(false, false, 0u);

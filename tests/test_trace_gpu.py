@@ -372,6 +372,34 @@ def test_drain_split_hits_identical_to_the_plain_persistent_launch(torch_cuda, l
     s.close()
 
 
+@pytest.mark.parametrize("kind", ["instanced", "motion"])
+def test_drain_split_on_two_level_scenes(torch_cuda, kind):
+    """Two-level scenes: helpers take BLAS entries (instance-space ray and
+    object) or TLAS entries (world ray); hits stay bit-identical to the plain
+    persistent launch.  Motion scenes ignore the bit (the plain loop runs).
+    262,144 rays, about two per resident lane."""
+    torch = torch_cuda
+    if kind == "instanced":
+        desc, closest, _ = W.config3(n_rays=1 << 18, n_meshes=4, freq=12, n_inst=300, extent=3.0, scale=(0.1, 0.4))
+    else:
+        desc, closest, _ = W.config_motion(n_rays=1 << 18, n_meshes=4, freq=12, n_inst=300, extent=3.0,
+                                           scale=(0.1, 0.4))
+    s = lrx.Scene(desc)
+    s.set_trace_config(64, 0, lrx.LRX_VARIANT_PERSISTENT, modes=1, refill=8)
+    plain = gpu_trace(torch, s, closest)
+    for pp, rf in ((0, 8), (8, 1)):
+        s.set_trace_config(64, pp, lrx.LRX_VARIANT_PERSISTENT | lrx.LRX_VARIANT_DRAIN_SPLIT, modes=1, refill=rf)
+        split = gpu_trace(torch, s, closest)
+        assert np.array_equal(split.view(np.uint8), plain.view(np.uint8)), (pp, rf)
+    if kind == "instanced":  # (motion against the oracle, within its tolerance: test_motion_gpu.py)
+        oracle = po.OracleScene(desc)
+        sample = closest[::16]
+        ref, _ = oracle.intersect(sample)
+        st = assert_parity(split[::16], ref, oracle, sample, min_hit_rate=0.05)
+        assert st["bitexact_t"] == 1.0
+    s.close()
+
+
 def test_default_closest_config_is_the_drain_split(torch_cuda):
     s = lrx.Scene(W.SceneDesc([W.heightfield_mesh(16, 3)]))
     cfg = s.trace_config(lrx.LRX_TRACE_CLOSEST)
