@@ -844,6 +844,14 @@ __device__ __forceinline__ void split_drain(TravState &s, TravStack &stack, Stac
 // has passed, the warp still claims rays (so the counter runs out as
 // before) but starts none of them -- their hits are not written and the
 // status word records it -- while rays already started finish their walks.
+// Drain loop (split builds), after the counter is spent: no rays are
+// claimed any more, and each trip steps every lane that holds a walk (its
+// own ray or a helper's subtree).  A walk finishes in a bounded number of
+// trips, a donation moves a stack entry to a lane that then walks it, so the
+// entries to walk only shrink; an owner whose walk is done waits only for
+// its helpers' walks, each of which ends and clears its bit.  The loop ends
+// when no lane holds a walk (a warp-uniform ballot), and every shuffle,
+// ballot and match in it is executed by all 32 lanes.
 // ---------------------------------------------------------------------------
 
 // Two-level builds carry the world ray and instance state on top of the
