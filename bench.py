@@ -1297,7 +1297,7 @@ def serving_line(args, rates, seconds: float, budget_runs: bool) -> dict:
         sess = g.integers(0, n_sess, t.size)
         return list(zip(t.tolist(), sess.tolist(), sizes.tolist()))
 
-    def one_run(policy, budget, rate, cache=True):
+    def one_run(policy, budget, rate, cache=True, seed=W.BASE_SEED + 77):
         server = lrx.Server(policy=policy, budget_bytes=budget, streams=args.serve_streams,
                             host_cache_bytes=0 if cache else 2 ** 64 - 1)
         ids = [server.add_scene(d) for d in descs]
@@ -1306,7 +1306,7 @@ def serving_line(args, rates, seconds: float, budget_runs: bool) -> dict:
                 c, _ = pools[k]
                 server.wait(server.submit(ids[k], c.data_ptr(), hits[0][0].data_ptr(), 1024, lrx.LRX_TRACE_CLOSEST))
         server.reset_stats()
-        sched = schedule(rate, seconds, W.BASE_SEED + 77)
+        sched = schedule(rate, seconds, seed)
         step = [0] * n_sess
         inflight = [[None] * k_buf for _ in range(n_sess)]
         deferred = 0
@@ -1354,6 +1354,17 @@ def serving_line(args, rates, seconds: float, budget_runs: bool) -> dict:
     for rate in rates:
         res[f"batched@{rate}"] = one_run(lrx.LRX_SERVE_BATCHED, full, rate)
         res[f"plain@{rate}"] = one_run(lrx.LRX_SERVE_PLAIN, full, rate)
+    # the first rate is above what the GPU serves: its backlog, and so p50 and
+    # p99, move from run to run (the same schedule gave p99/p50 from 2.3 to
+    # 4.7), so the batched server is run there twice more, on other Poisson
+    # schedules, and the line also gives the median ratio of the three runs
+    head_rate = rates[0]
+    repeats = [res[f"batched@{head_rate}"]]
+    for k in (1, 2):
+        r = one_run(lrx.LRX_SERVE_BATCHED, full, head_rate, seed=W.BASE_SEED + 77 + k)
+        res[f"batched@{head_rate}-schedule{k + 1}"] = r
+        repeats.append(r)
+    ratios = [round(v["p99_us"] / max(v["p50_us"], 1e-9), 2) for v in repeats]
     # scaled budget: ~40 % of the scene bytes, so scenes are evicted and rebuilt
     probe_total, probe_max = 0, 0
     for d in descs:
@@ -1383,6 +1394,7 @@ def serving_line(args, rates, seconds: float, budget_runs: bool) -> dict:
                    "scene_bytes_total_GB": round(probe_total / 2 ** 30, 3), "budgets_GB": [150, round(small / 2 ** 30, 3)],
                    "runs": res,
                    "p99_over_p50": {k: round(v["p99_us"] / max(v["p50_us"], 1e-9), 2) for k, v in res.items()},
+                   f"batched@{head_rate}_p99_over_p50_median_of_3_schedules": float(np.median(ratios)),
                    "batched_over_plain_Mrays": {f"@{r}": round(res[f"batched@{r}"]["Mrays_per_s"] /
                                                                max(res[f"plain@{r}"]["Mrays_per_s"], 1e-9), 3)
                                                 for r in rates}},
