@@ -739,8 +739,10 @@ __device__ __forceinline__ bool hit_key_less(float t, uint32_t mesh, uint32_t tr
 // time go along, for the instances a TLAS walk enters.
 // Every lane runs every ballot, shuffle and match here (the branches around
 // them are warp-uniform).  A donated entry is walked exactly once, by its
-// taker, so a ray's walk visits what it would have visited alone, less what
-// its shared hits cull.
+// taker.  The pieces may visit nodes the one-lane walk would have culled (a
+// helper learns of its owner's hits a trip late), but a lane culls only with
+// the t of a hit the ray has, so no piece skips the triangle of the ray's
+// best hit, and the merged answer is the one-lane answer.
 template <int SMEM, bool TWO_LEVEL>
 __device__ __forceinline__ void split_drain(TravState &s, TravStack &stack, StackTop top, uint32_t lane, uint32_t rid,
 		bool &helper, bool waiting, uint32_t &link) {
