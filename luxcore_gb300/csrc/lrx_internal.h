@@ -148,7 +148,7 @@ constexpr uint32_t kVarMotion = 0x200u;    // internal build bit: instance entry
 constexpr uint32_t kVarSmemStack16 = 0x400u;  // the top 16 stack entries in shared memory
 constexpr uint32_t kVarSmemStack32 = 0x800u;  // the top 32 stack entries in shared memory
 constexpr uint32_t kVarNodes4 = 0x1000u;   // internal build bit: the scene's nodes are 64-byte records
-constexpr uint32_t kVarDrainSplit = 0x2000u;  // with kVarPersistent, flat closest hit: idle lanes take subtrees at the drain
+constexpr uint32_t kVarDrainSplit = 0x2000u;  // with kVarPersistent, closest hit (no motion): idle lanes take subtrees at the drain
 constexpr uint32_t kVarAll = 0x2dffu;      // every public variant bit
 // The shared-memory stack bit of a variant (the deepest one asked for), or 0.
 constexpr uint32_t smem_stack_bits(uint32_t v) {
