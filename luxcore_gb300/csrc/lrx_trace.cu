@@ -728,7 +728,9 @@ __device__ __forceinline__ bool hit_key_less(float t, uint32_t mesh, uint32_t tr
 //   stack entries; that lane pops its top entry (a node group, or a deferred
 //   triangle group) and the free lane starts a walk of it with a copy of the
 //   ray and of its best hit (so ties keep their order), as a helper of the
-//   ray's owner -- the owner of the donor, when the donor is itself a helper;
+//   ray's owner -- the owner of the donor, when the donor is itself a helper.
+//   The copy includes b1 and b2: a helper's best may be a hit its owner has
+//   not seen yet, and the taker may hand it over first;
 // - each owner adds its new helpers' lanes to `link` (a helper's `link` is
 //   its owner's lane).
 // Two-level scenes: a lane inside an instance's BLAS gives only entries of
