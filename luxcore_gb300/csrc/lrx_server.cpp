@@ -248,13 +248,18 @@ bool lrx_server::launch_one(std::unique_lock<std::mutex> &lk) {
 	std::vector<uint32_t> pinned;
 	std::vector<char> drop;
 	// index-based: submitters may append to `pending` while a build runs unlocked
-	for (size_t i = 0; i < pending.size() && take.size() < max_req; ++i) {
+	// oldest first, until max_requests_per_launch requests or max_rays_per_launch
+	// rays (at least one request)
+	uint64_t take_rays = 0;
+	for (size_t i = 0; i < pending.size() && take.size() < max_req &&
+			(take.empty() || take_rays < opts.max_rays_per_launch); ++i) {
 		drop.resize(pending.size(), 0);
 		const uint32_t sid = pending[i].scene;
 		const lrx_status rc = make_resident(lk, sid, pinned);
 		drop.resize(pending.size(), 0);
 		if (rc == LRX_OK) {
 			take.push_back(pending[i]);
+			take_rays += pending[i].count;
 			if (std::find(pinned.begin(), pinned.end(), sid) == pinned.end()) pinned.push_back(sid);
 			drop[i] = 1;
 		} else if (rc == LRX_ERR_BUSY) {
@@ -409,14 +414,20 @@ lrx_status lrx_server_create(const lrx_server_opts *opts, lrx_server **out) {
 		s->opts.streams = 4;
 		s->opts.max_requests_per_launch = 384;
 		s->opts.host_cache_bytes = 16ull << 30;
+		s->opts.max_rays_per_launch = 8ull << 20;
 		if (opts) {
 			if (opts->struct_size < offsetof(lrx_server_opts, host_cache_bytes) || opts->policy > LRX_SERVE_PLAIN ||
 					opts->streams > 64) {
 				lrx::set_error("lrx_server_create: bad options");
 				return LRX_ERR_INVALID_ARGUMENT;
 			}
-			if (opts->struct_size >= sizeof(lrx_server_opts) && opts->host_cache_bytes)
+			// fields past the caller's struct keep their defaults
+			if (opts->struct_size >= offsetof(lrx_server_opts, host_cache_bytes) + sizeof(uint64_t) &&
+					opts->host_cache_bytes)
 				s->opts.host_cache_bytes = opts->host_cache_bytes;
+			if (opts->struct_size >= offsetof(lrx_server_opts, max_rays_per_launch) + sizeof(uint64_t) &&
+					opts->max_rays_per_launch)
+				s->opts.max_rays_per_launch = opts->max_rays_per_launch;
 			s->opts.policy = opts->policy;
 			s->opts.budget_bytes = opts->budget_bytes;
 			if (opts->streams) s->opts.streams = opts->streams;

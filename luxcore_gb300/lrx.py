@@ -264,7 +264,7 @@ def trace_batches(batches, stream: int = 0, d_tile_counters: int = 0, d_done_fla
 class ServerOpts(ctypes.Structure):
     _fields_ = [("struct_size", ctypes.c_uint32), ("policy", ctypes.c_uint32), ("budget_bytes", ctypes.c_uint64),
                 ("streams", ctypes.c_uint32), ("max_requests_per_launch", ctypes.c_uint32),
-                ("host_cache_bytes", ctypes.c_uint64)]
+                ("host_cache_bytes", ctypes.c_uint64), ("max_rays_per_launch", ctypes.c_uint64)]
 
 
 class ServerStats(ctypes.Structure):
@@ -301,11 +301,13 @@ class Server:
     launch per request (LRX_SERVE_PLAIN)."""
 
     def __init__(self, policy: int = LRX_SERVE_BATCHED, budget_bytes: int = 0, streams: int = 0,
-                 max_requests_per_launch: int = 0, host_cache_bytes: int = 0):
+                 max_requests_per_launch: int = 0, host_cache_bytes: int = 0, max_rays_per_launch: int = 0):
         """host_cache_bytes: blobs of evicted scenes (0 = library default,
-        2**64 - 1 = no cache)."""
+        2**64 - 1 = no cache).  max_rays_per_launch: rays a batched launch
+        takes before it stops admitting requests (0 = library default,
+        2**64 - 1 = no cap)."""
         o = ServerOpts(ctypes.sizeof(ServerOpts), policy, budget_bytes, streams, max_requests_per_launch,
-                       host_cache_bytes)
+                       host_cache_bytes, max_rays_per_launch)
         h = ctypes.c_void_p()
         check(load().lrx_server_create(ctypes.byref(o), ctypes.byref(h)))
         self.handle = h

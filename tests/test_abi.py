@@ -46,6 +46,7 @@ def test_struct_layouts():
     assert ctypes.sizeof(lrx.BuildOpts) == 20  # ABI 4: + node_layout
     assert ctypes.sizeof(lrx.SceneInfo) == 64
     assert ctypes.sizeof(lrx.TraceConfig) == 32  # ABI 3: + max_visits, deadline_us
+    assert ctypes.sizeof(lrx.ServerOpts) == 40  # ABI 4: + max_rays_per_launch
 
 
 def test_variant_constants_match_the_header():

@@ -145,6 +145,30 @@ def test_budget_smaller_than_a_scene_fails_the_request(torch_cuda):
     server.close()
 
 
+def test_launch_ray_cap_gives_each_larger_request_a_launch(torch_cuda):
+    """max_rays_per_launch: a batched launch stops admitting requests once
+    their rays reach the cap, so requests of more rays than the cap get one
+    launch each, however they queue; their hits are those of lone traces."""
+    torch = torch_cuda
+    descs = scene_set()[:1]
+    reqs = []
+    for k in range(12):
+        rays = W.random_rays(4096, 7700 + k)
+        reqs.append((0, torch.from_numpy(rays.view(np.uint8).reshape(-1).copy()).cuda(),
+                     torch.zeros(4096 * 20, dtype=torch.uint8, device="cuda"), 4096,
+                     lrx.LRX_TRACE_CLOSEST if k % 2 == 0 else lrx.LRX_TRACE_ANY))
+    ref = alone_results(torch, descs, reqs)
+    server = lrx.Server(max_rays_per_launch=1000)
+    ids = [server.add_scene(d) for d in descs]
+    server.reset_stats()
+    got = serve_all(server, ids, reqs)
+    st = server.stats()
+    server.close()
+    assert st["launches"] == len(reqs) and st["requests_done"] == len(reqs), st
+    for a, b in zip(got, ref):
+        assert np.array_equal(a, b)
+
+
 def test_concurrent_sessions(torch_cuda):
     torch = torch_cuda
     descs = scene_set()
