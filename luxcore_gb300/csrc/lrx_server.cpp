@@ -5,10 +5,11 @@
 //
 // Threads: callers submit and wait from any thread; one worker thread per
 // server owns every CUDA call.  The worker (1) reaps finished launches by
-// polling their completion events, (2) when a stream is free, takes every
-// pending request it can admit -- making its scene resident first, evicting
-// least-recently-used idle scenes while the budget is exceeded -- and
-// launches them together through the queue kernel (or, under the plain
+// polling their completion events, (2) when a stream is free, takes the
+// pending requests it can admit, oldest first, up to max_requests_per_launch
+// requests or max_rays_per_launch rays -- making each scene resident first,
+// evicting least-recently-used idle scenes while the budget is exceeded --
+// and launches them together through the queue kernel (or, under the plain
 // policy, one lrx_trace per request on a single stream), and (3) sleeps on a
 // condition variable when there is nothing to do.
 #include <algorithm>
