@@ -375,7 +375,7 @@ typedef struct lrx_server_opts {
 	                              ABI 1 struct is accepted and gets the default */
 	uint64_t max_rays_per_launch; /* batched policy: a launch takes pending requests (oldest first)
 	                              until their rays reach this many; a single larger request still
-	                              gets a launch of its own (0 = 8,388,608; UINT64_MAX = no cap).
+	                              gets a launch of its own (0 = 2,097,152; UINT64_MAX = no cap).
 	                              Bounds the work queued ahead of a launch's last request when
 	                              requests arrive faster than they are served.  Added in ABI 4:
 	                              the 32-byte struct of ABI 2-3 is accepted and gets the default */

@@ -415,7 +415,7 @@ lrx_status lrx_server_create(const lrx_server_opts *opts, lrx_server **out) {
 		s->opts.streams = 4;
 		s->opts.max_requests_per_launch = 384;
 		s->opts.host_cache_bytes = 16ull << 30;
-		s->opts.max_rays_per_launch = 8ull << 20;
+		s->opts.max_rays_per_launch = 2ull << 20;
 		if (opts) {
 			if (opts->struct_size < offsetof(lrx_server_opts, host_cache_bytes) || opts->policy > LRX_SERVE_PLAIN ||
 					opts->streams > 64) {
