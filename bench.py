@@ -939,9 +939,11 @@ def run_pathocl(args):
         scene = lrx.Scene(desc, stream=st)
     iters = 8
     forms = {}
-    for form, variant in (("persistent", lrx.LRX_VARIANT_PERSISTENT),
-                          ("persistent+compact", lrx.LRX_VARIANT_PERSISTENT | lrx.LRX_VARIANT_COMPACT)):
-        scene.set_trace_config(64, 8, variant, modes=1, refill=8)
+    default = scene.trace_config(lrx.LRX_TRACE_CLOSEST)  # the library's closest-hit default
+    for form, (pp, variant) in (("default", (default["postpone"], default["variant"])),
+                                ("default+compact", (default["postpone"], default["variant"] | lrx.LRX_VARIANT_COMPACT)),
+                                ("persistent, no drain split", (8, lrx.LRX_VARIANT_PERSISTENT))):
+        scene.set_trace_config(default["block_size"], pp, variant, modes=1, refill=default["refill"] or 8)
         with torch.cuda.stream(stream):
             wf = pathocl.WavefrontPaths(scene, desc, 1024, 1024, max_depth=4, stream=stream)
             wf.iterate(args.warmup * iters)
@@ -972,7 +974,7 @@ def run_pathocl(args):
                        "ms_per_iteration": round(loop_ms / (args.steps * iters), 4),
                        "trace_ms_per_iteration": round(trace_ms / (args.steps * iters), 4), "clocks": clk}
         del wf
-    best = forms["persistent"]
+    best = forms["default"]
     line = {
         "metric": "Mrays/s traced in a PATHOCL-style wavefront loop (trace + AdvancePaths stand-in on the device)",
         "value": best["loop_Mrays"], "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
