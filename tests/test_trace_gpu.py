@@ -308,6 +308,36 @@ def test_host_batches_overlap_and_match_device_traces(torch_cuda):
         assert np.array_equal(got.view(np.uint8), w.view(np.uint8))
 
 
+CHUNK = 393216  # the host pipeline's chunk (rays)
+
+
+@pytest.mark.parametrize("n", [CHUNK - 1, CHUNK, CHUNK + 1, 2 * CHUNK, 2 * CHUNK + 7])
+def test_host_batches_at_chunk_boundaries(torch_cuda, n):
+    """Batches just below, at and just above one and two host-pipeline
+    chunks, closest and any hit, pinned and pageable, through
+    lrx_trace_host_batches and lrx_trace_host: the device trace's hits, and
+    masked slots untouched."""
+    torch = torch_cuda
+    flat, frays = W.config1(n_tris=20000, n_rays=70000, seed=64)
+    rays = np.tile(frays, n // frays.shape[0] + 1)[:n].copy()
+    rays["flags"][::13] = W.RAY_FLAGS_MASKED
+    sc = lrx.Scene(flat)
+    for mode in (lrx.LRX_TRACE_CLOSEST, lrx.LRX_TRACE_ANY):
+        want = gpu_trace(torch, sc, rays, mode)
+        for pinned in (True, False):
+            hr = torch.from_numpy(rays.view(np.uint8).reshape(-1).copy())
+            hh = torch.empty(n * 20, dtype=torch.uint8)
+            if pinned:
+                hr, hh = hr.pin_memory(), hh.pin_memory()
+            hh.view(torch.int32).fill_(np.int32(np.uint32(SENT).view(np.int32)).item())
+            lrx.trace_host_batches([(sc, hr.data_ptr(), hh.data_ptr(), n, mode)])
+            got = hh.numpy().view(W.HIT_DTYPE)
+            assert np.array_equal(got.view(np.uint8), want.view(np.uint8)), (mode, pinned)
+        got = sc.trace_host(rays, hits=np.full(n * 5, SENT, dtype=np.uint32).view(W.HIT_DTYPE), mode=mode)
+        assert np.array_equal(got.view(np.uint8), want.view(np.uint8)), mode
+    sc.close()
+
+
 @pytest.mark.parametrize("mode", [lrx.LRX_TRACE_CLOSEST, lrx.LRX_TRACE_ANY])
 def test_host_entry_point_on_pinned_buffers(torch_cuda, mode):
     """lrx_trace_host on pinned host buffers: the same hits as device
