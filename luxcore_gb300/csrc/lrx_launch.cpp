@@ -226,10 +226,16 @@ lrx_status lrx_trace_batches_ex(const lrx_batch *batches, uint32_t n_batches, vo
 	// side stream.
 	SideStreams *side = nullptr;
 	auto trace_all = [&]() -> lrx_status {
+		// largest first: the longest launch starts first, and the others fill in
+		// beside it (the heightfield step 1.7261 against 1.7310 ms)
 		uint32_t n_direct = 0;
-		for (uint32_t k = 0; k < n_batches; ++k) {
+		std::vector<uint32_t> direct;
+		for (uint32_t k = 0; k < n_batches; ++k)
+			if (direct_batch(batches[k], big_direct)) direct.push_back(k);
+		std::stable_sort(direct.begin(), direct.end(),
+				[&](uint32_t x, uint32_t y) { return batches[x].count > batches[y].count; });
+		for (uint32_t k : direct) {
 			const lrx_batch &b = batches[k];
-			if (!direct_batch(b, big_direct)) continue;
 			if (!side) {
 				lrx_status rc = side_streams(dev, &side);
 				if (rc != LRX_OK) return rc;
