@@ -206,7 +206,7 @@ typedef struct lrx_host_batch {
 } lrx_host_batch;
 
 /* lrx_trace_host over several batches whose copies and traces overlap: the
- * batches are cut into chunks of at most 393,216 rays, and each chunk is
+ * batches, largest first, are cut into chunks of at most 393,216 rays, and each chunk is
  * copied in, traced (its scene's lrx_trace path, except that a configuration
  * with LRX_VARIANT_SORT_RAYS runs persistent warps on the chunk instead: the
  * chunks are traced side by side, and a sort of each gains less than it
