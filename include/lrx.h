@@ -189,7 +189,7 @@ lrx_status lrx_trace(lrx_scene *scene, const void *d_rays, void *d_hits,
 /* Same as lrx_trace for rays and hits in HOST memory: copies the rays in,
  * traces, copies the hits out and synchronises `stream`.  Staging buffers
  * are allocated on first use and kept by the scene.  Batches of more than
- * 393,216 rays go through lrx_trace_host_batches (chunks whose copies
+ * 524,288 rays go through lrx_trace_host_batches (chunks whose copies
  * overlap each other's traces).
  * Replaces: the serial IntersectionDevice::TraceRay loop
  * (include/luxrays/core/intersectiondevice.h:65-68) for batches. */
@@ -206,7 +206,7 @@ typedef struct lrx_host_batch {
 } lrx_host_batch;
 
 /* lrx_trace_host over several batches whose copies and traces overlap: the
- * batches, largest first, are cut into chunks of at most 393,216 rays, and each chunk is
+ * batches, largest first, are cut into chunks of at most 524,288 rays, and each chunk is
  * copied in, traced (its scene's lrx_trace path, except that a configuration
  * with LRX_VARIANT_SORT_RAYS runs persistent warps on the chunk instead: the
  * chunks are traced side by side, and a sort of each gains less than it

@@ -200,10 +200,11 @@ constexpr uint32_t kMaxFetchRays = 0x7f000000u;
 constexpr uint32_t kDirectBatchRays = 131072;  // lrx_trace_batches: batches this large get launches of their own
 constexpr uint32_t kMaxDirectBatches = 4;      // ... when a call holds at most this many of them
 constexpr uint32_t kSideStreams = 6;           // side streams per thread and device
-// lrx_trace_host_batches: rays per copy-in/trace/copy-out chunk.  384 k rays
-// (18 MB in, 7.5 MB out): on the heightfield step 2,660 Mrays/s end to end,
-// against 2,647 at 512 k, 2,616 at 768 k, 2,476 at 1 M and 2,571 at 256 k.
-constexpr uint32_t kHostChunkRays = 393216u;
+// lrx_trace_host_batches: rays per copy-in/trace/copy-out chunk.  512 k rays
+// (24 MB in, 10 MB out): on the heightfield step, batches largest first,
+// 2,801 Mrays/s end to end, against 2,733 at 384 k, 2,660 at 256 k, 2,640 at
+// 640 k, 2,656 at 768 k and 2,552 at 1 M.
+constexpr uint32_t kHostChunkRays = 524288u;
 struct QueueParams {
 	uint32_t n, total_tiles, slot;  // slot = launch_id % kQueueSlots
 	uint32_t fetch;         // 1: warp-level ray fetch (k_trace_queue_fetch), 0: 64-ray tiles per block

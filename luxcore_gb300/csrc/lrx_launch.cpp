@@ -384,7 +384,7 @@ lrx_status lrx_trace_host_batches(const lrx_host_batch *batches, uint32_t n_batc
 		uint32_t chunk = 0;
 		// largest batch first: its chunks' copies and traces start first, and the
 		// smaller batches' chunks fill in behind them (heightfield step end to end
-		// 2,745 against 2,662 Mrays/s in call order)
+		// with 384 k-ray chunks: 2,745 against 2,662 Mrays/s in call order)
 		std::vector<uint32_t> order(n_batches);
 		for (uint32_t k = 0; k < n_batches; ++k) order[k] = k;
 		std::stable_sort(order.begin(), order.end(),

@@ -308,7 +308,7 @@ def test_host_batches_overlap_and_match_device_traces(torch_cuda):
         assert np.array_equal(got.view(np.uint8), w.view(np.uint8))
 
 
-CHUNK = 393216  # the host pipeline's chunk (rays)
+CHUNK = 524288  # the host pipeline's chunk (rays)
 
 
 @pytest.mark.parametrize("n", [CHUNK - 1, CHUNK, CHUNK + 1, 2 * CHUNK, 2 * CHUNK + 7])
